@@ -1,0 +1,403 @@
+"""Benchmark of the GB300 descale executor on the Delanczos YUV420P16 workload.
+
+Workload (one "step"): Delanczos(taps=3) of 64 YUV420P16 frames
+1920x1080 -> 1440x810 (chroma 960x540 -> 720x405), f64mode=0 (auto: the
+plans are well conditioned, so the Float32 route), padding=1 (repeat), the
+plugin's chroma placement.  Synthetic frames: per plane a seeded uniform
+[0,1] base at the target size, Gaussian blur sigma 1.5, bicubic (b=0,
+c=0.5) upscale to the source size, N(0, 1e-3) noise, limited-range 16-bit
+quantisation.  The 64 frames (398 MB in, 224 MB out) exceed the 129 MB L2,
+so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is Mpix/s of source pixels summed
+over planes with inputs resident in HBM; `e2e` is the same metric through
+the synchronous host-frame C-ABI calls (pinned host planes, copies inside
+the timed region); `roofline` is measured with CUDA events around every
+kernel launch of the timed steps.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "vapoursynth-descalemvc_gb300"))
+
+SRC_W, SRC_H, DST_W, DST_H = 1920, 1080, 1440, 810
+FRAMES = 64
+KERNEL = dict(kernel="lanczos", taps=3, b=0.0, c=0.5, blur=1.0, border="repeat", f64_mode=0)
+METRIC = "descale Mpix/s (source pixels, Delanczos YUV420P16 1920x1080->1440x810)"
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def plane_requests(gb):
+    """Luma and chroma (4:2:0, left-aligned chroma placement) requests, as
+    prepare_filter_requests builds them (src/vs_plugin.cpp:656-705)."""
+    cs_w, cs_h = SRC_W >> 1, SRC_H >> 1
+    shift = 0.25 - 0.25 * DST_W / SRC_W
+    return {
+        "luma_h": gb.AxisRequest(SRC_W, DST_W, float(DST_W), 0.0, **KERNEL),
+        "luma_v": gb.AxisRequest(SRC_H, DST_H, float(DST_H), 0.0, **KERNEL),
+        "chroma_h": gb.AxisRequest(cs_w, DST_W >> 1, DST_W * cs_w / SRC_W, shift, **KERNEL),
+        "chroma_v": gb.AxisRequest(cs_h, DST_H >> 1, DST_H * cs_h / SRC_H, 0.0, **KERNEL),
+    }
+
+
+def _upscale_matrix(gb, src, dst):
+    """Forward bicubic (b=0, c=0.5) resampling dst -> src: the descale
+    matrix A of a plan, rebuilt from its A^T CSR."""
+    import scipy.sparse as sp
+    p = gb.AxisPlan(gb.AxisRequest(src, dst, float(dst), 0.0, "bicubic", 3, 0.0, 0.5, 1.0,
+                                   "symmetric", 1), cached=False)
+    at = sp.csr_matrix((p.array("transpose_weights").astype(np.float64),
+                        p.array("transpose_indices"), p.array("transpose_offsets")),
+                       shape=(dst, src))
+    return at.T.tocsr()
+
+
+def make_frames(gb, frames, seed):
+    """Seeded synthetic YUV420P16 frames (see the module docstring)."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    mats = {}
+    out = []
+    for _ in range(frames):
+        planes = []
+        for idx, (sw, sh, dw, dh) in enumerate([(SRC_W, SRC_H, DST_W, DST_H),
+                                                 (SRC_W >> 1, SRC_H >> 1, DST_W >> 1, DST_H >> 1),
+                                                 (SRC_W >> 1, SRC_H >> 1, DST_W >> 1, DST_H >> 1)]):
+            key = (sw, sh, dw, dh)
+            if key not in mats:
+                mats[key] = (_upscale_matrix(gb, sw, dw), _upscale_matrix(gb, sh, dh))
+            ah, av = mats[key]
+            base = gaussian_filter(rng.random((dh, dw)), 1.5)
+            up = av @ (ah @ base.T).T
+            up = up + rng.normal(0.0, 1e-3, up.shape)
+            if idx == 0:
+                q = np.rint(up * 56064.0 + 4096.0)
+            else:
+                q = np.rint((up - 0.5) * 57344.0 + 32768.0)
+            planes.append(np.clip(q, 0, 65535).astype(np.uint16))
+        out.append(planes)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pixels_per_frame():
+    return SRC_W * SRC_H + 2 * (SRC_W >> 1) * (SRC_H >> 1)
+
+
+def cpu_baseline(frames, threads, budget_s=12.0, kind="port"):
+    """The oracle port (or the reference engine built here) on the host
+    cores: whole frames through the scalar 2D route, one frame per thread."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    mod = O
+    if kind == "reference":
+        import reference as R
+        mod = R
+    reqs = {
+        "luma_h": (SRC_W, DST_W, float(DST_W), 0.0), "luma_v": (SRC_H, DST_H, float(DST_H), 0.0),
+        "chroma_h": (SRC_W >> 1, DST_W >> 1, DST_W * (SRC_W >> 1) / SRC_W, 0.25 - 0.25 * DST_W / SRC_W),
+        "chroma_v": (SRC_H >> 1, DST_H >> 1, DST_H * (SRC_H >> 1) / SRC_H, 0.0)}
+    plans = {k: mod.Plan(O.make_request(*v, "lanczos", 3, 0.0, 0.5, 1.0, "repeat", 0))
+             for k, v in reqs.items()}
+    luma = (4096.0, float(np.float32(1) / np.float32(56064)), 56064.0, 4096.0, 65535)
+    chroma = (32768.0, float(np.float32(1) / np.float32(57344)), 57344.0, 32768.0, 65535)
+
+    def one(frame):
+        y, u, v = frame
+        out = []
+        for plane, (h, vv, conv) in zip((y, u, v), [("luma_h", "luma_v", luma),
+                                                    ("chroma_h", "chroma_v", chroma),
+                                                    ("chroma_h", "chroma_v", chroma)]):
+            out.append(mod.inverse_2d(plans[h], plans[vv], plane, conv))
+        return out
+
+    one(frames[0])  # warm-up
+    done, t0 = 0, time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as pool:
+        while time.perf_counter() - t0 < budget_s or done == 0:
+            batch = [frames[(done + i) % len(frames)] for i in range(threads)]
+            list(pool.map(one, batch))
+            done += len(batch)
+    elapsed = time.perf_counter() - t0
+    return {"value": done * pixels_per_frame() / elapsed / 1e6, "unit": "Mpix/s",
+            "cores": threads, "kind": kind,
+            "sample": f"{done} frames (YUV420P16 1920x1080->1440x810, Delanczos taps=3), "
+                      f"{threads} threads x 1 frame, scalar 2D route, {elapsed:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference's own CPU implementation of the path
+    on the host cores (built from its sources when that build is present on
+    this machine, else the oracle port), all host threads."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    kind = "port"
+    try:
+        import reference as R
+        if R.available():
+            kind = "reference"
+    except Exception:
+        pass
+    sys.path.insert(0, os.path.join(REPO, "vapoursynth-descalemvc_gb300"))
+    import dsmvc_gb300 as gb
+    frames = make_frames(gb, 4, 1234)
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, 30.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_baseline(frames, threads, budget_s=0.1, kind=kind)
+    results = [cpu_baseline(frames, threads, budget_s=per_step, kind=kind)
+               for _ in range(args.steps)]
+    value = float(np.mean([r["value"] for r in results]))
+    ms = pixels_per_frame() * FRAMES / (value * 1e6) * 1e3
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": dict(results[-1], value=value),
+            "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config():
+    return {"workload": "Delanczos(taps=3) YUV420P16 1920x1080->1440x810, 64 frames, "
+                        "f64mode=0, padding=1",
+            "frames_per_step": FRAMES, "planes_per_frame": 3,
+            "source_pixels_per_step": pixels_per_frame() * FRAMES,
+            "l2": "inputs (398 MB) larger than L2; no flush", "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import dsmvc_gb300 as gb
+    torch.cuda.set_device(local)
+    ex = gb.Executor(local)
+    reqs = plane_requests(gb)
+    plans = {k: gb.AxisPlan(r) for k, r in reqs.items()}
+    for p in plans.values():
+        ex.prepare(p)
+    ex.seal()
+    assert not any(p.requires_float64 for p in plans.values())
+    luma_conv = gb.integer_conversion(16, chroma=False, full_range=False)
+    chroma_conv = gb.integer_conversion(16, chroma=True, full_range=False)
+
+    frames = make_frames(gb, 8, 20250 + rank)  # 8 distinct frames, reused cyclically
+    stream = torch.cuda.Stream()
+    dev_in, dev_out, tasks = [], [], []
+    for f in range(FRAMES):
+        for idx, plane in enumerate(frames[f % len(frames)]):
+            hk, vk, conv = ("luma_h", "luma_v", luma_conv) if idx == 0 else \
+                ("chroma_h", "chroma_v", chroma_conv)
+            h, v = plans[hk], plans[vk]
+            x = torch.from_numpy(plane.view(np.int16)).cuda()
+            y = torch.empty((v.destination_size, h.destination_size), dtype=torch.int16,
+                            device="cuda")
+            dev_in.append(x)
+            dev_out.append(y)
+            tasks.append(gb.PlaneTask(h, v, x.data_ptr(), h.source_size, y.data_ptr(),
+                                      h.destination_size, 2, 0, conv))
+    torch.cuda.synchronize()
+    sid = stream.cuda_stream
+    for _ in range(args.warmup):
+        ex.run_batch(tasks, stream=sid, synchronize=False)
+    torch.cuda.synchronize()
+    launches0 = ex.stats()["launches"]
+    ex.profile(True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                ex.run_batch(tasks, stream=sid, synchronize=False)
+            stop.record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    ex.stream_check(sid)
+    elapsed_ms = start.elapsed_time(stop)
+    ktimes = ex.kernel_times()
+    ex.profile(False)
+    launches = ex.stats()["launches"] - launches0
+    t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed_ms = float(t.item())
+    pix_step = pixels_per_frame() * FRAMES
+    value = world * args.steps * pix_step / (elapsed_ms / 1e3) / 1e6
+
+    # End to end: the synchronous host-frame calls of the C ABI, pinned host
+    # planes, 8 caller threads (the plugin's frame-parallel requests).
+    host_in, host_out, calls = [], [], []
+    for f in range(FRAMES):
+        for idx, plane in enumerate(frames[f % len(frames)]):
+            hk, vk, conv = ("luma_h", "luma_v", luma_conv) if idx == 0 else \
+                ("chroma_h", "chroma_v", chroma_conv)
+            h, v = plans[hk], plans[vk]
+            pin = torch.empty(plane.shape, dtype=torch.int16, pin_memory=True).numpy().view(np.uint16)
+            pin[...] = plane
+            out = torch.empty((v.destination_size, h.destination_size), dtype=torch.int16,
+                              pin_memory=True).numpy().view(np.uint16)
+            host_in.append(pin)
+            host_out.append(out)
+            calls.append((h, v, pin, conv, out))
+    h2d = sum(a.nbytes for a in host_in)
+    d2h = sum(a.nbytes for a in host_out)
+
+    def call(c):
+        ex.inverse_2d(c[0], c[1], c[2], c[3], out=c[4])
+
+    with cf.ThreadPoolExecutor(max_workers=8) as pool:
+        list(pool.map(call, calls))  # warm-up
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            list(pool.map(call, calls))
+        e2e_s = time.perf_counter() - t0
+    e2e = world * args.e2e_steps * pix_step / e2e_s / 1e6
+
+    hbm, peak_kind = peaks()
+    total_ms = sum(k["milliseconds"] for k in ktimes)
+    total_bytes = sum(k["bytes"] for k in ktimes)
+    dominant = max(ktimes, key=lambda k: k["milliseconds"]) if ktimes else None
+    achieved = total_bytes / (total_ms / 1e3) / 1e9 if total_ms else 0.0
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(frames, os.cpu_count() or 1, budget_s=args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(),
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "peak_source": peak_kind,
+                     "kernel": "2D descale (horizontal + vertical passes per step)",
+                     "kernels": [dict(k, share=k["milliseconds"] / total_ms) for k in ktimes],
+                     "dominant": dominant["name"] if dominant else None},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

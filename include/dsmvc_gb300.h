@@ -1,0 +1,241 @@
+/*
+ * dsmvc_gb300: C ABI of the GB300 (sm_103a) descale executor.
+ *
+ * The drop-in boundary for the reference's `backend="cuda"` path.  The
+ * VapourSynth plugin shim, the tests, the benchmark and the request loop all
+ * call these functions.  Plain C types only: no C++ or torch types cross this
+ * boundary.  Every function returns DSMVC_GB_OK (0) or an error code;
+ * dsmvc_gb_last_error() returns the calling thread's last message.  The
+ * reference reports the same conditions as C++ exceptions:
+ *   invalid_argument   -> DSMVC_GB_INVALID_ARGUMENT
+ *   runtime_error      -> DSMVC_GB_RUNTIME_ERROR (incl. Float64 NaN/inf)
+ *   length_error, out_of_range -> DSMVC_GB_LENGTH_ERROR
+ * (src/vs_plugin.cpp:1748-1757 turns them into setFilterError).
+ *
+ * Strides are in samples.  Host buffers may be exactly
+ * (rows - 1) * stride + width samples; row padding beyond the logical width
+ * is never read or written (include/dsmvc/engine.hpp:231-235).
+ */
+#ifndef DSMVC_GB300_H
+#define DSMVC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSMVC_GB_ABI_VERSION 1
+
+enum dsmvc_gb_status {
+    DSMVC_GB_OK = 0,
+    DSMVC_GB_INVALID_ARGUMENT = 1,
+    DSMVC_GB_RUNTIME_ERROR = 2,
+    DSMVC_GB_LENGTH_ERROR = 3,
+    DSMVC_GB_CUDA_ERROR = 4,
+    DSMVC_GB_OUT_OF_MEMORY = 5,
+    DSMVC_GB_UNAVAILABLE = 6
+};
+
+/* KernelKind, BorderMode, F64Mode: include/dsmvc/engine.hpp:16-60. */
+enum dsmvc_gb_kernel_kind {
+    DSMVC_GB_BILINEAR = 0, DSMVC_GB_BICUBIC = 1, DSMVC_GB_LANCZOS = 2,
+    DSMVC_GB_SPLINE16 = 3, DSMVC_GB_SPLINE36 = 4, DSMVC_GB_SPLINE64 = 5,
+    DSMVC_GB_CUSTOM = 6
+};
+enum dsmvc_gb_border {
+    DSMVC_GB_ZERO = 0, DSMVC_GB_REPEAT = 1, DSMVC_GB_REFLECT101 = 2,
+    DSMVC_GB_SYMMETRIC = 3, DSMVC_GB_MIRROR = 4
+};
+enum dsmvc_gb_f64_mode {
+    DSMVC_GB_F64_AUTO = 0, DSMVC_GB_F64_OFF = 1, DSMVC_GB_F64_FORCE = 2
+};
+enum dsmvc_gb_sample {
+    DSMVC_GB_FLOAT32 = 0, DSMVC_GB_UINT8 = 1, DSMVC_GB_UINT16 = 2
+};
+
+/* AxisRequest + KernelSpec (include/dsmvc/engine.hpp:62-76). */
+typedef struct dsmvc_gb_axis_request {
+    int32_t source_size;
+    int32_t destination_size;
+    double active_length;
+    double shift;
+    int32_t kernel;          /* enum dsmvc_gb_kernel_kind */
+    int32_t taps;
+    double b;
+    double c;
+    double blur;
+    int32_t border;          /* enum dsmvc_gb_border */
+    int32_t f64_mode;        /* enum dsmvc_gb_f64_mode */
+} dsmvc_gb_axis_request;
+
+/* IntegerConversion (include/dsmvc/engine.hpp:167-173); 20 bytes like the
+ * reference's IntegerConversionDescriptor (src/cuda/cuda_kernel.hpp:20-26). */
+typedef struct dsmvc_gb_conversion {
+    float input_offset;
+    float input_scale;
+    float output_scale;
+    float output_offset;
+    uint32_t output_maximum;
+} dsmvc_gb_conversion;
+
+/* Read-only summary of a plan (AxisPlan scalars, engine.hpp:82-138). */
+typedef struct dsmvc_gb_plan_info {
+    int32_t source_size;
+    int32_t destination_size;
+    int32_t support;
+    int32_t half_bandwidth;
+    int32_t requires_float64;
+    int32_t max_row_entries;
+    double active_length;
+    double shift;
+    double normal_rcond;
+    double normal_inf_norm;
+    uint64_t nonzeros;
+    uint64_t storage_bytes;
+} dsmvc_gb_plan_info;
+
+typedef struct dsmvc_gb_planner_stats {
+    uint64_t plan_hits;
+    uint64_t plan_builds;
+    uint64_t plan_entries;
+    uint64_t plan_resident_bytes;
+} dsmvc_gb_planner_stats;
+
+typedef struct dsmvc_gb_executor_stats {
+    uint64_t launches;
+    uint64_t plane_tasks;
+    uint64_t plan_uploads;
+    uint64_t device_plan_bytes;
+    uint64_t workspace_bytes;
+} dsmvc_gb_executor_stats;
+
+/* One plane of a device-resident batch.  `horizontal`/`vertical` may be
+ * NULL for a one-axis descale (then `vectors` is the row or column count). */
+typedef struct dsmvc_gb_plan dsmvc_gb_plan;
+typedef struct dsmvc_gb_plane_task {
+    const dsmvc_gb_plan *horizontal;
+    const dsmvc_gb_plan *vertical;
+    const void *input;            /* device pointer */
+    int64_t input_stride;         /* samples */
+    void *output;                 /* device pointer */
+    int64_t output_stride;        /* samples */
+    int32_t sample;               /* enum dsmvc_gb_sample */
+    int32_t vectors;
+    dsmvc_gb_conversion conversion;
+} dsmvc_gb_plane_task;
+
+typedef struct dsmvc_gb_executor dsmvc_gb_executor;
+typedef double (*dsmvc_gb_custom_kernel)(double x, void *user);
+
+/* ---- status --------------------------------------------------------- */
+const char *dsmvc_gb_last_error(void);
+int dsmvc_gb_abi_version(void);
+/* Nonzero when a CUDA device is visible (dsmvc::cuda_available,
+ * include/dsmvc/engine.hpp:204). */
+int dsmvc_gb_cuda_available(void);
+
+/* ---- planner (host, FP64) -------------------------------------------- */
+/* build_axis_plan (include/dsmvc/engine.hpp:175-176,
+ * src/axis_plan.cpp:1351).  `custom` is required for DSMVC_GB_CUSTOM. */
+int dsmvc_gb_plan_build(const dsmvc_gb_axis_request *request,
+                        dsmvc_gb_custom_kernel custom, void *user,
+                        dsmvc_gb_plan **out);
+/* get_or_build_axis_plan (engine.hpp:177-178, src/axis_plan.cpp:1358):
+ * single-flight LRU shared by all callers; custom kernels are not cached. */
+int dsmvc_gb_plan_get_or_build(const dsmvc_gb_axis_request *request,
+                               dsmvc_gb_custom_kernel custom, void *user,
+                               dsmvc_gb_plan **out);
+void dsmvc_gb_plan_release(dsmvc_gb_plan *plan);
+int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out);
+/* Read-only view of one plan array: 0 transpose_offsets (u32),
+ * 1 transpose_indices (i32), 2 transpose_weights (f32), 3 lower_ld (f32),
+ * 4 upper_l (f32), 5 inverse_diagonal (f32), 6 transpose_weights_f64,
+ * 7 normal_bands_f64, 8 ldlt_bands_f64, 9 inverse_diagonal_f64 (f64). */
+int dsmvc_gb_plan_get_array(const dsmvc_gb_plan *plan, int32_t which,
+                            const void **data, uint64_t *count);
+/* FNV-1a plan hashes of tests/numerical_conformance.hpp:193-248. */
+int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan,
+                         const dsmvc_gb_axis_request *request,
+                         uint64_t *f32_hash, uint64_t *complete_hash);
+/* planner_cache_stats / clear_planner_caches (engine.hpp:179-180). */
+int dsmvc_gb_planner_cache_stats(dsmvc_gb_planner_stats *out);
+void dsmvc_gb_clear_planner_caches(void);
+
+/* ---- executor -------------------------------------------------------- */
+/* CudaExecutor() (src/cuda/cuda_executor.hpp:15); device < 0 uses the
+ * current device.  Fails with DSMVC_GB_UNAVAILABLE without a CUDA device:
+ * an explicit CUDA backend never falls back (src/backend.cpp:53-58). */
+int dsmvc_gb_executor_create(int32_t device, dsmvc_gb_executor **out);
+void dsmvc_gb_executor_destroy(dsmvc_gb_executor *executor);
+/* Executor::prepare / seal (engine.hpp:383-385). */
+int dsmvc_gb_prepare(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan);
+int dsmvc_gb_seal(dsmvc_gb_executor *executor);
+int dsmvc_gb_executor_get_stats(dsmvc_gb_executor *executor,
+                                dsmvc_gb_executor_stats *out);
+
+/* Synchronous host-frame calls: Executor::inverse_rows, inverse_columns,
+ * inverse_2d, inverse_2d_u8, inverse_2d_u16 (engine.hpp:452-489,
+ * src/cuda/cuda_executor.hpp:27-52). */
+int dsmvc_gb_inverse_rows(dsmvc_gb_executor *executor,
+                          const dsmvc_gb_plan *plan,
+                          const float *input, int64_t input_stride,
+                          float *output, int64_t output_stride,
+                          int32_t rows);
+int dsmvc_gb_inverse_columns(dsmvc_gb_executor *executor,
+                             const dsmvc_gb_plan *plan,
+                             const float *input, int64_t input_stride,
+                             float *output, int64_t output_stride,
+                             int32_t columns);
+int dsmvc_gb_inverse_2d(dsmvc_gb_executor *executor,
+                        const dsmvc_gb_plan *horizontal,
+                        const dsmvc_gb_plan *vertical,
+                        const float *input, int64_t input_stride,
+                        float *output, int64_t output_stride);
+int dsmvc_gb_inverse_2d_u8(dsmvc_gb_executor *executor,
+                           const dsmvc_gb_plan *horizontal,
+                           const dsmvc_gb_plan *vertical,
+                           const uint8_t *input, int64_t input_stride,
+                           uint8_t *output, int64_t output_stride,
+                           const dsmvc_gb_conversion *conversion);
+int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor,
+                            const dsmvc_gb_plan *horizontal,
+                            const dsmvc_gb_plan *vertical,
+                            const uint16_t *input, int64_t input_stride,
+                            uint16_t *output, int64_t output_stride,
+                            const dsmvc_gb_conversion *conversion);
+
+/* Device-resident batch (replaces the reference's per-plane exported-frame
+ * calls, src/cuda/cuda_executor.hpp:60-76, and its launch layer,
+ * src/cuda/cuda_launch.hpp:11-149): every task is enqueued on `stream`
+ * (a cudaStream_t; NULL = the executor's own stream).  With `synchronize`
+ * nonzero the call waits and reports Float64 non-finite data; otherwise
+ * dsmvc_gb_stream_check() does that after the work completes. */
+int dsmvc_gb_run_batch(dsmvc_gb_executor *executor,
+                       const dsmvc_gb_plane_task *tasks, int32_t count,
+                       void *stream, int32_t synchronize);
+int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream);
+
+/* Kernel timing (the reference's NVTX ranges, src/cuda/nvtx.hpp:11-60, are
+ * replaced by CUDA events): while enabled, every launch is bracketed by
+ * events on its stream; dsmvc_gb_profile_read waits for them and returns one
+ * entry per kernel name with its launch count, summed milliseconds and the
+ * compulsory bytes (first-pass input + last-pass output) of those launches.
+ * Enabling clears earlier records. */
+typedef struct dsmvc_gb_kernel_time {
+    char name[64];
+    uint64_t launches;
+    double milliseconds;
+    uint64_t bytes;
+} dsmvc_gb_kernel_time;
+int dsmvc_gb_profile(dsmvc_gb_executor *executor, int32_t enable);
+int dsmvc_gb_profile_read(dsmvc_gb_executor *executor,
+                          dsmvc_gb_kernel_time *out, int32_t capacity,
+                          int32_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DSMVC_GB300_H */

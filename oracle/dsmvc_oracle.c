@@ -1135,3 +1135,95 @@ int orc_inverse_2d_u16(const orc_plan *h, const orc_plan *v,
 {
     return inverse_2d_integer(h, v, in, is, out, os, conv, 2);
 }
+
+/* ---- Reference CUDA operation order ------------------------------------ */
+
+/* The Float32 arithmetic of the reference CUDA kernels
+ * (src/cuda/dsmvc_cuda.cu:62-148 inverse_axis_ring and :396-466 solve_axis):
+ * the gather is one fmaf chain in CSR order; the forward pass subtracts
+ * lower*y with fmaf in descending distance and multiplies by the inverse
+ * diagonal; the backward pass accumulates upper*x with fmaf (ascending
+ * distance for half-bandwidth 3, descending otherwise) and subtracts the sum
+ * once.  The GB300 kernels that solve each vector sequentially follow the
+ * same order, so this is their bit-exact expectation. */
+void orc_inverse_axis_f32_gpu(const orc_plan *p, const float *in,
+                              ptrdiff_t is, float *out, ptrdiff_t os)
+{
+    const int32_t n = p->destination_size, hb = p->half_bandwidth;
+    const size_t w = (size_t)n;
+    for (int32_t i = 0; i < n; ++i) {
+        float sum = 0.0f;
+        for (uint32_t k = p->transpose_offsets[i]; k < p->transpose_offsets[i + 1]; ++k) {
+            sum = fmaf(p->transpose_weights[k],
+                       in[(ptrdiff_t)p->transpose_indices[k] * is], sum);
+        }
+        for (int32_t d = imin(hb, i); d >= 1; --d) {
+            sum = fmaf(-p->lower_ld[(size_t)(d - 1) * w + (size_t)i],
+                       out[(ptrdiff_t)(i - d) * os], sum);
+        }
+        out[(ptrdiff_t)i * os] = sum * p->inverse_diagonal[i];
+    }
+    for (int32_t i = n - 2; i >= 0; --i) {
+        float sum = 0.0f;
+        const int32_t avail = imin(hb, n - i - 1);
+        if (hb == 3) {
+            for (int32_t d = 1; d <= avail; ++d)
+                sum = fmaf(p->upper_l[(size_t)(d - 1) * w + (size_t)i],
+                           out[(ptrdiff_t)(i + d) * os], sum);
+        } else {
+            for (int32_t d = avail; d >= 1; --d)
+                sum = fmaf(p->upper_l[(size_t)(d - 1) * w + (size_t)i],
+                           out[(ptrdiff_t)(i + d) * os], sum);
+        }
+        out[(ptrdiff_t)i * os] = out[(ptrdiff_t)i * os] - sum;
+    }
+}
+
+/* Float32 2D in that order: every source row (with the integer input
+ * normalisation (v - offset) * scale), then every column of the
+ * intermediate, then the CPU's integer output conversion
+ * (src/cpu_executor.cpp:1919-1939).  kind 0 float, 1 u8, 2 u16. */
+int orc_inverse_2d_gpu_order(const orc_plan *h, const orc_plan *v, int kind,
+                             const void *input, ptrdiff_t is, void *output,
+                             ptrdiff_t os, const orc_conversion *conv)
+{
+    if (!plan_ok(h) || !plan_ok(v) || !input || !output) return ORC_INVALID;
+    const size_t ms = (size_t)h->destination_size;
+    float *mid = malloc((size_t)v->source_size * ms * sizeof(float));
+    float *row = malloc((size_t)h->source_size * sizeof(float));
+    float *col = malloc((size_t)v->destination_size * sizeof(float));
+    if (!mid || !row || !col) { free(mid); free(row); free(col); return ORC_NOMEM; }
+    for (int32_t r = 0; r < v->source_size; ++r) {
+        for (int32_t c = 0; c < h->source_size; ++c) {
+            const ptrdiff_t at = (ptrdiff_t)r * is + c;
+            if (kind == 0) {
+                row[c] = ((const float *)input)[at];
+            } else {
+                const float s = kind == 1 ? (float)((const uint8_t *)input)[at]
+                                          : (float)((const uint16_t *)input)[at];
+                row[c] = (s - conv->input_offset) * conv->input_scale;
+            }
+        }
+        orc_inverse_axis_f32_gpu(h, row, 1, mid + (size_t)r * ms, 1);
+    }
+    for (int32_t c = 0; c < h->destination_size; ++c) {
+        orc_inverse_axis_f32_gpu(v, mid + c, (ptrdiff_t)ms, col, 1);
+        for (int32_t r = 0; r < v->destination_size; ++r) {
+            const ptrdiff_t at = (ptrdiff_t)r * os + c;
+            if (kind == 0) {
+                ((float *)output)[at] = col[r];
+                continue;
+            }
+            const float hi = (float)conv->output_maximum;
+            float s = col[r] * conv->output_scale + conv->output_offset;
+            s = s < 0.0f ? 0.0f : (hi < s ? hi : s);
+            const float q = nearbyintf(s);
+            if (kind == 1) ((uint8_t *)output)[at] = (uint8_t)q;
+            else ((uint16_t *)output)[at] = (uint16_t)q;
+        }
+    }
+    free(mid);
+    free(row);
+    free(col);
+    return ORC_OK;
+}

@@ -110,6 +110,18 @@ void orc_inverse_axis_f64_ordered(const orc_plan *plan, const double *input,
                                   ptrdiff_t input_stride, double *output,
                                   ptrdiff_t output_stride);
 
+/* The reference CUDA kernels' Float32 operation order (fmaf chains,
+ * src/cuda/dsmvc_cuda.cu:62-148), per axis and composed in 2D; kind 0 float,
+ * 1 u8, 2 u16. */
+void orc_inverse_axis_f32_gpu(const orc_plan *plan, const float *input,
+                              ptrdiff_t input_stride, float *output,
+                              ptrdiff_t output_stride);
+int orc_inverse_2d_gpu_order(const orc_plan *horizontal,
+                             const orc_plan *vertical, int kind,
+                             const void *input, ptrdiff_t input_stride,
+                             void *output, ptrdiff_t output_stride,
+                             const orc_conversion *conversion);
+
 /* CpuExecutor(CpuPath::scalar) routes (src/cpu_executor.cpp). Strides are
  * in samples. */
 int orc_inverse_rows(const orc_plan *plan, const float *input,

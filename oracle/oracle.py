@@ -99,6 +99,11 @@ def lib():
                                          C.c_void_p, C.c_ssize_t, C.c_int32]
         L.orc_inverse_2d.argtypes = [P, P, C.c_void_p, C.c_ssize_t,
                                      C.c_void_p, C.c_ssize_t]
+        L.orc_inverse_axis_f32_gpu.argtypes = [P, C.c_void_p, C.c_ssize_t,
+                                               C.c_void_p, C.c_ssize_t]
+        L.orc_inverse_2d_gpu_order.argtypes = [P, P, C.c_int, C.c_void_p, C.c_ssize_t,
+                                               C.c_void_p, C.c_ssize_t,
+                                               C.POINTER(Conversion)]
         for name in ("orc_inverse_2d_u8", "orc_inverse_2d_u16"):
             getattr(L, name).argtypes = [P, P, C.c_void_p, C.c_ssize_t,
                                          C.c_void_p, C.c_ssize_t,
@@ -185,6 +190,13 @@ class Plan:
         lib().orc_inverse_axis_f32_ordered(self._ptr, x.ctypes.data, 1, out.ctypes.data, 1)
         return out
 
+    def inverse_axis_f32_gpu(self, x):
+        """Reference CUDA operation order (fmaf chains)."""
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.empty(self.destination_size, np.float32)
+        lib().orc_inverse_axis_f32_gpu(self._ptr, x.ctypes.data, 1, out.ctypes.data, 1)
+        return out
+
     def inverse_axis_f64(self, x):
         x = np.ascontiguousarray(x, np.float64)
         out = np.empty(self.destination_size, np.float64)
@@ -258,3 +270,26 @@ def inverse_2d_into(h: Plan, v: Plan, x: np.ndarray, out: np.ndarray,
     fn = lib().orc_inverse_2d_u8 if x.dtype == np.uint8 else lib().orc_inverse_2d_u16
     _check(fn(h._ptr, v._ptr, x.ctypes.data, x.shape[1], out.ctypes.data,
               out.shape[1], C.byref(conv)), "inverse_2d_integer")
+
+
+def inverse_2d_gpu_order(h: Plan, v: Plan, x: np.ndarray, conversion=None) -> np.ndarray:
+    """Float32 2D in the reference CUDA kernels' operation order: the exact
+    expectation of the sequential GB300 kernels."""
+    x = np.ascontiguousarray(x)
+    out = np.empty((v.destination_size, h.destination_size), x.dtype)
+    kind = {np.dtype(np.float32): 0, np.dtype(np.uint8): 1, np.dtype(np.uint16): 2}[x.dtype]
+    conv = Conversion(*(conversion or (0.0, 1.0, 1.0, 0.0, 255)))
+    _check(lib().orc_inverse_2d_gpu_order(h._ptr, v._ptr, kind, x.ctypes.data, x.shape[1],
+                                          out.ctypes.data, out.shape[1], C.byref(conv)),
+           "inverse_2d_gpu_order")
+    return out
+
+
+def inverse_rows_gpu_order(plan: Plan, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    return np.stack([plan.inverse_axis_f32_gpu(r) for r in x])
+
+
+def inverse_columns_gpu_order(plan: Plan, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    return np.stack([plan.inverse_axis_f32_gpu(c) for c in x.T]).T.copy()

@@ -1,0 +1,38 @@
+import os
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for sub in ("", "oracle", "vapoursynth-descalemvc_gb300", "tests"):
+    path = os.path.join(REPO, sub)
+    if path not in sys.path:
+        sys.path.insert(0, path)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300)")
+
+
+def _ensure_library():
+    import dsmvc_gb300
+    if not os.path.exists(dsmvc_gb300.LIB_PATH):
+        dsmvc_gb300.build()
+    return dsmvc_gb300
+
+
+@pytest.fixture(scope="session")
+def gb():
+    """The product package with its library loaded."""
+    mod = _ensure_library()
+    mod.lib()
+    return mod
+
+
+@pytest.fixture(scope="session")
+def executor(gb):
+    if not gb.cuda_available():
+        pytest.skip("no CUDA device")
+    ex = gb.Executor(0)
+    yield ex
+    ex.close()

@@ -1,0 +1,209 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle.
+
+Bars (written into each test):
+  * sequential kernels, Float32: bit-exact against the oracle's statement of
+    the reference CUDA operation order (fmaf chains), and within the
+    reference's Float32 tolerance of the CPU scalar route (max-abs 2e-5,
+    mean-abs 1e-6, tests/vs_gpu_concurrency.py:57);
+  * integer output: within 1 code of the CPU scalar route;
+  * Float64 route: equal to the CPU scalar Float64 route (<= 1 float ULP is
+    the contract; the kernels reproduce its operation order exactly).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from common import (F32_MAX_ABS, F32_MEAN_ABS, INT_MAX_CODES, load_golden, make_input,
+                    max_ulp, oracle_request, product_request)
+
+pytestmark = pytest.mark.gpu
+
+
+def plans(gb, executor, req, prepare=True):
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    if prepare:
+        executor.prepare(p)
+    return p, O.Plan(oracle_request(req))
+
+
+def image(rows, cols, seed):
+    rng = np.random.default_rng(seed)
+    return rng.random((rows, cols), dtype=np.float32)
+
+
+HB_CASES = [
+    ("bilinear", (90, 61, 61.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "symmetric", 1)),
+    ("bicubic", (90, 61, 61.0, 0.3, "bicubic", 3, 0, 0.5, 1.0, "reflect101", 1)),
+    ("lanczos3", (90, 61, 60.5, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 1)),
+    ("spline64", (90, 61, 61.0, -0.2, "spline64", 3, 0, 0.5, 1.0, "zero", 1)),
+    ("spline64-blur-hb9", (90, 61, 61.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 1)),
+    ("lanczos6-hb11", (120, 70, 70.0, 0.0, "lanczos", 6, 0, 0.5, 1.0, "mirror", 1)),
+    ("lanczos7-generic-hb13", (120, 70, 70.0, 0.0, "lanczos", 7, 0, 0.5, 1.0, "symmetric", 1)),
+    ("dest-1-hb0", (9, 1, 1.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)),
+]
+
+
+@pytest.mark.parametrize("name,req", HB_CASES, ids=[c[0] for c in HB_CASES])
+def test_rows_and_columns_bit_exact(gb, executor, name, req):
+    p, o = plans(gb, executor, req)
+    x = image(37, p.source_size, 1)
+    got = executor.inverse_rows(p, x)
+    assert np.array_equal(got, O.inverse_rows_gpu_order(o, x))
+    scalar = O.inverse_rows(o, x)
+    assert np.max(np.abs(got - scalar)) <= F32_MAX_ABS * max(1.0, np.max(np.abs(scalar)))
+    xc = image(p.source_size, 29, 2)
+    gotc = executor.inverse_columns(p, xc)
+    assert np.array_equal(gotc, O.inverse_columns_gpu_order(o, xc))
+
+
+CASES_2D = [
+    ("c0-shape-small", (240, 160, 160.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1),
+     (135, 90, 90.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)),
+    ("lanczos3-repeat", (192, 144, 144.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0),
+     (108, 81, 81.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0)),
+    ("mitchell-blur-odd", (161, 107, 106.5, 0.2, "bicubic", 3, 1 / 3, 1 / 3, 1.1, "mirror", 0),
+     (93, 61, 61.0, -0.1, "bicubic", 3, 1 / 3, 1 / 3, 1.1, "mirror", 0)),
+    ("spline36-x-bilinear", (100, 77, 77.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "zero", 0),
+     (64, 49, 49.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "zero", 0)),
+]
+
+
+@pytest.mark.parametrize("name,hq,vq", CASES_2D, ids=[c[0] for c in CASES_2D])
+def test_2d_float32(gb, executor, name, hq, vq):
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = image(v.source_size, h.source_size, 3)
+    got = executor.inverse_2d(h, v, x)
+    assert np.array_equal(got, O.inverse_2d_gpu_order(oh, ov, x))
+    scalar = O.inverse_2d(oh, ov, x)
+    err = np.abs(got.astype(np.float64) - scalar)
+    assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+
+
+@pytest.mark.parametrize("sample", ["u8", "u16"])
+@pytest.mark.parametrize("name,hq,vq", CASES_2D[:3], ids=[c[0] for c in CASES_2D[:3]])
+def test_2d_integer(gb, executor, sample, name, hq, vq):
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = make_input(v.source_size, h.source_size, sample, 11)
+    bits = 8 if sample == "u8" else 16
+    conv = gb.integer_conversion(bits, chroma=False, full_range=False)
+    got = executor.inverse_2d(h, v, x, conv)
+    assert np.array_equal(got, O.inverse_2d_gpu_order(oh, ov, x, conv))
+    scalar = O.inverse_2d(oh, ov, x, conv)
+    assert np.max(np.abs(got.astype(np.int64) - scalar.astype(np.int64))) <= INT_MAX_CODES
+
+
+F64_CASES = [
+    ("forced-both", (97, 67, 67.0, 0.1, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2),
+     (73, 51, 51.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "reflect101", 2)),
+    ("auto-risk-horizontal", (1080, 980, 978.1, 0.95, "lanczos", 2, 0, 0.5, 1.0, "symmetric", 0),
+     (40, 30, 30.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 0)),
+    ("auto-risk-vertical", (40, 30, 30.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "symmetric", 0),
+     (1920, 1734, 1732.0888888888887, 0.9555555555556339, "bilinear", 3, 0, 0.5, 1.0, "symmetric", 0)),
+    ("forced-spline64-blur-hb9", (128, 86, 85.5, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2),
+     (72, 48, 48.0, 0.0, "lanczos", 7, 0, 0.5, 1.0, "symmetric", 2)),
+]
+
+
+@pytest.mark.parametrize("name,hq,vq", F64_CASES, ids=[c[0] for c in F64_CASES])
+def test_2d_float64_route(gb, executor, name, hq, vq):
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    assert h.requires_float64 or v.requires_float64
+    x = image(v.source_size, h.source_size, 5)
+    got = executor.inverse_2d(h, v, x)
+    want = O.inverse_2d(oh, ov, x)
+    assert max_ulp(got, want) <= 0  # contract: <= 1 ULP; the order is reproduced exactly
+    xi = make_input(v.source_size, h.source_size, "u16", 6)
+    conv = gb.integer_conversion(16, chroma=True, full_range=False)
+    goti = executor.inverse_2d(h, v, xi, conv)
+    assert np.array_equal(goti, O.inverse_2d(oh, ov, xi, conv))
+
+
+def test_float64_rows_and_columns(gb, executor):
+    req = (73, 61, 60.5, 0.125, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2)
+    p, o = plans(gb, executor, req)
+    x = image(19, p.source_size, 8)
+    assert max_ulp(executor.inverse_rows(p, x), O.inverse_rows(o, x)) == 0
+    xc = image(p.source_size, 23, 9)
+    assert max_ulp(executor.inverse_columns(p, xc), O.inverse_columns(o, xc)) == 0
+
+
+@pytest.mark.parametrize("case", load_golden("reference_outputs.json")["cases"],
+                         ids=lambda c: c["name"])
+def test_against_reference_engine_outputs(gb, executor, case):
+    h, oh = plans(gb, executor, case["horizontal"])
+    v, ov = plans(gb, executor, case["vertical"])
+    x = make_input(v.source_size, h.source_size, case["sample"], case["seed"])
+    got = executor.inverse_2d(h, v, x, case["conversion"])
+    if h.requires_float64 or v.requires_float64:
+        # The Float64 route reproduces the reference CPU output bit for bit.
+        assert O.output_hash(got.astype(np.float32)) == case["output_hash"]
+    else:
+        want = O.inverse_2d(oh, ov, x, case["conversion"])
+        assert O.output_hash(want.astype(np.float32)) == case["output_hash"]
+        if case["sample"] == "f32":
+            scale = max(1.0, float(np.max(np.abs(want))))
+            assert np.max(np.abs(got - want)) <= F32_MAX_ABS * scale
+        else:
+            assert np.max(np.abs(got.astype(np.int64) - want.astype(np.int64))) <= INT_MAX_CODES
+
+
+def test_strides_and_padding_are_respected(gb, executor):
+    # include/dsmvc/engine.hpp:231-235: row padding is neither read nor written.
+    hq, vq = CASES_2D[0][1], CASES_2D[0][2]
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = image(v.source_size, h.source_size, 12)
+    xin = np.full((v.source_size, h.source_size + 5), np.nan, np.float32)
+    xin[:, :h.source_size] = x
+    out = np.full((v.destination_size, h.destination_size + 3), -777.0, np.float32)
+    executor.inverse_2d(h, v, xin[:, :h.source_size], out=out[:, :h.destination_size])
+    assert np.all(out[:, h.destination_size:] == -777.0)
+    assert np.array_equal(out[:, :h.destination_size], O.inverse_2d_gpu_order(oh, ov, x))
+
+
+def test_unprepared_plans_still_run(gb, executor):
+    req = (50, 40, 40.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)
+    p, o = plans(gb, executor, req, prepare=False)
+    x = image(5, 50, 13)
+    assert np.array_equal(executor.inverse_rows(p, x), O.inverse_rows_gpu_order(o, x))
+
+
+def test_float64_nonfinite_input_raises(gb, executor):
+    req = (40, 30, 30.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2)
+    p, _ = plans(gb, executor, req)
+    x = image(30 + 10, 40, 14)
+    x[3, 7] = np.inf
+    with pytest.raises(gb.DescaleError):
+        executor.inverse_2d(p, p, x[:40, :40])
+    # The executor stays usable after the error.
+    y = executor.inverse_2d(p, p, image(40, 40, 15))
+    assert np.all(np.isfinite(y))
+
+
+def test_device_batch_matches_host_calls(gb, executor):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    tasks, expect, keep = [], [], []
+    geoms = [(CASES_2D[0][1], CASES_2D[0][2], "f32"), (CASES_2D[1][1], CASES_2D[1][2], "u16"),
+             (CASES_2D[2][1], CASES_2D[2][2], "f32"), (F64_CASES[0][1], F64_CASES[0][2], "u8")]
+    for i, (hq, vq, sample) in enumerate(geoms * 2):
+        h, oh = plans(gb, executor, hq)
+        v, ov = plans(gb, executor, vq)
+        x = make_input(v.source_size, h.source_size, sample, 100 + i)
+        conv = gb.integer_conversion(8 if sample == "u8" else 16, False, False) if sample != "f32" else None
+        # uint16 planes travel as int16 tensors (same bytes).
+        dx = torch.from_numpy(x.view(np.int16) if sample == "u16" else x).cuda()
+        dy = torch.empty((v.destination_size, h.destination_size), dtype=dx.dtype, device="cuda")
+        keep += [dx, dy, h, v]
+        tasks.append(gb.PlaneTask(h, v, dx.data_ptr(), h.source_size, dy.data_ptr(),
+                                  h.destination_size, {"f32": 0, "u8": 1, "u16": 2}[sample], 0, conv))
+        expect.append((dy, executor.inverse_2d(h, v, x, conv), sample))
+    executor.run_batch(tasks, stream=torch.cuda.current_stream().cuda_stream, synchronize=True)
+    for dy, want, sample in expect:
+        got = dy.cpu().numpy()
+        if sample == "u16":
+            got = got.view(np.uint16)
+        assert np.array_equal(got, want)

@@ -1,0 +1,337 @@
+// extern "C" boundary (include/dsmvc_gb300.h): converts C++ exceptions to
+// status codes plus a thread-local message; no exception crosses the ABI.
+#include "../../include/dsmvc_gb300.h"
+
+#include "executor.hpp"
+#include "planner.hpp"
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+struct dsmvc_gb_plan {
+    std::shared_ptr<const dsmvc_gb::AxisPlan> plan;
+    dsmvc_gb::AxisRequest request;
+};
+
+struct dsmvc_gb_executor {
+    dsmvc_gb::Executor executor;
+    explicit dsmvc_gb_executor(int device) : executor(device) {}
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+template <class F>
+int guarded(F &&f) noexcept {
+    try {
+        g_error.clear();
+        f();
+        return DSMVC_GB_OK;
+    } catch (const std::invalid_argument &e) {
+        g_error = e.what();
+        return DSMVC_GB_INVALID_ARGUMENT;
+    } catch (const std::length_error &e) {
+        g_error = e.what();
+        return DSMVC_GB_LENGTH_ERROR;
+    } catch (const std::out_of_range &e) {
+        g_error = e.what();
+        return DSMVC_GB_LENGTH_ERROR;
+    } catch (const std::bad_alloc &) {
+        g_error = "out of host memory";
+        return DSMVC_GB_OUT_OF_MEMORY;
+    } catch (const std::logic_error &e) {
+        g_error = e.what();
+        return DSMVC_GB_INVALID_ARGUMENT;
+    } catch (const std::runtime_error &e) {
+        g_error = e.what();
+        const std::string m = e.what();
+        if (m.rfind("CUDA", 0) == 0) {
+            return m.find("out of memory") != std::string::npos ? DSMVC_GB_OUT_OF_MEMORY
+                                                                : DSMVC_GB_CUDA_ERROR;
+        }
+        if (m.find("requires an available CUDA device") != std::string::npos) return DSMVC_GB_UNAVAILABLE;
+        return DSMVC_GB_RUNTIME_ERROR;
+    } catch (...) {
+        g_error = "unknown error";
+        return DSMVC_GB_RUNTIME_ERROR;
+    }
+}
+
+dsmvc_gb::AxisRequest to_request(const dsmvc_gb_axis_request *r) {
+    if (!r) throw std::invalid_argument("request is null");
+    if (r->kernel < 0 || r->kernel > DSMVC_GB_CUSTOM) throw std::invalid_argument("kernel kind is invalid");
+    if (r->border < 0 || r->border > DSMVC_GB_MIRROR) throw std::invalid_argument("padding mode is invalid");
+    if (r->f64_mode < 0 || r->f64_mode > DSMVC_GB_F64_FORCE) throw std::invalid_argument("f64 mode is invalid");
+    dsmvc_gb::AxisRequest q;
+    q.source_size = r->source_size;
+    q.destination_size = r->destination_size;
+    q.active_length = r->active_length;
+    q.shift = r->shift;
+    q.kernel.kind = static_cast<dsmvc_gb::KernelKind>(r->kernel);
+    q.kernel.taps = r->taps;
+    q.kernel.b = r->b;
+    q.kernel.c = r->c;
+    q.kernel.blur = r->blur;
+    q.border = static_cast<dsmvc_gb::BorderMode>(r->border);
+    q.f64_mode = static_cast<dsmvc_gb::F64Mode>(r->f64_mode);
+    return q;
+}
+
+dsmvc_gb::CustomKernel to_custom(dsmvc_gb_custom_kernel fn, void *user) {
+    if (!fn) return {};
+    return [fn, user](double x) { return fn(x, user); };
+}
+
+const dsmvc_gb::AxisPlan &plan_of(const dsmvc_gb_plan *p) {
+    if (!p || !p->plan) throw std::invalid_argument("plan is null");
+    return *p->plan;
+}
+
+dsmvc_gb::Executor &exec_of(dsmvc_gb_executor *e) {
+    if (!e) throw std::invalid_argument("executor is null");
+    return e->executor;
+}
+
+dsmvc_gb::IntegerConversion to_conversion(const dsmvc_gb_conversion *c) {
+    if (!c) throw std::invalid_argument("conversion is null");
+    return {c->input_offset, c->input_scale, c->output_scale, c->output_offset, c->output_maximum};
+}
+
+} // namespace
+
+extern "C" {
+
+const char *dsmvc_gb_last_error(void) { return g_error.c_str(); }
+
+int dsmvc_gb_abi_version(void) { return DSMVC_GB_ABI_VERSION; }
+
+int dsmvc_gb_cuda_available(void) {
+    int count = 0;
+    return cudaGetDeviceCount(&count) == cudaSuccess && count > 0 ? 1 : 0;
+}
+
+int dsmvc_gb_plan_build(const dsmvc_gb_axis_request *request, dsmvc_gb_custom_kernel custom,
+                        void *user, dsmvc_gb_plan **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        auto q = to_request(request);
+        auto plan = std::make_shared<const dsmvc_gb::AxisPlan>(
+            dsmvc_gb::build_axis_plan(q, to_custom(custom, user)));
+        *out = new dsmvc_gb_plan{std::move(plan), q};
+    });
+}
+
+int dsmvc_gb_plan_get_or_build(const dsmvc_gb_axis_request *request, dsmvc_gb_custom_kernel custom,
+                               void *user, dsmvc_gb_plan **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        auto q = to_request(request);
+        auto plan = dsmvc_gb::get_or_build_axis_plan(q, to_custom(custom, user));
+        *out = new dsmvc_gb_plan{std::move(plan), q};
+    });
+}
+
+void dsmvc_gb_plan_release(dsmvc_gb_plan *plan) { delete plan; }
+
+int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out) {
+    return guarded([&] {
+        const auto &p = plan_of(plan);
+        if (!out) throw std::invalid_argument("output is null");
+        out->source_size = p.source_size;
+        out->destination_size = p.destination_size;
+        out->support = p.support;
+        out->half_bandwidth = p.half_bandwidth;
+        out->requires_float64 = p.requires_float64() ? 1 : 0;
+        out->max_row_entries = p.max_row_entries;
+        out->active_length = p.active_length;
+        out->shift = p.shift;
+        out->normal_rcond = p.normal_rcond;
+        out->normal_inf_norm = p.normal_inf_norm;
+        out->nonzeros = p.transpose_indices.size();
+        out->storage_bytes = p.storage_bytes();
+    });
+}
+
+int dsmvc_gb_plan_get_array(const dsmvc_gb_plan *plan, int32_t which, const void **data,
+                            uint64_t *count) {
+    return guarded([&] {
+        const auto &p = plan_of(plan);
+        if (!data || !count) throw std::invalid_argument("output is null");
+        switch (which) {
+        case 0: *data = p.transpose_offsets.data(); *count = p.transpose_offsets.size(); break;
+        case 1: *data = p.transpose_indices.data(); *count = p.transpose_indices.size(); break;
+        case 2: *data = p.transpose_weights.data(); *count = p.transpose_weights.size(); break;
+        case 3: *data = p.lower_ld.data(); *count = p.lower_ld.size(); break;
+        case 4: *data = p.upper_l.data(); *count = p.upper_l.size(); break;
+        case 5: *data = p.inverse_diagonal.data(); *count = p.inverse_diagonal.size(); break;
+        case 6: *data = p.transpose_weights_f64.data(); *count = p.transpose_weights_f64.size(); break;
+        case 7: *data = p.normal_bands_f64.data(); *count = p.normal_bands_f64.size(); break;
+        case 8: *data = p.ldlt_bands_f64.data(); *count = p.ldlt_bands_f64.size(); break;
+        case 9: *data = p.inverse_diagonal_f64.data(); *count = p.inverse_diagonal_f64.size(); break;
+        default: throw std::invalid_argument("plan array index is invalid");
+        }
+    });
+}
+
+int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan, const dsmvc_gb_axis_request *request,
+                         uint64_t *f32_hash, uint64_t *complete_hash) {
+    return guarded([&] {
+        const auto &p = plan_of(plan);
+        const auto q = request ? to_request(request) : plan->request;
+        if (f32_hash) *f32_hash = dsmvc_gb::f32_plan_hash(q, p);
+        if (complete_hash) *complete_hash = dsmvc_gb::complete_plan_hash(q, p);
+    });
+}
+
+int dsmvc_gb_planner_cache_stats(dsmvc_gb_planner_stats *out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output is null");
+        const auto s = dsmvc_gb::planner_cache_stats();
+        out->plan_hits = s.plan_hits;
+        out->plan_builds = s.plan_builds;
+        out->plan_entries = s.plan_entries;
+        out->plan_resident_bytes = s.plan_resident_bytes;
+    });
+}
+
+void dsmvc_gb_clear_planner_caches(void) { dsmvc_gb::clear_planner_caches(); }
+
+int dsmvc_gb_executor_create(int32_t device, dsmvc_gb_executor **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        *out = new dsmvc_gb_executor(device);
+    });
+}
+
+void dsmvc_gb_executor_destroy(dsmvc_gb_executor *executor) { delete executor; }
+
+int dsmvc_gb_prepare(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan) {
+    return guarded([&] {
+        plan_of(plan);
+        exec_of(executor).prepare(plan->plan);
+    });
+}
+
+int dsmvc_gb_seal(dsmvc_gb_executor *executor) {
+    return guarded([&] { exec_of(executor).seal(); });
+}
+
+int dsmvc_gb_executor_get_stats(dsmvc_gb_executor *executor, dsmvc_gb_executor_stats *out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output is null");
+        const auto s = exec_of(executor).stats();
+        out->launches = s.launches;
+        out->plane_tasks = s.plane_tasks;
+        out->plan_uploads = s.plan_uploads;
+        out->device_plan_bytes = s.device_plan_bytes;
+        out->workspace_bytes = s.workspace_bytes;
+    });
+}
+
+int dsmvc_gb_inverse_rows(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan,
+                          const float *input, int64_t input_stride, float *output,
+                          int64_t output_stride, int32_t rows) {
+    return guarded([&] {
+        exec_of(executor).inverse_rows(plan_of(plan), input, input_stride, output, output_stride, rows);
+    });
+}
+
+int dsmvc_gb_inverse_columns(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan,
+                             const float *input, int64_t input_stride, float *output,
+                             int64_t output_stride, int32_t columns) {
+    return guarded([&] {
+        exec_of(executor).inverse_columns(plan_of(plan), input, input_stride, output, output_stride,
+                                          columns);
+    });
+}
+
+int dsmvc_gb_inverse_2d(dsmvc_gb_executor *executor, const dsmvc_gb_plan *horizontal,
+                        const dsmvc_gb_plan *vertical, const float *input, int64_t input_stride,
+                        float *output, int64_t output_stride) {
+    return guarded([&] {
+        exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::f32,
+                                     input, input_stride, output, output_stride, {});
+    });
+}
+
+int dsmvc_gb_inverse_2d_u8(dsmvc_gb_executor *executor, const dsmvc_gb_plan *horizontal,
+                           const dsmvc_gb_plan *vertical, const uint8_t *input, int64_t input_stride,
+                           uint8_t *output, int64_t output_stride,
+                           const dsmvc_gb_conversion *conversion) {
+    return guarded([&] {
+        exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::u8,
+                                     input, input_stride, output, output_stride,
+                                     to_conversion(conversion));
+    });
+}
+
+int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor, const dsmvc_gb_plan *horizontal,
+                            const dsmvc_gb_plan *vertical, const uint16_t *input,
+                            int64_t input_stride, uint16_t *output, int64_t output_stride,
+                            const dsmvc_gb_conversion *conversion) {
+    return guarded([&] {
+        exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::u16,
+                                     input, input_stride, output, output_stride,
+                                     to_conversion(conversion));
+    });
+}
+
+int dsmvc_gb_run_batch(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task *tasks, int32_t count,
+                       void *stream, int32_t synchronize) {
+    return guarded([&] {
+        auto &ex = exec_of(executor);
+        if (count < 0 || (count > 0 && !tasks)) throw std::invalid_argument("invalid task list");
+        std::vector<dsmvc_gb::PlaneTask> list(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) {
+            const auto &t = tasks[i];
+            if (t.sample < DSMVC_GB_FLOAT32 || t.sample > DSMVC_GB_UINT16)
+                throw std::invalid_argument("sample kind is invalid");
+            auto &d = list[static_cast<std::size_t>(i)];
+            d.horizontal = t.horizontal ? &plan_of(t.horizontal) : nullptr;
+            d.vertical = t.vertical ? &plan_of(t.vertical) : nullptr;
+            d.input = t.input;
+            d.input_stride = t.input_stride;
+            d.output = t.output;
+            d.output_stride = t.output_stride;
+            d.sample = static_cast<dsmvc_gb::dev::Sample>(t.sample);
+            d.vectors = t.vectors;
+            d.conversion = to_conversion(&t.conversion);
+        }
+        ex.run_batch(list, stream, synchronize != 0);
+    });
+}
+
+int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream) {
+    return guarded([&] { exec_of(executor).check_status(stream); });
+}
+
+int dsmvc_gb_profile(dsmvc_gb_executor *executor, int32_t enable) {
+    return guarded([&] { exec_of(executor).set_profiling(enable != 0); });
+}
+
+int dsmvc_gb_profile_read(dsmvc_gb_executor *executor, dsmvc_gb_kernel_time *out,
+                          int32_t capacity, int32_t *count) {
+    return guarded([&] {
+        if (!count || capacity < 0 || (capacity > 0 && !out))
+            throw std::invalid_argument("invalid profile buffer");
+        const auto times = exec_of(executor).kernel_times();
+        *count = static_cast<int32_t>(times.size());
+        for (std::size_t i = 0; i < times.size() && static_cast<int32_t>(i) < capacity; ++i) {
+            auto &o = out[i];
+            std::snprintf(o.name, sizeof(o.name), "%s", times[i].name.c_str());
+            o.launches = times[i].launches;
+            o.milliseconds = times[i].milliseconds;
+            o.bytes = times[i].bytes;
+        }
+    });
+}
+
+} // extern "C"

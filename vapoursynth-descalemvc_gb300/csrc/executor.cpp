@@ -1,0 +1,689 @@
+// GB300 descale executor (see executor.hpp).
+//
+// Device layout of one prepared plan: a single allocation holding the A^T CSR
+// (offsets, indices, Float32 weights), the Float32 factor bands lower/upper,
+// the inverse diagonal and, for plans that retain Float64, the Float64
+// weights and LDL^T bands; every sub-array starts on a 256-byte boundary.
+//
+// A 2D plane runs as two batched launches per half-bandwidth group: the
+// horizontal pass (one vector per source row) into a Float32 intermediate
+// (Float64 in the Float64 route), then the vertical pass (one vector per
+// destination column) into the output, with integer conversion fused into
+// the load of the first pass and the store of the second.
+#include "executor.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+
+namespace dsmvc_gb {
+namespace {
+
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string("CUDA ") + what + ": " + cudaGetErrorString(e));
+}
+void cuda_check(int e, const char *what) { cuda_check(static_cast<cudaError_t>(e), what); }
+
+constexpr std::size_t kAlign = 256;
+std::size_t align_up(std::size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+std::size_t sample_bytes(dev::Sample s) {
+    switch (s) {
+    case dev::Sample::u8: return 1;
+    case dev::Sample::u16: return 2;
+    case dev::Sample::f64: return 8;
+    default: return 4;
+    }
+}
+
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+    void reserve(std::size_t bytes) {
+        if (bytes <= bytes_) return;
+        release();
+        cuda_check(cudaMalloc(&ptr_, bytes), "allocating workspace");
+        bytes_ = bytes;
+    }
+    void release() {
+        if (ptr_) cudaFree(ptr_);
+        ptr_ = nullptr;
+        bytes_ = 0;
+    }
+    [[nodiscard]] char *data() const { return static_cast<char *>(ptr_); }
+    [[nodiscard]] std::size_t size() const { return bytes_; }
+
+private:
+    void *ptr_ = nullptr;
+    std::size_t bytes_ = 0;
+};
+
+struct DevicePlan {
+    std::shared_ptr<const AxisPlan> keep;
+    DeviceBuffer memory;
+    dev::PlanView view{};
+    std::size_t bytes = 0;
+};
+
+std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
+    if (!plan || !plan->valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
+    const AxisPlan &p = *plan;
+    const bool f64 = p.requires_float64();
+    std::vector<std::pair<const void *, std::size_t>> parts = {
+        {p.transpose_offsets.data(), p.transpose_offsets.size() * 4},
+        {p.transpose_indices.data(), p.transpose_indices.size() * 4},
+        {p.transpose_weights.data(), p.transpose_weights.size() * 4},
+        {p.lower_ld.data(), p.lower_ld.size() * 4},
+        {p.upper_l.data(), p.upper_l.size() * 4},
+        {p.inverse_diagonal.data(), p.inverse_diagonal.size() * 4},
+        {f64 ? p.transpose_weights_f64.data() : nullptr, f64 ? p.transpose_weights_f64.size() * 8 : 0},
+        {f64 ? p.ldlt_bands_f64.data() : nullptr, f64 ? p.ldlt_bands_f64.size() * 8 : 0},
+    };
+    std::size_t total = 0;
+    std::vector<std::size_t> offsets;
+    for (auto &part : parts) {
+        offsets.push_back(total);
+        total += align_up(std::max<std::size_t>(part.second, 1));
+    }
+    std::vector<char> host(total, 0);
+    for (std::size_t i = 0; i < parts.size(); ++i)
+        if (parts[i].second) std::memcpy(host.data() + offsets[i], parts[i].first, parts[i].second);
+    auto dp = std::make_unique<DevicePlan>();
+    dp->memory.reserve(total);
+    cuda_check(cudaMemcpy(dp->memory.data(), host.data(), total, cudaMemcpyHostToDevice), "uploading plan");
+    char *base = dp->memory.data();
+    auto &v = dp->view;
+    v.source_size = p.source_size;
+    v.destination_size = p.destination_size;
+    v.half_bandwidth = p.half_bandwidth;
+    v.retains_f64 = f64 ? 1 : 0;
+    v.offsets = reinterpret_cast<const std::uint32_t *>(base + offsets[0]);
+    v.indices = reinterpret_cast<const std::int32_t *>(base + offsets[1]);
+    v.weights = reinterpret_cast<const float *>(base + offsets[2]);
+    v.lower = reinterpret_cast<const float *>(base + offsets[3]);
+    v.upper = reinterpret_cast<const float *>(base + offsets[4]);
+    v.inv_diag = reinterpret_cast<const float *>(base + offsets[5]);
+    v.weights64 = f64 ? reinterpret_cast<const double *>(base + offsets[6]) : nullptr;
+    v.bands64 = f64 ? reinterpret_cast<const double *>(base + offsets[7]) : nullptr;
+    dp->bytes = total;
+    dp->keep = std::move(plan);
+    return dp;
+}
+
+// Per-stream scratch: intermediate, forward scratch, staged host frames, job
+// table and the Float64 status word.
+struct Workspace {
+    cudaStream_t stream = nullptr;
+    bool owns_stream = false;
+    DeviceBuffer scratch;
+    DeviceBuffer staging;
+    DeviceBuffer jobs;
+    std::uint32_t *status = nullptr;      // device
+    std::uint32_t *status_host = nullptr; // pinned
+    std::vector<dev::AxisJob> host_jobs;
+
+    explicit Workspace(cudaStream_t s) : stream(s) {
+        if (!stream) {
+            cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "creating stream");
+            owns_stream = true;
+        }
+        cuda_check(cudaMalloc(&status, sizeof(std::uint32_t)), "allocating status");
+        cuda_check(cudaMallocHost(&status_host, sizeof(std::uint32_t)), "allocating status");
+        cuda_check(cudaMemsetAsync(status, 0, sizeof(std::uint32_t), stream), "clearing status");
+    }
+    ~Workspace() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (status) cudaFree(status);
+        if (status_host) cudaFreeHost(status_host);
+        if (owns_stream) cudaStreamDestroy(stream);
+    }
+};
+
+struct DeviceGuard {
+    int previous = -1;
+    explicit DeviceGuard(int device) {
+        cudaGetDevice(&previous);
+        if (previous != device) cuda_check(cudaSetDevice(device), "selecting device");
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        cudaGetDevice(&now);
+        if (previous >= 0 && now != previous) cudaSetDevice(previous);
+    }
+};
+
+} // namespace
+
+struct Executor::Impl {
+    int device = 0;
+    mutable std::mutex mutex;
+    std::unordered_map<const AxisPlan *, std::unique_ptr<DevicePlan>> plans;
+    bool sealed = false;
+    // Synchronous host calls take one of these slots (the reference's
+    // execution slots, src/cuda/cuda_executor.cpp:1102-1160).
+    std::vector<std::unique_ptr<Workspace>> slots;
+    std::vector<bool> slot_busy;
+    std::condition_variable slot_free;
+    std::map<cudaStream_t, std::unique_ptr<Workspace>> stream_spaces;
+    ExecutorStats stats;
+
+    // Optional per-launch CUDA-event timing (dsmvc_gb_profile).
+    struct Record {
+        std::string name;
+        cudaEvent_t start = nullptr, stop = nullptr;
+        std::uint64_t bytes = 0;
+    };
+    bool profiling = false;
+    std::vector<Record> records;
+
+    const dev::PlanView &view(const AxisPlan &plan, std::vector<std::unique_ptr<DevicePlan>> &temporaries) {
+        {
+            std::scoped_lock lock(mutex);
+            if (auto it = plans.find(&plan); it != plans.end()) return it->second->view;
+        }
+        // Not prepared: upload a private copy for this call only.
+        temporaries.push_back(upload_plan(std::make_shared<const AxisPlan>(plan)));
+        std::scoped_lock lock(mutex);
+        ++stats.plan_uploads;
+        return temporaries.back()->view;
+    }
+
+    Workspace &acquire_slot(std::size_t &index) {
+        std::unique_lock lock(mutex);
+        for (;;) {
+            for (std::size_t i = 0; i < slots.size(); ++i) {
+                if (!slot_busy[i]) {
+                    slot_busy[i] = true;
+                    index = i;
+                    return *slots[i];
+                }
+            }
+            if (slots.size() < 4) {
+                slots.push_back(std::make_unique<Workspace>(nullptr));
+                slot_busy.push_back(true);
+                index = slots.size() - 1;
+                return *slots.back();
+            }
+            slot_free.wait(lock);
+        }
+    }
+
+    void release_slot(std::size_t index) {
+        {
+            std::scoped_lock lock(mutex);
+            slot_busy[index] = false;
+        }
+        slot_free.notify_one();
+    }
+
+    Workspace &stream_space(cudaStream_t stream) {
+        std::scoped_lock lock(mutex);
+        auto &ws = stream_spaces[stream];
+        if (!ws) ws = std::make_unique<Workspace>(stream);
+        return *ws;
+    }
+
+    void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks);
+    void finish(Workspace &ws);
+};
+
+namespace {
+
+struct GroupKey {
+    int pass;      // 0 horizontal, 1 vertical
+    bool f64;
+    int hb;
+    dev::Sample in, out;
+    bool operator<(const GroupKey &o) const {
+        return std::tie(pass, f64, hb, in, out) < std::tie(o.pass, o.f64, o.hb, o.in, o.out);
+    }
+};
+
+dev::Conversion to_dev(const IntegerConversion &c) {
+    return {c.input_offset, c.input_scale, c.output_scale, c.output_offset, c.output_maximum};
+}
+
+} // namespace
+
+void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks) {
+    std::vector<std::unique_ptr<DevicePlan>> temporaries;
+    // Scratch layout: per task, an intermediate and a forward scratch.
+    struct Scratch { std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0; bool f64 = false; };
+    std::vector<Scratch> scratch(tasks.size());
+    std::size_t bytes = 0;
+    for (std::size_t t = 0; t < tasks.size(); ++t) {
+        const auto &task = tasks[t];
+        const AxisPlan *h = task.horizontal, *v = task.vertical;
+        if (!h && !v) throw std::invalid_argument("plane task without a plan");
+        auto &s = scratch[t];
+        s.f64 = (h && h->requires_float64()) || (v && v->requires_float64());
+        const std::size_t es = s.f64 ? 8 : 4;
+        if (h && v) {
+            s.mid_stride = static_cast<std::size_t>(h->destination_size);
+            s.mid = bytes;
+            bytes += align_up(s.mid_stride * static_cast<std::size_t>(v->source_size) * es);
+            if (s.f64 || task.sample != dev::Sample::f32) {
+                s.fwd_stride = static_cast<std::size_t>(h->destination_size);
+                s.fwd = bytes;
+                bytes += align_up(s.fwd_stride * static_cast<std::size_t>(v->destination_size) * es);
+            }
+        } else if (s.f64) {
+            const AxisPlan *p = h ? h : v;
+            s.fwd_stride = h ? static_cast<std::size_t>(p->destination_size) : static_cast<std::size_t>(task.vectors);
+            const std::size_t lines = h ? static_cast<std::size_t>(task.vectors) : static_cast<std::size_t>(p->destination_size);
+            s.fwd = bytes;
+            bytes += align_up(s.fwd_stride * lines * 8);
+        }
+    }
+    ws.scratch.reserve(std::max<std::size_t>(bytes, kAlign));
+    char *base = ws.scratch.data();
+
+    // Each job carries its compulsory bytes (input read by a first pass,
+    // output written by a last pass) for the roofline accounting.
+    std::map<GroupKey, std::vector<std::pair<dev::AxisJob, std::uint64_t>>> groups;
+    for (std::size_t t = 0; t < tasks.size(); ++t) {
+        const auto &task = tasks[t];
+        const auto &s = scratch[t];
+        const AxisPlan *h = task.horizontal, *v = task.vertical;
+        const dev::Conversion conv = to_dev(task.conversion);
+        const dev::Sample mid_kind = s.f64 ? dev::Sample::f64 : dev::Sample::f32;
+        if (h) {
+            dev::AxisJob j{};
+            j.plan = view(*h, temporaries);
+            j.in = task.input;
+            j.in_elem = 1;
+            j.in_vec = task.input_stride;
+            j.vectors = v ? v->source_size : task.vectors;
+            j.conv = conv;
+            GroupKey key{0, s.f64, h->half_bandwidth, task.sample, v ? mid_kind : task.sample};
+            if (v) {
+                j.out = base + s.mid;
+                j.out_elem = 1;
+                j.out_vec = static_cast<std::int64_t>(s.mid_stride);
+                j.fwd = j.out;
+                j.fwd_elem = 1;
+                j.fwd_vec = j.out_vec;
+            } else {
+                j.out = task.output;
+                j.out_elem = 1;
+                j.out_vec = task.output_stride;
+                if (s.f64) {
+                    j.fwd = base + s.fwd;
+                    j.fwd_elem = 1;
+                    j.fwd_vec = static_cast<std::int64_t>(s.fwd_stride);
+                } else {
+                    j.fwd = j.out;
+                    j.fwd_elem = 1;
+                    j.fwd_vec = j.out_vec;
+                }
+            }
+            std::uint64_t hb_bytes = static_cast<std::uint64_t>(j.vectors) * h->source_size
+                * sample_bytes(task.sample);
+            if (!v) hb_bytes += static_cast<std::uint64_t>(j.vectors) * h->destination_size * 4;
+            groups[key].push_back({j, hb_bytes});
+        }
+        if (v) {
+            dev::AxisJob j{};
+            j.plan = view(*v, temporaries);
+            j.conv = conv;
+            if (h) {
+                j.in = base + s.mid;
+                j.in_elem = static_cast<std::int64_t>(s.mid_stride);
+                j.in_vec = 1;
+                j.vectors = h->destination_size;
+            } else {
+                j.in = task.input;
+                j.in_elem = task.input_stride;
+                j.in_vec = 1;
+                j.vectors = task.vectors;
+            }
+            j.out = task.output;
+            j.out_elem = task.output_stride;
+            j.out_vec = 1;
+            if (s.fwd_stride) {
+                j.fwd = base + s.fwd;
+                j.fwd_elem = static_cast<std::int64_t>(s.fwd_stride);
+                j.fwd_vec = 1;
+            } else {
+                j.fwd = j.out;
+                j.fwd_elem = j.out_elem;
+                j.fwd_vec = 1;
+            }
+            GroupKey key{1, s.f64, v->half_bandwidth, h ? mid_kind : task.sample, task.sample};
+            std::uint64_t vb_bytes = static_cast<std::uint64_t>(j.vectors) * v->destination_size
+                * sample_bytes(task.sample);
+            if (!h) vb_bytes += static_cast<std::uint64_t>(j.vectors) * v->source_size * 4;
+            groups[key].push_back({j, vb_bytes});
+        }
+    }
+
+    constexpr int kThreads = 128;
+    std::vector<dev::AxisJob> &all = ws.host_jobs;
+    all.clear();
+    struct Launch { GroupKey key; std::size_t first; int count; int blocks; std::uint64_t bytes; };
+    std::vector<Launch> launches;
+    for (auto &[key, jobs] : groups) {
+        int blocks = 0;
+        std::uint64_t bytes = 0;
+        std::vector<dev::AxisJob> kept;
+        for (auto &[j, b] : jobs) {
+            if (j.vectors <= 0) continue;
+            j.first_block = blocks;
+            blocks += (j.vectors + kThreads - 1) / kThreads;
+            bytes += b;
+            kept.push_back(j);
+        }
+        if (kept.empty()) continue;
+        launches.push_back({key, all.size(), static_cast<int>(kept.size()), blocks, bytes});
+        all.insert(all.end(), kept.begin(), kept.end());
+    }
+    if (launches.empty()) return;
+    const std::size_t table = all.size() * sizeof(dev::AxisJob);
+    ws.jobs.reserve(table);
+    cuda_check(cudaMemcpyAsync(ws.jobs.data(), all.data(), table, cudaMemcpyHostToDevice, ws.stream),
+               "uploading job table");
+    auto *device_jobs = reinterpret_cast<const dev::AxisJob *>(ws.jobs.data());
+    for (const auto &l : launches) {
+        Record *rec = nullptr;
+        if (profiling) {
+            std::scoped_lock lock(mutex);
+            records.emplace_back();
+            rec = &records.back();
+            rec->name = std::string(l.key.f64 ? "axis_f64" : "axis_f32") + (l.key.pass ? "/vertical" : "/horizontal")
+                + "/hb" + std::to_string(l.key.hb);
+            rec->bytes = l.bytes;
+            cuda_check(cudaEventCreate(&rec->start), "creating event");
+            cuda_check(cudaEventCreate(&rec->stop), "creating event");
+            cuda_check(cudaEventRecord(rec->start, ws.stream), "recording event");
+        }
+        const int rc = l.key.f64
+            ? launch_axis_f64(device_jobs + l.first, l.count, l.blocks, kThreads, l.key.hb,
+                              l.key.in, l.key.out, ws.status, ws.stream)
+            : launch_axis_f32(device_jobs + l.first, l.count, l.blocks, kThreads, l.key.hb,
+                              l.key.in, l.key.out, ws.stream);
+        cuda_check(rc, "launching axis kernel");
+        if (rec) cuda_check(cudaEventRecord(rec->stop, ws.stream), "recording event");
+    }
+    {
+        std::scoped_lock lock(mutex);
+        stats.launches += launches.size();
+        stats.plane_tasks += tasks.size();
+    }
+    if (!temporaries.empty()) {
+        // Private plan copies must outlive the kernels that read them.
+        cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
+    }
+}
+
+void Executor::Impl::finish(Workspace &ws) {
+    cuda_check(cudaMemcpyAsync(ws.status_host, ws.status, sizeof(std::uint32_t),
+                               cudaMemcpyDeviceToHost, ws.stream), "reading status");
+    cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
+    const std::uint32_t status = *ws.status_host;
+    if (status) {
+        cuda_check(cudaMemsetAsync(ws.status, 0, sizeof(std::uint32_t), ws.stream), "clearing status");
+        cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
+        if (status & dev::kStatusNonFiniteInput)
+            throw std::runtime_error("Float64 input contains NaN or infinity");
+        throw std::runtime_error("Float64 execution produced NaN or infinity");
+    }
+}
+
+Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        throw std::runtime_error("backend 'cuda' requires an available CUDA device");
+    if (device < 0) cuda_check(cudaGetDevice(&device), "querying device");
+    if (device >= count) throw std::invalid_argument("CUDA device index out of range");
+    impl_->device = device;
+    DeviceGuard guard(device);
+    cuda_check(cudaFree(nullptr), "initialising the primary context");
+}
+
+Executor::~Executor() {
+    if (!impl_) return;
+    DeviceGuard guard(impl_->device);
+    impl_->slots.clear();
+    impl_->stream_spaces.clear();
+    impl_->plans.clear();
+}
+
+int Executor::device() const noexcept { return impl_->device; }
+
+void Executor::prepare(std::shared_ptr<const AxisPlan> plan) {
+    if (!plan || !plan->valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
+    {
+        std::scoped_lock lock(impl_->mutex);
+        if (impl_->plans.count(plan.get())) return;
+        if (impl_->sealed) throw std::logic_error("executor is sealed; prepare plans before seal()");
+    }
+    DeviceGuard guard(impl_->device);
+    auto dp = upload_plan(plan);
+    std::scoped_lock lock(impl_->mutex);
+    impl_->stats.plan_uploads += 1;
+    impl_->stats.device_plan_bytes += dp->bytes;
+    impl_->plans.emplace(plan.get(), std::move(dp));
+}
+
+void Executor::seal() {
+    std::scoped_lock lock(impl_->mutex);
+    impl_->sealed = true;
+}
+
+namespace {
+
+void check_rows(const AxisPlan &plan, const void *in, std::ptrdiff_t is, const void *out,
+                std::ptrdiff_t os, std::int32_t rows) {
+    if (!plan.valid() || !in || !out || is < plan.source_size || os < plan.destination_size || rows < 0)
+        throw std::invalid_argument("invalid row executor arguments");
+}
+
+void check_columns(const AxisPlan &plan, const void *in, std::ptrdiff_t is, const void *out,
+                   std::ptrdiff_t os, std::int32_t columns) {
+    if (!plan.valid() || !in || !out || columns < 0 || is < columns || os < columns)
+        throw std::invalid_argument("invalid column executor arguments");
+}
+
+} // namespace
+
+void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdiff_t is,
+                            float *output, std::ptrdiff_t os, std::int32_t rows) {
+    check_rows(plan, input, is, output, os, rows);
+    if (rows == 0) return;
+    DeviceGuard guard(impl_->device);
+    std::size_t slot = 0;
+    Workspace &ws = impl_->acquire_slot(slot);
+    try {
+        const std::size_t in_bytes = align_up(static_cast<std::size_t>(rows) * plan.source_size * 4);
+        const std::size_t out_bytes = align_up(static_cast<std::size_t>(rows) * plan.destination_size * 4);
+        ws.staging.reserve(in_bytes + out_bytes);
+        char *din = ws.staging.data();
+        char *dout = din + in_bytes;
+        cuda_check(cudaMemcpy2DAsync(din, plan.source_size * 4, input, is * 4, plan.source_size * 4,
+                                     rows, cudaMemcpyHostToDevice, ws.stream), "uploading rows");
+        PlaneTask t;
+        t.horizontal = &plan;
+        t.input = din;
+        t.input_stride = plan.source_size;
+        t.output = dout;
+        t.output_stride = plan.destination_size;
+        t.vectors = rows;
+        impl_->enqueue(ws, {t});
+        cuda_check(cudaMemcpy2DAsync(output, os * 4, dout, plan.destination_size * 4,
+                                     plan.destination_size * 4, rows, cudaMemcpyDeviceToHost, ws.stream),
+                   "downloading rows");
+        impl_->finish(ws);
+    } catch (...) {
+        cudaStreamSynchronize(ws.stream);
+        impl_->release_slot(slot);
+        throw;
+    }
+    impl_->release_slot(slot);
+}
+
+void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::ptrdiff_t is,
+                               float *output, std::ptrdiff_t os, std::int32_t columns) {
+    check_columns(plan, input, is, output, os, columns);
+    if (columns == 0) return;
+    DeviceGuard guard(impl_->device);
+    std::size_t slot = 0;
+    Workspace &ws = impl_->acquire_slot(slot);
+    try {
+        const std::size_t in_bytes = align_up(static_cast<std::size_t>(plan.source_size) * columns * 4);
+        const std::size_t out_bytes = align_up(static_cast<std::size_t>(plan.destination_size) * columns * 4);
+        ws.staging.reserve(in_bytes + out_bytes);
+        char *din = ws.staging.data();
+        char *dout = din + in_bytes;
+        cuda_check(cudaMemcpy2DAsync(din, columns * 4, input, is * 4, columns * 4, plan.source_size,
+                                     cudaMemcpyHostToDevice, ws.stream), "uploading columns");
+        PlaneTask t;
+        t.vertical = &plan;
+        t.input = din;
+        t.input_stride = columns;
+        t.output = dout;
+        t.output_stride = columns;
+        t.vectors = columns;
+        impl_->enqueue(ws, {t});
+        cuda_check(cudaMemcpy2DAsync(output, os * 4, dout, columns * 4, columns * 4,
+                                     plan.destination_size, cudaMemcpyDeviceToHost, ws.stream),
+                   "downloading columns");
+        impl_->finish(ws);
+    } catch (...) {
+        cudaStreamSynchronize(ws.stream);
+        impl_->release_slot(slot);
+        throw;
+    }
+    impl_->release_slot(slot);
+}
+
+void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
+                          const void *input, std::ptrdiff_t is, void *output, std::ptrdiff_t os,
+                          const IntegerConversion &conv) {
+    if (!h.valid() || !v.valid() || !input || !output || is < h.source_size
+        || os < h.destination_size || sample == dev::Sample::f64)
+        throw std::invalid_argument("invalid 2D executor arguments");
+    if (sample != dev::Sample::f32) {
+        const std::uint32_t limit = sample == dev::Sample::u8 ? 255U : 65535U;
+        if (!(conv.input_scale > 0.0F) || !(conv.output_scale > 0.0F)
+            || !std::isfinite(conv.input_offset) || !std::isfinite(conv.input_scale)
+            || !std::isfinite(conv.output_scale) || !std::isfinite(conv.output_offset)
+            || conv.output_maximum == 0U || conv.output_maximum > limit)
+            throw std::invalid_argument("invalid integer 2D executor arguments");
+    }
+    const std::size_t es = sample_bytes(sample);
+    DeviceGuard guard(impl_->device);
+    std::size_t slot = 0;
+    Workspace &ws = impl_->acquire_slot(slot);
+    try {
+        const std::size_t in_row = static_cast<std::size_t>(h.source_size) * es;
+        const std::size_t out_row = static_cast<std::size_t>(h.destination_size) * es;
+        const std::size_t in_bytes = align_up(in_row * v.source_size);
+        const std::size_t out_bytes = align_up(out_row * v.destination_size);
+        ws.staging.reserve(in_bytes + out_bytes);
+        char *din = ws.staging.data();
+        char *dout = din + in_bytes;
+        cuda_check(cudaMemcpy2DAsync(din, in_row, input, is * es, in_row, v.source_size,
+                                     cudaMemcpyHostToDevice, ws.stream), "uploading plane");
+        PlaneTask t;
+        t.horizontal = &h;
+        t.vertical = &v;
+        t.input = din;
+        t.input_stride = h.source_size;
+        t.output = dout;
+        t.output_stride = h.destination_size;
+        t.sample = sample;
+        t.conversion = conv;
+        impl_->enqueue(ws, {t});
+        cuda_check(cudaMemcpy2DAsync(output, os * es, dout, out_row, out_row, v.destination_size,
+                                     cudaMemcpyDeviceToHost, ws.stream), "downloading plane");
+        impl_->finish(ws);
+    } catch (...) {
+        cudaStreamSynchronize(ws.stream);
+        impl_->release_slot(slot);
+        throw;
+    }
+    impl_->release_slot(slot);
+}
+
+void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize) {
+    DeviceGuard guard(impl_->device);
+    for (const auto &t : tasks) {
+        const AxisPlan *h = t.horizontal, *v = t.vertical;
+        if ((!h && !v) || !t.input || !t.output || (h && !h->valid()) || (v && !v->valid()))
+            throw std::invalid_argument("invalid batch plane");
+        if (h && v) {
+            if (t.input_stride < h->source_size || t.output_stride < h->destination_size)
+                throw std::invalid_argument("invalid batch plane strides");
+        } else if (h) {
+            if (t.sample != dev::Sample::f32 || t.vectors < 0 || t.input_stride < h->source_size
+                || t.output_stride < h->destination_size)
+                throw std::invalid_argument("invalid batch row task");
+        } else {
+            if (t.sample != dev::Sample::f32 || t.vectors < 0 || t.input_stride < t.vectors
+                || t.output_stride < t.vectors)
+                throw std::invalid_argument("invalid batch column task");
+        }
+    }
+    Workspace &ws = impl_->stream_space(static_cast<cudaStream_t>(stream));
+    impl_->enqueue(ws, tasks);
+    if (synchronize) impl_->finish(ws);
+}
+
+void Executor::check_status(void *stream) {
+    DeviceGuard guard(impl_->device);
+    impl_->finish(impl_->stream_space(static_cast<cudaStream_t>(stream)));
+}
+
+void Executor::set_profiling(bool enable) {
+    DeviceGuard guard(impl_->device);
+    std::scoped_lock lock(impl_->mutex);
+    for (auto &r : impl_->records) {
+        if (r.start) cudaEventDestroy(r.start);
+        if (r.stop) cudaEventDestroy(r.stop);
+    }
+    impl_->records.clear();
+    impl_->profiling = enable;
+}
+
+std::vector<KernelTime> Executor::kernel_times() {
+    DeviceGuard guard(impl_->device);
+    std::scoped_lock lock(impl_->mutex);
+    std::vector<KernelTime> out;
+    for (auto &r : impl_->records) {
+        cuda_check(cudaEventSynchronize(r.stop), "waiting for profiled kernel");
+        float ms = 0.0F;
+        cuda_check(cudaEventElapsedTime(&ms, r.start, r.stop), "reading event");
+        auto it = std::find_if(out.begin(), out.end(), [&](const KernelTime &k) { return k.name == r.name; });
+        if (it == out.end()) {
+            out.push_back({r.name, 0, 0.0, 0});
+            it = out.end() - 1;
+        }
+        it->launches += 1;
+        it->milliseconds += ms;
+        it->bytes += r.bytes;
+    }
+    return out;
+}
+
+ExecutorStats Executor::stats() const {
+    std::scoped_lock lock(impl_->mutex);
+    ExecutorStats s = impl_->stats;
+    for (const auto &ws : impl_->slots) s.workspace_bytes += ws->scratch.size() + ws->staging.size();
+    for (const auto &[k, ws] : impl_->stream_spaces) s.workspace_bytes += ws->scratch.size();
+    return s;
+}
+
+} // namespace dsmvc_gb

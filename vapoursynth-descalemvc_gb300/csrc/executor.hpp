@@ -1,0 +1,108 @@
+// GB300 descale executor: the backend behind the C ABI (capi.cpp).
+//
+// Mirrors the reference's CUDA executor contract (src/cuda/cuda_executor.hpp:
+// 11-110, include/dsmvc/engine.hpp:363-504): plans are prepared once and
+// sealed, host-frame calls are synchronous (the output is written when the
+// call returns), strides are in samples, row padding is never read past the
+// logical width nor written, and a Float64 plan on either axis sends the
+// whole 2D call through the Float64 route, which raises on non-finite data.
+// Added for GPU-resident callers: device-pointer calls enqueued on a stream
+// and batched submissions of many planes (frames x planes, candidate sweeps)
+// in one set of launches.
+#pragma once
+
+#include "kernels.cuh"
+#include "planner.hpp"
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace dsmvc_gb {
+
+struct IntegerConversion {
+    float input_offset = 0.0F;
+    float input_scale = 1.0F;
+    float output_scale = 1.0F;
+    float output_offset = 0.0F;
+    std::uint32_t output_maximum = 255U;
+};
+
+// One 2D plane of a batch, device pointers.  `horizontal` or `vertical` may
+// be null for a one-axis descale of that plane (rows only / columns only).
+struct PlaneTask {
+    const AxisPlan *horizontal = nullptr;
+    const AxisPlan *vertical = nullptr;
+    const void *input = nullptr;
+    std::ptrdiff_t input_stride = 0;    // samples
+    void *output = nullptr;
+    std::ptrdiff_t output_stride = 0;   // samples
+    dev::Sample sample = dev::Sample::f32;
+    IntegerConversion conversion{};
+    // Source extent of a one-axis task: rows for rows-only, columns for
+    // columns-only (ignored for 2D tasks).
+    std::int32_t vectors = 0;
+};
+
+// Per-kernel CUDA-event timing aggregated by kernel name; `bytes` counts the
+// compulsory traffic of the launches (first-pass input, last-pass output).
+struct KernelTime {
+    std::string name;
+    std::uint64_t launches = 0;
+    double milliseconds = 0.0;
+    std::uint64_t bytes = 0;
+};
+
+struct ExecutorStats {
+    std::uint64_t launches = 0;        // kernel launches issued
+    std::uint64_t plane_tasks = 0;
+    std::uint64_t plan_uploads = 0;
+    std::size_t device_plan_bytes = 0;
+    std::size_t workspace_bytes = 0;
+};
+
+class Executor {
+public:
+    explicit Executor(int device = -1);
+    ~Executor();
+    Executor(const Executor &) = delete;
+    Executor &operator=(const Executor &) = delete;
+
+    [[nodiscard]] int device() const noexcept;
+
+    // Uploads the plan's coefficients once; later calls with the same plan
+    // object reuse them (keyed by identity, kept alive by the executor).
+    void prepare(std::shared_ptr<const AxisPlan> plan);
+    void seal();
+
+    // Synchronous host-frame calls (reference Executor contract).
+    void inverse_rows(const AxisPlan &plan, const float *input, std::ptrdiff_t input_stride,
+                      float *output, std::ptrdiff_t output_stride, std::int32_t rows);
+    void inverse_columns(const AxisPlan &plan, const float *input, std::ptrdiff_t input_stride,
+                         float *output, std::ptrdiff_t output_stride, std::int32_t columns);
+    void inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
+                    const void *input, std::ptrdiff_t input_stride, void *output,
+                    std::ptrdiff_t output_stride, const IntegerConversion &conversion);
+
+    // Device-pointer batch: every task is enqueued on `stream` (null: the
+    // executor's own).  With `synchronize` the call waits and raises on a
+    // Float64 non-finite status; otherwise check_status() does that later.
+    void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize);
+    void check_status(void *stream);
+
+    [[nodiscard]] ExecutorStats stats() const;
+
+    // Records CUDA events around every launch while enabled (enabling
+    // clears earlier records); kernel_times() waits for them.
+    void set_profiling(bool enable);
+    [[nodiscard]] std::vector<KernelTime> kernel_times();
+
+    struct Impl;
+
+private:
+    std::unique_ptr<Impl> impl_;
+};
+
+} // namespace dsmvc_gb

@@ -1,0 +1,389 @@
+"""Python binding of the GB300 descale executor's C ABI (include/dsmvc_gb300.h).
+
+The shared library ``libdsmvc_gb300.so`` (built in-tree by ``build.py``)
+holds the host planner and the CUDA executor; this module only marshals
+arguments.  There is no CPU fallback: executor calls raise when the library
+or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdsmvc_gb300.so")
+
+KERNELS = {"bilinear": 0, "bicubic": 1, "lanczos": 2, "spline16": 3,
+           "spline36": 4, "spline64": 5, "custom": 6}
+BORDERS = {"zero": 0, "repeat": 1, "reflect101": 2, "symmetric": 3, "mirror": 4}
+SAMPLES = {np.dtype(np.float32): 0, np.dtype(np.uint8): 1, np.dtype(np.uint16): 2}
+
+OK, INVALID_ARGUMENT, RUNTIME_ERROR, LENGTH_ERROR, CUDA_ERROR, OUT_OF_MEMORY, UNAVAILABLE = range(7)
+
+
+class DescaleError(RuntimeError):
+    """Error raised by the executor; ``code`` is the C status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+_EXC = {INVALID_ARGUMENT: ValueError, LENGTH_ERROR: OverflowError,
+        OUT_OF_MEMORY: MemoryError}
+
+
+class AxisRequestC(C.Structure):
+    _fields_ = [("source_size", C.c_int32), ("destination_size", C.c_int32),
+                ("active_length", C.c_double), ("shift", C.c_double),
+                ("kernel", C.c_int32), ("taps", C.c_int32), ("b", C.c_double),
+                ("c", C.c_double), ("blur", C.c_double), ("border", C.c_int32),
+                ("f64_mode", C.c_int32)]
+
+
+class ConversionC(C.Structure):
+    _fields_ = [("input_offset", C.c_float), ("input_scale", C.c_float),
+                ("output_scale", C.c_float), ("output_offset", C.c_float),
+                ("output_maximum", C.c_uint32)]
+
+
+class PlanInfoC(C.Structure):
+    _fields_ = [("source_size", C.c_int32), ("destination_size", C.c_int32),
+                ("support", C.c_int32), ("half_bandwidth", C.c_int32),
+                ("requires_float64", C.c_int32), ("max_row_entries", C.c_int32),
+                ("active_length", C.c_double), ("shift", C.c_double),
+                ("normal_rcond", C.c_double), ("normal_inf_norm", C.c_double),
+                ("nonzeros", C.c_uint64), ("storage_bytes", C.c_uint64)]
+
+
+class PlannerStatsC(C.Structure):
+    _fields_ = [("plan_hits", C.c_uint64), ("plan_builds", C.c_uint64),
+                ("plan_entries", C.c_uint64), ("plan_resident_bytes", C.c_uint64)]
+
+
+class ExecutorStatsC(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("plane_tasks", C.c_uint64),
+                ("plan_uploads", C.c_uint64), ("device_plan_bytes", C.c_uint64),
+                ("workspace_bytes", C.c_uint64)]
+
+
+class PlaneTaskC(C.Structure):
+    _fields_ = [("horizontal", C.c_void_p), ("vertical", C.c_void_p),
+                ("input", C.c_void_p), ("input_stride", C.c_int64),
+                ("output", C.c_void_p), ("output_stride", C.c_int64),
+                ("sample", C.c_int32), ("vectors", C.c_int32),
+                ("conversion", ConversionC)]
+
+
+class KernelTimeC(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("launches", C.c_uint64),
+                ("milliseconds", C.c_double), ("bytes", C.c_uint64)]
+
+
+CUSTOM_FN = C.CFUNCTYPE(C.c_double, C.c_double, C.c_void_p)
+
+# Every symbol the header declares, with its ctypes signature.
+SIGNATURES = {
+    "dsmvc_gb_last_error": ([], C.c_char_p),
+    "dsmvc_gb_abi_version": ([], C.c_int),
+    "dsmvc_gb_cuda_available": ([], C.c_int),
+    "dsmvc_gb_plan_build": ([C.POINTER(AxisRequestC), CUSTOM_FN, C.c_void_p,
+                             C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_plan_get_or_build": ([C.POINTER(AxisRequestC), CUSTOM_FN, C.c_void_p,
+                                    C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_plan_release": ([C.c_void_p], None),
+    "dsmvc_gb_plan_get_info": ([C.c_void_p, C.POINTER(PlanInfoC)], C.c_int),
+    "dsmvc_gb_plan_get_array": ([C.c_void_p, C.c_int32, C.POINTER(C.c_void_p),
+                                 C.POINTER(C.c_uint64)], C.c_int),
+    "dsmvc_gb_plan_hashes": ([C.c_void_p, C.POINTER(AxisRequestC), C.POINTER(C.c_uint64),
+                              C.POINTER(C.c_uint64)], C.c_int),
+    "dsmvc_gb_planner_cache_stats": ([C.POINTER(PlannerStatsC)], C.c_int),
+    "dsmvc_gb_clear_planner_caches": ([], None),
+    "dsmvc_gb_executor_create": ([C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_executor_destroy": ([C.c_void_p], None),
+    "dsmvc_gb_prepare": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_seal": ([C.c_void_p], C.c_int),
+    "dsmvc_gb_executor_get_stats": ([C.c_void_p, C.POINTER(ExecutorStatsC)], C.c_int),
+    "dsmvc_gb_inverse_rows": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                               C.c_int64, C.c_int32], C.c_int),
+    "dsmvc_gb_inverse_columns": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                  C.c_void_p, C.c_int64, C.c_int32], C.c_int),
+    "dsmvc_gb_inverse_2d": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                             C.c_void_p, C.c_int64], C.c_int),
+    "dsmvc_gb_inverse_2d_u8": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                C.c_void_p, C.c_int64, C.POINTER(ConversionC)], C.c_int),
+    "dsmvc_gb_inverse_2d_u16": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                 C.c_void_p, C.c_int64, C.POINTER(ConversionC)], C.c_int),
+    "dsmvc_gb_run_batch": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_void_p,
+                            C.c_int32], C.c_int),
+    "dsmvc_gb_stream_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
+    "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
+                               C.POINTER(C.c_int32)], C.c_int),
+}
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the library in-tree (see ../build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_dsmvc_gb300_build", os.path.join(os.path.dirname(HERE), "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """Load libdsmvc_gb300.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run build.py (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(code: int) -> None:
+    if code != OK:
+        msg = lib().dsmvc_gb_last_error().decode(errors="replace")
+        cls = _EXC.get(code)
+        if cls is not None:
+            raise cls(msg)
+        raise DescaleError(code, msg)
+
+
+def cuda_available() -> bool:
+    return bool(lib().dsmvc_gb_cuda_available())
+
+
+@dataclass(frozen=True)
+class AxisRequest:
+    """AxisRequest (include/dsmvc/engine.hpp:68-76)."""
+    source_size: int
+    destination_size: int
+    active_length: float
+    shift: float = 0.0
+    kernel: str = "bicubic"
+    taps: int = 3
+    b: float = 0.0
+    c: float = 0.5
+    blur: float = 1.0
+    border: str = "symmetric"
+    f64_mode: int = 0
+
+    def to_c(self) -> AxisRequestC:
+        return AxisRequestC(int(self.source_size), int(self.destination_size),
+                            float(self.active_length), float(self.shift),
+                            KERNELS[self.kernel] if isinstance(self.kernel, str) else int(self.kernel),
+                            int(self.taps), float(self.b), float(self.c), float(self.blur),
+                            BORDERS[self.border] if isinstance(self.border, str) else int(self.border),
+                            int(self.f64_mode))
+
+
+class AxisPlan:
+    """A host plan handle (shared, immutable)."""
+
+    _ARRAYS = [("transpose_offsets", np.uint32), ("transpose_indices", np.int32),
+               ("transpose_weights", np.float32), ("lower_ld", np.float32),
+               ("upper_l", np.float32), ("inverse_diagonal", np.float32),
+               ("transpose_weights_f64", np.float64), ("normal_bands_f64", np.float64),
+               ("ldlt_bands_f64", np.float64), ("inverse_diagonal_f64", np.float64)]
+
+    def __init__(self, request: AxisRequest, custom: Optional[Callable[[float], float]] = None,
+                 cached: bool = True):
+        self.request = request
+        self._req_c = request.to_c()
+        self._custom = CUSTOM_FN(lambda x, _u: float(custom(x))) if custom else CUSTOM_FN()
+        h = C.c_void_p()
+        fn = lib().dsmvc_gb_plan_get_or_build if cached else lib().dsmvc_gb_plan_build
+        _check(fn(C.byref(self._req_c), self._custom, None, C.byref(h)))
+        self._h = h
+        info = PlanInfoC()
+        _check(lib().dsmvc_gb_plan_get_info(h, C.byref(info)))
+        for name, _ in info._fields_:
+            setattr(self, name, getattr(info, name))
+        self.requires_float64 = bool(info.requires_float64)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def array(self, name: str) -> np.ndarray:
+        for i, (n, dt) in enumerate(self._ARRAYS):
+            if n == name:
+                ptr, count = C.c_void_p(), C.c_uint64()
+                _check(lib().dsmvc_gb_plan_get_array(self._h, i, C.byref(ptr), C.byref(count)))
+                if count.value == 0:
+                    return np.zeros(0, dt)
+                nbytes = count.value * np.dtype(dt).itemsize
+                return np.frombuffer((C.c_char * nbytes).from_address(ptr.value), dt).copy()
+        raise KeyError(name)
+
+    def hashes(self):
+        f, c = C.c_uint64(), C.c_uint64()
+        _check(lib().dsmvc_gb_plan_hashes(self._h, C.byref(self._req_c), C.byref(f), C.byref(c)))
+        return "%016x" % f.value, "%016x" % c.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.dsmvc_gb_plan_release(h)
+            self._h = None
+
+
+def planner_cache_stats() -> dict:
+    s = PlannerStatsC()
+    _check(lib().dsmvc_gb_planner_cache_stats(C.byref(s)))
+    return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+def clear_planner_caches() -> None:
+    lib().dsmvc_gb_clear_planner_caches()
+
+
+def _conv(conversion) -> ConversionC:
+    if conversion is None:
+        return ConversionC(0.0, 1.0, 1.0, 0.0, 255)
+    if isinstance(conversion, ConversionC):
+        return conversion
+    return ConversionC(*[float(x) for x in conversion[:4]], int(conversion[4]))
+
+
+@dataclass
+class PlaneTask:
+    """One device plane of a batch (pointers are device addresses)."""
+    horizontal: Optional[AxisPlan]
+    vertical: Optional[AxisPlan]
+    input: int
+    input_stride: int
+    output: int
+    output_stride: int
+    sample: int = 0
+    vectors: int = 0
+    conversion: object = None
+
+
+class Executor:
+    """CudaExecutor equivalent (src/cuda/cuda_executor.hpp:11-110)."""
+
+    def __init__(self, device: int = -1):
+        h = C.c_void_p()
+        _check(lib().dsmvc_gb_executor_create(int(device), C.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
+            _lib.dsmvc_gb_executor_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def prepare(self, plan: AxisPlan) -> None:
+        _check(lib().dsmvc_gb_prepare(self._h, plan.handle))
+        self._keep.append(plan)
+
+    def seal(self) -> None:
+        _check(lib().dsmvc_gb_seal(self._h))
+
+    def stats(self) -> dict:
+        s = ExecutorStatsC()
+        _check(lib().dsmvc_gb_executor_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    # -- synchronous host calls --------------------------------------------
+    def inverse_rows(self, plan: AxisPlan, x: np.ndarray, out: Optional[np.ndarray] = None):
+        x = np.asarray(x, np.float32)
+        if out is None:
+            out = np.empty((x.shape[0], plan.destination_size), np.float32)
+        _check(lib().dsmvc_gb_inverse_rows(self._h, plan.handle, x.ctypes.data,
+                                           x.strides[0] // 4, out.ctypes.data,
+                                           out.strides[0] // 4, x.shape[0]))
+        return out
+
+    def inverse_columns(self, plan: AxisPlan, x: np.ndarray, out: Optional[np.ndarray] = None):
+        x = np.asarray(x, np.float32)
+        if out is None:
+            out = np.empty((plan.destination_size, x.shape[1]), np.float32)
+        _check(lib().dsmvc_gb_inverse_columns(self._h, plan.handle, x.ctypes.data,
+                                              x.strides[0] // 4, out.ctypes.data,
+                                              out.strides[0] // 4, x.shape[1]))
+        return out
+
+    def inverse_2d(self, h: AxisPlan, v: AxisPlan, x: np.ndarray, conversion=None,
+                   out: Optional[np.ndarray] = None):
+        """inverse_2d / inverse_2d_u8 / inverse_2d_u16 on a host plane; row
+        strides come from the arrays (padding is never touched)."""
+        assert x.strides[1] == x.itemsize, "rows must be contiguous"
+        if out is None:
+            out = np.empty((v.destination_size, h.destination_size), x.dtype)
+        es = x.itemsize
+        if x.dtype == np.float32:
+            _check(lib().dsmvc_gb_inverse_2d(self._h, h.handle, v.handle, x.ctypes.data,
+                                             x.strides[0] // es, out.ctypes.data,
+                                             out.strides[0] // es))
+        elif x.dtype in (np.uint8, np.uint16):
+            fn = lib().dsmvc_gb_inverse_2d_u8 if x.dtype == np.uint8 else lib().dsmvc_gb_inverse_2d_u16
+            conv = _conv(conversion)
+            _check(fn(self._h, h.handle, v.handle, x.ctypes.data, x.strides[0] // es,
+                      out.ctypes.data, out.strides[0] // es, C.byref(conv)))
+        else:
+            raise ValueError(f"unsupported sample type {x.dtype}")
+        return out
+
+    # -- device-resident batches ------------------------------------------
+    def run_batch(self, tasks: Sequence[PlaneTask], stream: int = 0, synchronize: bool = True):
+        arr = (PlaneTaskC * len(tasks))()
+        for i, t in enumerate(tasks):
+            arr[i] = PlaneTaskC(t.horizontal.handle if t.horizontal else None,
+                                t.vertical.handle if t.vertical else None,
+                                int(t.input), int(t.input_stride), int(t.output),
+                                int(t.output_stride), int(t.sample), int(t.vectors),
+                                _conv(t.conversion))
+        _check(lib().dsmvc_gb_run_batch(self._h, arr, len(tasks), C.c_void_p(stream or None),
+                                        1 if synchronize else 0))
+
+    def stream_check(self, stream: int = 0) -> None:
+        _check(lib().dsmvc_gb_stream_check(self._h, C.c_void_p(stream or None)))
+
+    def profile(self, enable: bool) -> None:
+        _check(lib().dsmvc_gb_profile(self._h, 1 if enable else 0))
+
+    def kernel_times(self) -> list:
+        """[{name, launches, milliseconds, bytes}] since profile(True)."""
+        buf = (KernelTimeC * 64)()
+        n = C.c_int32()
+        _check(lib().dsmvc_gb_profile_read(self._h, buf, 64, C.byref(n)))
+        return [{"name": buf[i].name.decode(), "launches": buf[i].launches,
+                 "milliseconds": buf[i].milliseconds, "bytes": buf[i].bytes}
+                for i in range(min(n.value, 64))]
+
+
+def integer_conversion(bits: int, chroma: bool, full_range: bool) -> tuple:
+    """integer_conversion (src/vs_plugin.cpp:761-782): returns
+    (input_offset, input_scale, output_scale, output_offset, output_maximum)."""
+    maximum = (1 << bits) - 1
+    offset, scale = 0, maximum
+    if not full_range:
+        depth = 1 << (bits - 8)
+        offset = (128 if chroma else 16) * depth
+        scale = (224 if chroma else 219) * depth
+    elif chroma:
+        offset = 1 << (bits - 1)
+    return (float(offset), float(np.float32(1.0) / np.float32(scale)), float(scale),
+            float(offset), maximum)
+
+
+from .plugin import (Debicubic, Debilinear, Delanczos, Descale, Despline16,  # noqa: E402
+                     Despline36, Despline64, Frame, VideoFormat)
