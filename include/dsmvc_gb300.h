@@ -159,6 +159,26 @@ int dsmvc_gb_plan_get_array(const dsmvc_gb_plan *plan, int32_t which,
 int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan,
                          const dsmvc_gb_axis_request *request,
                          uint64_t *f32_hash, uint64_t *complete_hash);
+/* Which kernel family a Float32 plan runs on, and the packed records of the
+ * streaming kernels (no reference counterpart: the reference's equivalent
+ * choice is solve_partition::choose, src/solve_partition.cpp:32-57).
+ * `forward`/`backward` may be NULL to query the sizes only. */
+typedef struct dsmvc_gb_stream_info {
+    int32_t eligible;            /* streaming kernels usable */
+    int32_t window;              /* dense gather window */
+    int32_t forward_stride;      /* floats per forward record */
+    int32_t backward_stride;     /* floats per backward record */
+    int32_t ring_ok_u16;         /* 16-byte u16 row loads fit the ring */
+    int32_t ring_ok_u8;          /* 16-byte u8 row loads fit the ring */
+    int32_t chunk;               /* destinations per register chunk */
+    int32_t ring;                /* source samples per thread ring */
+    double backward_transfer;    /* carry influence after one chunk */
+    char reason[96];             /* why not eligible */
+} dsmvc_gb_stream_info;
+int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
+                              dsmvc_gb_stream_info *info, float *forward,
+                              uint64_t forward_capacity, float *backward,
+                              uint64_t backward_capacity);
 /* planner_cache_stats / clear_planner_caches (engine.hpp:179-180). */
 int dsmvc_gb_planner_cache_stats(dsmvc_gb_planner_stats *out);
 void dsmvc_gb_clear_planner_caches(void);

@@ -36,3 +36,21 @@ def executor(gb):
     ex = gb.Executor(0)
     yield ex
     ex.close()
+
+
+@pytest.fixture(scope="session")
+def seq_executor(gb):
+    """An executor pinned to the sequential kernels (DSMVC_GB_STREAM=0)."""
+    if not gb.cuda_available():
+        pytest.skip("no CUDA device")
+    old = os.environ.get("DSMVC_GB_STREAM")
+    os.environ["DSMVC_GB_STREAM"] = "0"
+    try:
+        ex = gb.Executor(0)
+    finally:
+        if old is None:
+            del os.environ["DSMVC_GB_STREAM"]
+        else:
+            os.environ["DSMVC_GB_STREAM"] = old
+    yield ex
+    ex.close()

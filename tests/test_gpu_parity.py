@@ -5,6 +5,9 @@ Bars (written into each test):
     the reference CUDA operation order (fmaf chains), and within the
     reference's Float32 tolerance of the CPU scalar route (max-abs 2e-5,
     mean-abs 1e-6, tests/vs_gpu_concurrency.py:57);
+  * streaming kernels (chunk-delayed backward pass), Float32: within
+    STREAM_REL (4e-7) of the largest output magnitude of that same CUDA-order
+    result, and within the reference tolerance of the CPU scalar route;
   * integer output: within 1 code of the CPU scalar route;
   * Float64 route: equal to the CPU scalar Float64 route (<= 1 float ULP is
     the contract; the kernels reproduce its operation order exactly).
@@ -17,6 +20,8 @@ from common import (F32_MAX_ABS, F32_MEAN_ABS, INT_MAX_CODES, load_golden, make_
                     max_ulp, oracle_request, product_request)
 
 pytestmark = pytest.mark.gpu
+
+STREAM_REL = 4e-7   # streaming vs sequential CUDA order, relative to max |x|
 
 
 def plans(gb, executor, req, prepare=True):
@@ -44,7 +49,8 @@ HB_CASES = [
 
 
 @pytest.mark.parametrize("name,req", HB_CASES, ids=[c[0] for c in HB_CASES])
-def test_rows_and_columns_bit_exact(gb, executor, name, req):
+def test_rows_and_columns_bit_exact(gb, seq_executor, name, req):
+    executor = seq_executor
     p, o = plans(gb, executor, req)
     x = image(37, p.source_size, 1)
     got = executor.inverse_rows(p, x)
@@ -69,27 +75,37 @@ CASES_2D = [
 
 
 @pytest.mark.parametrize("name,hq,vq", CASES_2D, ids=[c[0] for c in CASES_2D])
-def test_2d_float32(gb, executor, name, hq, vq):
-    h, oh = plans(gb, executor, hq)
-    v, ov = plans(gb, executor, vq)
+def test_2d_float32(gb, executor, seq_executor, name, hq, vq):
+    h, oh = plans(gb, seq_executor, hq)
+    v, ov = plans(gb, seq_executor, vq)
+    executor.prepare(h)
+    executor.prepare(v)
     x = image(v.source_size, h.source_size, 3)
-    got = executor.inverse_2d(h, v, x)
-    assert np.array_equal(got, O.inverse_2d_gpu_order(oh, ov, x))
+    exact = O.inverse_2d_gpu_order(oh, ov, x)
     scalar = O.inverse_2d(oh, ov, x)
-    err = np.abs(got.astype(np.float64) - scalar)
-    assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+    seq = seq_executor.inverse_2d(h, v, x)
+    assert np.array_equal(seq, exact)
+    got = executor.inverse_2d(h, v, x)
+    assert np.max(np.abs(got - exact)) <= STREAM_REL * np.max(np.abs(exact))
+    for y in (seq, got):
+        err = np.abs(y.astype(np.float64) - scalar)
+        assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
 
 
 @pytest.mark.parametrize("sample", ["u8", "u16"])
 @pytest.mark.parametrize("name,hq,vq", CASES_2D[:3], ids=[c[0] for c in CASES_2D[:3]])
-def test_2d_integer(gb, executor, sample, name, hq, vq):
-    h, oh = plans(gb, executor, hq)
-    v, ov = plans(gb, executor, vq)
+def test_2d_integer(gb, executor, seq_executor, sample, name, hq, vq):
+    h, oh = plans(gb, seq_executor, hq)
+    v, ov = plans(gb, seq_executor, vq)
+    executor.prepare(h)
+    executor.prepare(v)
     x = make_input(v.source_size, h.source_size, sample, 11)
     bits = 8 if sample == "u8" else 16
     conv = gb.integer_conversion(bits, chroma=False, full_range=False)
+    exact = O.inverse_2d_gpu_order(oh, ov, x, conv)
+    assert np.array_equal(seq_executor.inverse_2d(h, v, x, conv), exact)
     got = executor.inverse_2d(h, v, x, conv)
-    assert np.array_equal(got, O.inverse_2d_gpu_order(oh, ov, x, conv))
+    assert np.max(np.abs(got.astype(np.int64) - exact.astype(np.int64))) <= INT_MAX_CODES
     scalar = O.inverse_2d(oh, ov, x, conv)
     assert np.max(np.abs(got.astype(np.int64) - scalar.astype(np.int64))) <= INT_MAX_CODES
 
@@ -162,6 +178,56 @@ def test_strides_and_padding_are_respected(gb, executor):
     executor.inverse_2d(h, v, xin[:, :h.source_size], out=out[:, :h.destination_size])
     assert np.all(out[:, h.destination_size:] == -777.0)
     assert np.array_equal(out[:, :h.destination_size], O.inverse_2d_gpu_order(oh, ov, x))
+
+
+def test_strides_and_padding_streaming(gb, executor):
+    hq, vq = CASES_2D[1][1], CASES_2D[1][2]
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = make_input(v.source_size, h.source_size, "u16", 31)
+    conv = gb.integer_conversion(16, chroma=False, full_range=False)
+    xin = np.full((v.source_size, h.source_size + 8), 0xFFFF, np.uint16)
+    xin[:, :h.source_size] = x
+    out = np.full((v.destination_size, h.destination_size + 5), 0xBEEF, np.uint16)
+    executor.inverse_2d(h, v, xin[:, :h.source_size], conv, out=out[:, :h.destination_size])
+    assert np.all(out[:, h.destination_size:] == 0xBEEF)
+    scalar = O.inverse_2d(oh, ov, x, conv)
+    assert np.max(np.abs(out[:, :h.destination_size].astype(np.int64) - scalar)) <= INT_MAX_CODES
+
+
+FULL = [
+    ("c1-luma-lanczos3-u16", (1920, 1440, 1440.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0),
+     (1080, 810, 810.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), "u16"),
+    ("c1-chroma-lanczos3-u16", (960, 720, 720.0, 0.25 - 0.25 * 1440 / 1920, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0),
+     (540, 405, 405.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), "u16"),
+    ("c0-bicubic-f32", (1920, 1280, 1280.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1),
+     (1080, 720, 720.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1), "f32"),
+]
+
+
+@pytest.mark.parametrize("name,hq,vq,sample", FULL, ids=[c[0] for c in FULL])
+def test_full_size_frames_use_streaming_kernels(gb, executor, name, hq, vq, sample):
+    """Full-size frames of the benchmark configurations: the streaming
+    kernels run (profiled kernel names) and agree with the CPU scalar route
+    within the reference tolerance."""
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    assert h.stream_info()["eligible"] and v.stream_info()["eligible"]
+    x = make_input(v.source_size, h.source_size, sample, 41) if sample != "f32" else \
+        image(v.source_size, h.source_size, 41)
+    conv = gb.integer_conversion(16, chroma="chroma" in name, full_range=False) if sample != "f32" else None
+    executor.profile(True)
+    got = executor.inverse_2d(h, v, x, conv)
+    names = {k["name"] for k in executor.kernel_times()}
+    executor.profile(False)
+    assert any(n.startswith("stream_f32/rows") for n in names), names
+    assert any(n.startswith("stream_f32/columns") for n in names), names
+    scalar = O.inverse_2d(oh, ov, x, conv)
+    if sample == "f32":
+        err = np.abs(got.astype(np.float64) - scalar)
+        assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+    else:
+        assert np.max(np.abs(got.astype(np.int64) - scalar.astype(np.int64))) <= INT_MAX_CODES
 
 
 def test_unprepared_plans_still_run(gb, executor):

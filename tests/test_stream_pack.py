@@ -1,0 +1,128 @@
+"""Host logic of the streaming kernels (CPU): eligibility, record layout, and
+a numpy emulation of the kernel's algorithm on the packed records (exact
+forward pass, chunk-delayed backward pass with a zero-carry warm-up) checked
+against the oracle's reference CUDA operation order."""
+import numpy as np
+import pytest
+
+import oracle as O
+from common import oracle_request, product_request
+
+
+def fma32(a, b, c):
+    return (np.float64(a) * np.float64(b) + np.float64(c)).astype(np.float32)
+
+
+def emulate(info, plan, x):
+    """x: (vectors, m) float32 -> (vectors, n) float32, kernel algorithm."""
+    fwd, bwd = info["forward"], info["backward"]
+    K, hb, n, LC = info["window"], plan.half_bandwidth, plan.destination_size, info["chunk"]
+    V = x.shape[0]
+    y = np.zeros((V, n), np.float32)
+    for j in range(n):
+        rec = fwd[j]
+        s0 = int(rec[:1].view(np.int32)[0])
+        s = np.zeros(V, np.float32)
+        for k in range(K):
+            s = fma32(rec[4 + k], x[:, s0 + k], s)
+        for q in range(hb):
+            d = hb - q
+            prev = y[:, j - d] if j - d >= 0 else np.zeros(V, np.float32)
+            s = fma32(rec[4 + K + q], prev, s)
+        y[:, j] = s * rec[1]
+
+    def back(lo, hi, carry, yv):
+        """Backward over [lo, hi) from carry (x_{hi..hi+hb-1}); returns x."""
+        xs = {hi + e: carry[e] for e in range(hb)}
+        out = {}
+        for j in range(hi - 1, lo - 1, -1):
+            s = np.zeros(V, np.float32)
+            if j < n:
+                for q in range(hb):
+                    d = q + 1 if hb == 3 else hb - q
+                    s = fma32(bwd[j, q], xs.get(j + d, np.zeros(V, np.float32)), s)
+                v = (yv[:, j] - s).astype(np.float32)
+            else:
+                v = np.zeros(V, np.float32)
+            xs[j] = v
+            out[j] = v
+        return out
+
+    chunks = (n + LC - 1) // LC
+    zero = [np.zeros(V, np.float32)] * hb
+    res = np.zeros((V, n), np.float32)
+    for c in range(chunks):
+        lo, hi = c * LC, (c + 1) * LC
+        if c == chunks - 1:
+            carry = zero
+        elif c + 1 == chunks - 1:
+            nxt = back(hi, hi + LC, zero, y)
+            carry = [nxt[hi + e] if hi + e < n else np.zeros(V, np.float32) for e in range(hb)]
+        else:
+            warm = back(hi, hi + LC, zero, y)
+            carry = [warm[hi + e] for e in range(hb)]
+        xs = back(lo, hi, carry, y)
+        for j in range(lo, min(hi, n)):
+            res[:, j] = xs[j]
+    return res
+
+
+CASES = [
+    ("lanczos3-1920-1440", (1920, 1440, 1440.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), True),
+    ("lanczos3-chroma-v", (540, 405, 405.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), True),
+    ("bicubic-1080-720", (1080, 720, 720.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1), True),
+    ("bilinear-odd", (201, 150, 149.5, 0.3, "bilinear", 3, 0, 0.5, 1.0, "zero", 0), True),
+    ("spline64-hb7", (300, 200, 200.0, -0.2, "spline64", 3, 0, 0.5, 1.0, "reflect101", 0), True),
+    ("short-single-chunk", (40, 30, 30.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "mirror", 0), True),
+    ("spline64-blur-hb9", (300, 200, 200.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0), False),
+    ("f64-forced", (100, 70, 70.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2), False),
+]
+
+
+@pytest.mark.parametrize("name,req,eligible", CASES, ids=[c[0] for c in CASES])
+def test_stream_eligibility_and_emulation(gb, name, req, eligible):
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info(records=True)
+    assert bool(info["eligible"]) == eligible, info["reason"]
+    if not eligible:
+        assert info["reason"]
+        return
+    assert info["backward_transfer"] <= 2.0 ** -26
+    o = O.Plan(oracle_request(req))
+    rng = np.random.default_rng(3)
+    x = rng.random((6, p.source_size), dtype=np.float32)
+    got = emulate(info, o, x)
+    want = np.stack([o.inverse_axis_f32_gpu(r) for r in x])
+    scale = float(np.max(np.abs(want)))
+    assert np.max(np.abs(got - want)) <= 4e-7 * scale
+    # The forward pass is exact: the last chunk's outputs equal the oracle's.
+    last = (p.destination_size - 1) // info["chunk"] * info["chunk"]
+    assert np.max(np.abs(got[:, last:] - want[:, last:])) <= 2e-7 * scale
+
+
+def test_record_layout(gb):
+    req = (47, 39, 39.0, -0.3125, "bicubic", 3, 0, 0.5, 1.0, "reflect101", 1)
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info(records=True)
+    assert info["eligible"] and info["window"] % 4 == 0
+    off = p.array("transpose_offsets")
+    idx = p.array("transpose_indices")
+    w = p.array("transpose_weights")
+    lower = p.array("lower_ld").reshape(p.half_bandwidth, -1)
+    upper = p.array("upper_l").reshape(p.half_bandwidth, -1)
+    K, hb = info["window"], p.half_bandwidth
+    prev = 0
+    for j in range(p.destination_size):
+        rec = info["forward"][j]
+        s0 = int(rec[:1].view(np.int32)[0])
+        assert s0 >= prev and 0 <= s0 <= p.source_size - K
+        prev = s0
+        dense = np.zeros(K, np.float32)
+        dense[idx[off[j]:off[j + 1]] - s0] = w[off[j]:off[j + 1]]
+        assert np.array_equal(rec[4:4 + K], dense)
+        assert rec[1] == p.array("inverse_diagonal")[j]
+        for q in range(hb):
+            d = hb - q
+            assert rec[4 + K + q] == (-lower[d - 1, j] if d <= j else 0.0)
+            du = q + 1  # half-bandwidth 3: ascending
+            assert info["backward"][j, q] == (upper[du - 1, j] if du <= min(hb, p.destination_size - j - 1) else 0.0)

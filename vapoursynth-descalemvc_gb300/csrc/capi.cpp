@@ -4,6 +4,10 @@
 
 #include "executor.hpp"
 #include "planner.hpp"
+#include "stream.cuh"
+#include "stream_plan.hpp"
+
+#include <algorithm>
 
 #include <cuda_runtime.h>
 
@@ -187,6 +191,31 @@ int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan, const dsmvc_gb_axis_request 
         const auto q = request ? to_request(request) : plan->request;
         if (f32_hash) *f32_hash = dsmvc_gb::f32_plan_hash(q, p);
         if (complete_hash) *complete_hash = dsmvc_gb::complete_plan_hash(q, p);
+    });
+}
+
+int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *info, float *forward,
+                              uint64_t forward_capacity, float *backward, uint64_t backward_capacity) {
+    return guarded([&] {
+        const auto &p = plan_of(plan);
+        if (!info) throw std::invalid_argument("output is null");
+        const auto pack = dsmvc_gb::pack_stream_plan(p, dsmvc_gb::kStreamChunk, dsmvc_gb::kStreamRing,
+                                                     dsmvc_gb::stream_supports(p.half_bandwidth));
+        *info = {};
+        info->eligible = pack.eligible ? 1 : 0;
+        info->window = pack.window;
+        info->forward_stride = pack.forward_stride;
+        info->backward_stride = pack.backward_stride;
+        info->ring_ok_u16 = pack.ring_ok_u16 ? 1 : 0;
+        info->ring_ok_u8 = pack.ring_ok_u8 ? 1 : 0;
+        info->chunk = dsmvc_gb::kStreamChunk;
+        info->ring = dsmvc_gb::kStreamRing;
+        info->backward_transfer = pack.backward_transfer;
+        std::snprintf(info->reason, sizeof(info->reason), "%s", pack.reason.c_str());
+        if (forward && forward_capacity >= pack.forward.size())
+            std::copy(pack.forward.begin(), pack.forward.end(), forward);
+        if (backward && backward_capacity >= pack.backward.size())
+            std::copy(pack.backward.begin(), pack.backward.end(), backward);
     });
 }
 

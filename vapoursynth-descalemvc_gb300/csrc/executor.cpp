@@ -11,6 +11,8 @@
 // destination column) into the output, with integer conversion fused into
 // the load of the first pass and the store of the second.
 #include "executor.hpp"
+#include "stream.cuh"
+#include "stream_plan.hpp"
 
 #include <cuda_runtime.h>
 
@@ -23,6 +25,7 @@
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <cstdlib>
 #include <unordered_map>
 
 namespace dsmvc_gb {
@@ -75,6 +78,10 @@ struct DevicePlan {
     std::shared_ptr<const AxisPlan> keep;
     DeviceBuffer memory;
     dev::PlanView view{};
+    // Streaming-kernel records (when the plan qualifies, stream_plan.hpp).
+    bool stream = false;
+    bool stream_u16 = false, stream_u8 = false;
+    dev::StreamPlanView stream_view{};
     std::size_t bytes = 0;
 };
 
@@ -92,6 +99,12 @@ std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
         {f64 ? p.transpose_weights_f64.data() : nullptr, f64 ? p.transpose_weights_f64.size() * 8 : 0},
         {f64 ? p.ldlt_bands_f64.data() : nullptr, f64 ? p.ldlt_bands_f64.size() * 8 : 0},
     };
+    const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing,
+                                             stream_supports(p.half_bandwidth));
+    if (pack.eligible) {
+        parts.push_back({pack.forward.data(), pack.forward.size() * 4});
+        parts.push_back({pack.backward.data(), pack.backward.size() * 4});
+    }
     std::size_t total = 0;
     std::vector<std::size_t> offsets;
     for (auto &part : parts) {
@@ -118,6 +131,20 @@ std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
     v.inv_diag = reinterpret_cast<const float *>(base + offsets[5]);
     v.weights64 = f64 ? reinterpret_cast<const double *>(base + offsets[6]) : nullptr;
     v.bands64 = f64 ? reinterpret_cast<const double *>(base + offsets[7]) : nullptr;
+    if (pack.eligible) {
+        dp->stream = true;
+        dp->stream_u16 = pack.ring_ok_u16;
+        dp->stream_u8 = pack.ring_ok_u8;
+        auto &sv = dp->stream_view;
+        sv.source_size = p.source_size;
+        sv.destination_size = p.destination_size;
+        sv.half_bandwidth = p.half_bandwidth;
+        sv.window = pack.window;
+        sv.forward_stride = pack.forward_stride;
+        sv.backward_stride = pack.backward_stride;
+        sv.forward = reinterpret_cast<const float *>(base + offsets[8]);
+        sv.backward = reinterpret_cast<const float *>(base + offsets[9]);
+    }
     dp->bytes = total;
     dp->keep = std::move(plan);
     return dp;
@@ -133,7 +160,7 @@ struct Workspace {
     DeviceBuffer jobs;
     std::uint32_t *status = nullptr;      // device
     std::uint32_t *status_host = nullptr; // pinned
-    std::vector<dev::AxisJob> host_jobs;
+    std::vector<char> host_table;
 
     explicit Workspace(cudaStream_t s) : stream(s) {
         if (!stream) {
@@ -187,18 +214,22 @@ struct Executor::Impl {
         std::uint64_t bytes = 0;
     };
     bool profiling = false;
+    // DSMVC_GB_STREAM=0 keeps every plan on the sequential kernels (the
+    // counterpart of the reference's DSMVC_GPU_SOLVE_PARTITION switch).
+    bool allow_stream = true;
     std::vector<Record> records;
 
-    const dev::PlanView &view(const AxisPlan &plan, std::vector<std::unique_ptr<DevicePlan>> &temporaries) {
+    const DevicePlan &device_plan(const AxisPlan &plan,
+                                  std::vector<std::unique_ptr<DevicePlan>> &temporaries) {
         {
             std::scoped_lock lock(mutex);
-            if (auto it = plans.find(&plan); it != plans.end()) return it->second->view;
+            if (auto it = plans.find(&plan); it != plans.end()) return *it->second;
         }
         // Not prepared: upload a private copy for this call only.
         temporaries.push_back(upload_plan(std::make_shared<const AxisPlan>(plan)));
         std::scoped_lock lock(mutex);
         ++stats.plan_uploads;
-        return temporaries.back()->view;
+        return *temporaries.back();
     }
 
     Workspace &acquire_slot(std::size_t &index) {
@@ -242,13 +273,15 @@ struct Executor::Impl {
 
 namespace {
 
+// Launch groups: one launch per kernel variant, every job of a group shares
+// half-bandwidth and sample kinds.
 struct GroupKey {
-    int pass;      // 0 horizontal, 1 vertical
-    bool f64;
+    int pass;        // 0 first pass (rows), 1 second pass (columns)
+    int kind;        // 0 sequential Float32, 1 sequential Float64, 2 streaming
     int hb;
     dev::Sample in, out;
     bool operator<(const GroupKey &o) const {
-        return std::tie(pass, f64, hb, in, out) < std::tie(o.pass, o.f64, o.hb, o.in, o.out);
+        return std::tie(pass, kind, hb, in, out) < std::tie(o.pass, o.kind, o.hb, o.in, o.out);
     }
 };
 
@@ -256,164 +289,203 @@ dev::Conversion to_dev(const IntegerConversion &c) {
     return {c.input_offset, c.input_scale, c.output_scale, c.output_offset, c.output_maximum};
 }
 
+bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
+    if (!dp.stream) return false;
+    if (in == dev::Sample::u16) return dp.stream_u16;
+    if (in == dev::Sample::u8) return dp.stream_u8;
+    return in == dev::Sample::f32;
+}
+
+std::string kernel_name(const GroupKey &k) {
+    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32"};
+    return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
+}
+
 } // namespace
 
 void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks) {
     std::vector<std::unique_ptr<DevicePlan>> temporaries;
-    // Scratch layout: per task, an intermediate and a forward scratch.
-    struct Scratch { std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0; bool f64 = false; };
-    std::vector<Scratch> scratch(tasks.size());
+    // Per task: which kernels run each pass, and the scratch they need.
+    struct Route {
+        const DevicePlan *h = nullptr, *v = nullptr;
+        bool f64 = false, h_stream = false, v_stream = false;
+        std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0;
+    };
+    std::vector<Route> routes(tasks.size());
     std::size_t bytes = 0;
     for (std::size_t t = 0; t < tasks.size(); ++t) {
         const auto &task = tasks[t];
         const AxisPlan *h = task.horizontal, *v = task.vertical;
         if (!h && !v) throw std::invalid_argument("plane task without a plan");
-        auto &s = scratch[t];
-        s.f64 = (h && h->requires_float64()) || (v && v->requires_float64());
-        const std::size_t es = s.f64 ? 8 : 4;
+        auto &r = routes[t];
+        r.h = h ? &device_plan(*h, temporaries) : nullptr;
+        r.v = v ? &device_plan(*v, temporaries) : nullptr;
+        r.f64 = (h && h->requires_float64()) || (v && v->requires_float64());
+        if (!r.f64 && allow_stream) {
+            r.h_stream = r.h && stream_row_ok(*r.h, h && v ? task.sample : dev::Sample::f32);
+            r.v_stream = r.v && r.v->stream;
+        }
+        const std::size_t es = r.f64 ? 8 : 4;
         if (h && v) {
-            s.mid_stride = static_cast<std::size_t>(h->destination_size);
-            s.mid = bytes;
-            bytes += align_up(s.mid_stride * static_cast<std::size_t>(v->source_size) * es);
-            if (s.f64 || task.sample != dev::Sample::f32) {
-                s.fwd_stride = static_cast<std::size_t>(h->destination_size);
-                s.fwd = bytes;
-                bytes += align_up(s.fwd_stride * static_cast<std::size_t>(v->destination_size) * es);
+            r.mid_stride = static_cast<std::size_t>(h->destination_size);
+            r.mid = bytes;
+            bytes += align_up(r.mid_stride * static_cast<std::size_t>(v->source_size) * es);
+            if (r.f64 || (!r.v_stream && task.sample != dev::Sample::f32)) {
+                r.fwd_stride = static_cast<std::size_t>(h->destination_size);
+                r.fwd = bytes;
+                bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * es);
             }
-        } else if (s.f64) {
+        } else if (r.f64) {
             const AxisPlan *p = h ? h : v;
-            s.fwd_stride = h ? static_cast<std::size_t>(p->destination_size) : static_cast<std::size_t>(task.vectors);
+            r.fwd_stride = h ? static_cast<std::size_t>(p->destination_size) : static_cast<std::size_t>(task.vectors);
             const std::size_t lines = h ? static_cast<std::size_t>(task.vectors) : static_cast<std::size_t>(p->destination_size);
-            s.fwd = bytes;
-            bytes += align_up(s.fwd_stride * lines * 8);
+            r.fwd = bytes;
+            bytes += align_up(r.fwd_stride * lines * 8);
         }
     }
     ws.scratch.reserve(std::max<std::size_t>(bytes, kAlign));
     char *base = ws.scratch.data();
 
-    // Each job carries its compulsory bytes (input read by a first pass,
-    // output written by a last pass) for the roofline accounting.
-    std::map<GroupKey, std::vector<std::pair<dev::AxisJob, std::uint64_t>>> groups;
+    struct Item {
+        dev::AxisJob axis{};
+        dev::StreamJob stream{};
+        std::uint64_t bytes = 0;
+    };
+    std::map<GroupKey, std::vector<Item>> groups;
     for (std::size_t t = 0; t < tasks.size(); ++t) {
         const auto &task = tasks[t];
-        const auto &s = scratch[t];
+        const auto &r = routes[t];
         const AxisPlan *h = task.horizontal, *v = task.vertical;
         const dev::Conversion conv = to_dev(task.conversion);
-        const dev::Sample mid_kind = s.f64 ? dev::Sample::f64 : dev::Sample::f32;
+        const dev::Sample mid_kind = r.f64 ? dev::Sample::f64 : dev::Sample::f32;
+        const int seq_kind = r.f64 ? 1 : 0;
         if (h) {
-            dev::AxisJob j{};
-            j.plan = view(*h, temporaries);
-            j.in = task.input;
-            j.in_elem = 1;
-            j.in_vec = task.input_stride;
-            j.vectors = v ? v->source_size : task.vectors;
-            j.conv = conv;
-            GroupKey key{0, s.f64, h->half_bandwidth, task.sample, v ? mid_kind : task.sample};
-            if (v) {
-                j.out = base + s.mid;
-                j.out_elem = 1;
-                j.out_vec = static_cast<std::int64_t>(s.mid_stride);
-                j.fwd = j.out;
-                j.fwd_elem = 1;
-                j.fwd_vec = j.out_vec;
+            // Rows: source rows of the input, into the intermediate (2D) or
+            // the output (rows only).
+            const void *in = task.input;
+            const std::int64_t in_vec = task.input_stride;
+            void *out = v ? static_cast<void *>(base + r.mid) : task.output;
+            const std::int64_t out_vec = v ? static_cast<std::int64_t>(r.mid_stride) : task.output_stride;
+            const int vectors = v ? v->source_size : task.vectors;
+            const dev::Sample out_kind = v ? mid_kind : task.sample;
+            Item it;
+            it.bytes = static_cast<std::uint64_t>(vectors) * h->source_size * sample_bytes(task.sample);
+            if (!v) it.bytes += static_cast<std::uint64_t>(vectors) * h->destination_size * 4;
+            if (r.h_stream) {
+                auto &j = it.stream;
+                j.plan = r.h->stream_view;
+                j.in = in; j.in_elem = 1; j.in_vec = in_vec;
+                j.out = out; j.out_elem = 1; j.out_vec = out_vec;
+                j.vectors = vectors;
+                j.conv = conv;
+                groups[{0, 2, h->half_bandwidth, task.sample, out_kind}].push_back(it);
             } else {
-                j.out = task.output;
-                j.out_elem = 1;
-                j.out_vec = task.output_stride;
-                if (s.f64) {
-                    j.fwd = base + s.fwd;
-                    j.fwd_elem = 1;
-                    j.fwd_vec = static_cast<std::int64_t>(s.fwd_stride);
+                auto &j = it.axis;
+                j.plan = r.h->view;
+                j.in = in; j.in_elem = 1; j.in_vec = in_vec;
+                j.out = out; j.out_elem = 1; j.out_vec = out_vec;
+                if (!v && r.f64) {
+                    j.fwd = base + r.fwd; j.fwd_elem = 1; j.fwd_vec = static_cast<std::int64_t>(r.fwd_stride);
                 } else {
-                    j.fwd = j.out;
-                    j.fwd_elem = 1;
-                    j.fwd_vec = j.out_vec;
+                    j.fwd = out; j.fwd_elem = 1; j.fwd_vec = out_vec;
                 }
+                j.vectors = vectors;
+                j.conv = conv;
+                groups[{0, seq_kind, h->half_bandwidth, task.sample, out_kind}].push_back(it);
             }
-            std::uint64_t hb_bytes = static_cast<std::uint64_t>(j.vectors) * h->source_size
-                * sample_bytes(task.sample);
-            if (!v) hb_bytes += static_cast<std::uint64_t>(j.vectors) * h->destination_size * 4;
-            groups[key].push_back({j, hb_bytes});
         }
         if (v) {
-            dev::AxisJob j{};
-            j.plan = view(*v, temporaries);
-            j.conv = conv;
-            if (h) {
-                j.in = base + s.mid;
-                j.in_elem = static_cast<std::int64_t>(s.mid_stride);
-                j.in_vec = 1;
-                j.vectors = h->destination_size;
+            // Columns: destination columns of the intermediate (2D) or of the
+            // input (columns only), into the output.
+            const void *in = h ? static_cast<const void *>(base + r.mid) : task.input;
+            const std::int64_t in_elem = h ? static_cast<std::int64_t>(r.mid_stride) : task.input_stride;
+            const int vectors = h ? h->destination_size : task.vectors;
+            const dev::Sample in_kind = h ? mid_kind : task.sample;
+            Item it;
+            it.bytes = static_cast<std::uint64_t>(vectors) * v->destination_size * sample_bytes(task.sample);
+            if (!h) it.bytes += static_cast<std::uint64_t>(vectors) * v->source_size * 4;
+            if (r.v_stream) {
+                auto &j = it.stream;
+                j.plan = r.v->stream_view;
+                j.in = in; j.in_elem = in_elem; j.in_vec = 1;
+                j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
+                j.vectors = vectors;
+                j.conv = conv;
+                groups[{1, 2, v->half_bandwidth, in_kind, task.sample}].push_back(it);
             } else {
-                j.in = task.input;
-                j.in_elem = task.input_stride;
-                j.in_vec = 1;
-                j.vectors = task.vectors;
+                auto &j = it.axis;
+                j.plan = r.v->view;
+                j.in = in; j.in_elem = in_elem; j.in_vec = 1;
+                j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
+                if (r.fwd_stride) {
+                    j.fwd = base + r.fwd; j.fwd_elem = static_cast<std::int64_t>(r.fwd_stride); j.fwd_vec = 1;
+                } else {
+                    j.fwd = task.output; j.fwd_elem = task.output_stride; j.fwd_vec = 1;
+                }
+                j.vectors = vectors;
+                j.conv = conv;
+                groups[{1, seq_kind, v->half_bandwidth, in_kind, task.sample}].push_back(it);
             }
-            j.out = task.output;
-            j.out_elem = task.output_stride;
-            j.out_vec = 1;
-            if (s.fwd_stride) {
-                j.fwd = base + s.fwd;
-                j.fwd_elem = static_cast<std::int64_t>(s.fwd_stride);
-                j.fwd_vec = 1;
-            } else {
-                j.fwd = j.out;
-                j.fwd_elem = j.out_elem;
-                j.fwd_vec = 1;
-            }
-            GroupKey key{1, s.f64, v->half_bandwidth, h ? mid_kind : task.sample, task.sample};
-            std::uint64_t vb_bytes = static_cast<std::uint64_t>(j.vectors) * v->destination_size
-                * sample_bytes(task.sample);
-            if (!h) vb_bytes += static_cast<std::uint64_t>(j.vectors) * v->source_size * 4;
-            groups[key].push_back({j, vb_bytes});
         }
     }
 
-    constexpr int kThreads = 128;
-    std::vector<dev::AxisJob> &all = ws.host_jobs;
-    all.clear();
-    struct Launch { GroupKey key; std::size_t first; int count; int blocks; std::uint64_t bytes; };
+    // One job table for every group: AxisJob and StreamJob records share a
+    // byte buffer, each group's records contiguous and 256-byte aligned.
+    constexpr int kSeqThreads = 128;
+    const int stream_block = stream_threads();
+    struct Launch { GroupKey key; std::size_t offset; int count; int blocks; std::uint64_t bytes; };
     std::vector<Launch> launches;
-    for (auto &[key, jobs] : groups) {
-        int blocks = 0;
-        std::uint64_t bytes = 0;
-        std::vector<dev::AxisJob> kept;
-        for (auto &[j, b] : jobs) {
-            if (j.vectors <= 0) continue;
-            j.first_block = blocks;
-            blocks += (j.vectors + kThreads - 1) / kThreads;
-            bytes += b;
-            kept.push_back(j);
+    std::vector<char> &table = ws.host_table;
+    table.clear();
+    for (auto &[key, items] : groups) {
+        const bool is_stream = key.kind == 2;
+        const int per_block = is_stream ? stream_block : kSeqThreads;
+        const std::size_t rec = is_stream ? sizeof(dev::StreamJob) : sizeof(dev::AxisJob);
+        int blocks = 0, count = 0;
+        std::uint64_t bytes_moved = 0;
+        const std::size_t offset = align_up(table.size());
+        table.resize(offset);
+        for (auto &it : items) {
+            const int vectors = is_stream ? it.stream.vectors : it.axis.vectors;
+            if (vectors <= 0) continue;
+            if (is_stream) it.stream.first_block = blocks; else it.axis.first_block = blocks;
+            blocks += (vectors + per_block - 1) / per_block;
+            bytes_moved += it.bytes;
+            const char *src = is_stream ? reinterpret_cast<const char *>(&it.stream)
+                                        : reinterpret_cast<const char *>(&it.axis);
+            table.insert(table.end(), src, src + rec);
+            ++count;
         }
-        if (kept.empty()) continue;
-        launches.push_back({key, all.size(), static_cast<int>(kept.size()), blocks, bytes});
-        all.insert(all.end(), kept.begin(), kept.end());
+        if (count) launches.push_back({key, offset, count, blocks, bytes_moved});
     }
     if (launches.empty()) return;
-    const std::size_t table = all.size() * sizeof(dev::AxisJob);
-    ws.jobs.reserve(table);
-    cuda_check(cudaMemcpyAsync(ws.jobs.data(), all.data(), table, cudaMemcpyHostToDevice, ws.stream),
+    ws.jobs.reserve(table.size());
+    cuda_check(cudaMemcpyAsync(ws.jobs.data(), table.data(), table.size(), cudaMemcpyHostToDevice, ws.stream),
                "uploading job table");
-    auto *device_jobs = reinterpret_cast<const dev::AxisJob *>(ws.jobs.data());
     for (const auto &l : launches) {
         Record *rec = nullptr;
         if (profiling) {
             std::scoped_lock lock(mutex);
             records.emplace_back();
             rec = &records.back();
-            rec->name = std::string(l.key.f64 ? "axis_f64" : "axis_f32") + (l.key.pass ? "/vertical" : "/horizontal")
-                + "/hb" + std::to_string(l.key.hb);
+            rec->name = kernel_name(l.key);
             rec->bytes = l.bytes;
             cuda_check(cudaEventCreate(&rec->start), "creating event");
             cuda_check(cudaEventCreate(&rec->stop), "creating event");
             cuda_check(cudaEventRecord(rec->start, ws.stream), "recording event");
         }
-        const int rc = l.key.f64
-            ? launch_axis_f64(device_jobs + l.first, l.count, l.blocks, kThreads, l.key.hb,
-                              l.key.in, l.key.out, ws.status, ws.stream)
-            : launch_axis_f32(device_jobs + l.first, l.count, l.blocks, kThreads, l.key.hb,
-                              l.key.in, l.key.out, ws.stream);
+        const char *dev_table = ws.jobs.data() + l.offset;
+        int rc = 0;
+        if (l.key.kind == 2) {
+            rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
+                               l.key.hb, kStreamChunk, l.key.pass == 0, l.key.in, l.key.out, ws.stream);
+        } else if (l.key.kind == 1) {
+            rc = launch_axis_f64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
+                                 kSeqThreads, l.key.hb, l.key.in, l.key.out, ws.status, ws.stream);
+        } else {
+            rc = launch_axis_f32(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
+                                 kSeqThreads, l.key.hb, l.key.in, l.key.out, ws.stream);
+        }
         cuda_check(rc, "launching axis kernel");
         if (rec) cuda_check(cudaEventRecord(rec->stop, ws.stream), "recording event");
     }
@@ -449,6 +521,8 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     if (device < 0) cuda_check(cudaGetDevice(&device), "querying device");
     if (device >= count) throw std::invalid_argument("CUDA device index out of range");
     impl_->device = device;
+    if (const char *env = std::getenv("DSMVC_GB_STREAM"); env && std::string(env) == "0")
+        impl_->allow_stream = false;
     DeviceGuard guard(device);
     cuda_check(cudaFree(nullptr), "initialising the primary context");
 }

@@ -1,0 +1,31 @@
+// Dispatch of the streaming axis kernels by half-bandwidth.
+#include "stream.cuh"
+
+#include <cuda_runtime.h>
+
+namespace dsmvc_gb {
+
+int launch_stream_hb1(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
+int launch_stream_hb3(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
+int launch_stream_hb5(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
+int launch_stream_hb7(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
+
+int stream_threads() { return 128; }
+
+bool stream_supports(int half_bandwidth) {
+    return half_bandwidth == 1 || half_bandwidth == 3 || half_bandwidth == 5 || half_bandwidth == 7;
+}
+
+int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
+                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, void *stream) {
+    if (chunk != 32) return static_cast<int>(cudaErrorInvalidValue);
+    switch (half_bandwidth) {
+    case 1: return launch_stream_hb1(jobs, job_count, total_blocks, contiguous, in, out, stream);
+    case 3: return launch_stream_hb3(jobs, job_count, total_blocks, contiguous, in, out, stream);
+    case 5: return launch_stream_hb5(jobs, job_count, total_blocks, contiguous, in, out, stream);
+    case 7: return launch_stream_hb7(jobs, job_count, total_blocks, contiguous, in, out, stream);
+    default: return static_cast<int>(cudaErrorInvalidValue);
+    }
+}
+
+} // namespace dsmvc_gb

@@ -1,0 +1,55 @@
+// Packed plan records and jobs of the streaming axis kernels (stream.cu).
+#pragma once
+
+#include "kernels.cuh"
+
+#include <cstdint>
+
+namespace dsmvc_gb::dev {
+
+// Per-destination records, all float-aligned to 16 bytes:
+//   forward[j * forward_stride + ...]:
+//     [0] window start s0 (int bits), [1] inverse diagonal, [2..3] 0,
+//     [4 .. 4+window)  A^T weights of sources s0 .. s0+window-1 (0 where
+//                      the source does not contribute),
+//     [4+window ..)    forward factors -lower_ld for d = HB..1 (0 for d > j),
+//                      padded to a multiple of 4;
+//   backward[j * backward_stride + ...]: upper_l in use order (d = 1..3 for
+//     half-bandwidth 3, d = HB..1 otherwise; 0 beyond the vector end),
+//     padded to a multiple of 4.
+struct StreamPlanView {
+    std::int32_t source_size;
+    std::int32_t destination_size;
+    std::int32_t half_bandwidth;
+    std::int32_t window;            // multiple of 4
+    std::int32_t forward_stride;    // floats
+    std::int32_t backward_stride;   // floats
+    const float *forward;
+    const float *backward;
+};
+
+struct StreamJob {
+    StreamPlanView plan;
+    const void *in;
+    std::int64_t in_elem, in_vec;
+    void *out;
+    std::int64_t out_elem, out_vec;
+    std::int32_t vectors;
+    std::int32_t first_block;
+    Conversion conv;
+};
+
+} // namespace dsmvc_gb::dev
+
+namespace dsmvc_gb {
+
+int stream_threads();
+bool stream_supports(int half_bandwidth);
+constexpr int kStreamChunk = 32;     // destinations per register chunk
+constexpr int kStreamRing = 32;      // source samples held per thread
+// `chunk` is 32 or 64; contiguous = the vector's samples are adjacent
+// (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
+int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
+                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, void *stream);
+
+} // namespace dsmvc_gb

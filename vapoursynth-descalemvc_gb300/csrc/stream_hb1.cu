@@ -1,0 +1,13 @@
+// Streaming axis kernels for half-bandwidth 1 (see stream_impl.cuh); one
+// translation unit per half-bandwidth keeps the build parallel.
+#include "stream_impl.cuh"
+
+namespace dsmvc_gb {
+
+int launch_stream_hb1(const dev::StreamJob *jobs, int count, int blocks, bool contiguous,
+                        dev::Sample in, dev::Sample out, void *stream) {
+    return launch_hb<1, 32>(jobs, count, blocks, contiguous, in, out,
+                             static_cast<cudaStream_t>(stream));
+}
+
+} // namespace dsmvc_gb

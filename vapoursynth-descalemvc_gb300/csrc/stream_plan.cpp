@@ -1,0 +1,128 @@
+// Streaming-kernel packing (see stream_plan.hpp).
+#include "stream_plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace dsmvc_gb {
+namespace {
+
+int round4(int v) { return (v + 3) / 4 * 4; }
+
+// Simulates the kernel's ring feeder: loads of `granule` samples while they
+// fit in the vector, single samples at the tail.  True when every window is
+// still resident when its destination is computed.
+bool ring_fits(const std::vector<int> &s0, int window, int size, int granule, int ring) {
+    int have = 0;
+    for (const int start : s0) {
+        const int need = start + window;
+        while (have < need) have += (have + granule <= size) ? granule : 1;
+        if (have - start > ring) return false;
+    }
+    return true;
+}
+
+} // namespace
+
+StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supported) {
+    StreamPack out;
+    const int n = p.destination_size, m = p.source_size, hb = p.half_bandwidth;
+    if (!hb_supported) {
+        out.reason = "half-bandwidth without a streaming kernel";
+        return out;
+    }
+    if (p.requires_float64()) {
+        out.reason = "Float64 plan";
+        return out;
+    }
+    // Dense window: widest span of sources feeding one destination.
+    int span = 1;
+    for (int j = 0; j < n; ++j) {
+        const auto b = p.transpose_offsets[j], e = p.transpose_offsets[j + 1];
+        if (b < e) span = std::max(span, p.transpose_indices[e - 1] - p.transpose_indices[b] + 1);
+    }
+    const int window = round4(span);
+    if (window > m || window > ring) {
+        out.reason = "gather window exceeds the source or the ring";
+        return out;
+    }
+    std::vector<int> s0(static_cast<std::size_t>(n));
+    int previous = 0;
+    for (int j = 0; j < n; ++j) {
+        const auto b = p.transpose_offsets[j], e = p.transpose_offsets[j + 1];
+        int first = b < e ? p.transpose_indices[b] : previous;
+        first = std::min(first, m - window);
+        if (first < previous) {
+            out.reason = "gather windows move backwards";
+            return out;
+        }
+        s0[j] = first;
+        previous = first;
+    }
+    out.ring_ok_f32 = ring_fits(s0, window, m, 4, ring);
+    out.ring_ok_u16 = ring_fits(s0, window, m, 8, ring);
+    out.ring_ok_u8 = ring_fits(s0, window, m, 16, ring);
+    if (!out.ring_ok_f32) {
+        out.reason = "gather windows advance faster than the ring";
+        return out;
+    }
+
+    // Backward warm-up accuracy: the carry entering a chunk's end, pushed
+    // through the chunk's homogeneous backward recurrence, must vanish.
+    const auto w = static_cast<std::size_t>(n);
+    const int chunks = (n + chunk - 1) / chunk;
+    double worst = 0.0;
+    std::vector<double> x(static_cast<std::size_t>(chunk + hb));
+    for (int k = 1; k + 1 < chunks; ++k) {           // chunks that serve as warm-up
+        const int lo = k * chunk, hi = lo + chunk;     // full chunk [lo, hi)
+        for (int e = 0; e < hb; ++e) {
+            std::fill(x.begin(), x.end(), 0.0);
+            x[static_cast<std::size_t>(chunk + e)] = 1.0; // unit carry at x_{hi+e}
+            for (int t = hi - 1; t >= lo; --t) {
+                double s = 0.0;
+                for (int d = 1; d <= hb && t + d < n; ++d) {
+                    s += static_cast<double>(p.upper_l[static_cast<std::size_t>(d - 1) * w + static_cast<std::size_t>(t)])
+                        * x[static_cast<std::size_t>(t + d - lo)];
+                }
+                x[static_cast<std::size_t>(t - lo)] = -s;
+            }
+            for (int q = 0; q < hb; ++q) worst = std::max(worst, std::abs(x[static_cast<std::size_t>(q)]));
+        }
+    }
+    out.backward_transfer = worst;
+    if (!(worst <= std::ldexp(1.0, -26))) {
+        out.reason = "backward carry decays too slowly for one chunk";
+        return out;
+    }
+
+    const int low = round4(hb);
+    out.window = window;
+    out.forward_stride = 4 + window + low;
+    out.backward_stride = std::max(4, low);
+    out.forward.assign(w * static_cast<std::size_t>(out.forward_stride), 0.0F);
+    out.backward.assign(w * static_cast<std::size_t>(out.backward_stride), 0.0F);
+    for (int j = 0; j < n; ++j) {
+        float *f = out.forward.data() + static_cast<std::size_t>(j) * out.forward_stride;
+        std::memcpy(&f[0], &s0[j], sizeof(int));
+        f[1] = p.inverse_diagonal[j];
+        for (auto k = p.transpose_offsets[j]; k < p.transpose_offsets[j + 1]; ++k)
+            f[4 + (p.transpose_indices[k] - s0[j])] = p.transpose_weights[k];
+        for (int q = 0; q < hb; ++q) {
+            const int d = hb - q;                      // use order d = hb..1
+            f[4 + window + q] = d <= j
+                ? -p.lower_ld[static_cast<std::size_t>(d - 1) * w + static_cast<std::size_t>(j)] : 0.0F;
+        }
+        float *b = out.backward.data() + static_cast<std::size_t>(j) * out.backward_stride;
+        const int avail = std::min(hb, n - j - 1);
+        for (int q = 0; q < hb; ++q) {
+            const int d = hb == 3 ? q + 1 : hb - q;    // use order of the reference
+            b[q] = d <= avail
+                ? p.upper_l[static_cast<std::size_t>(d - 1) * w + static_cast<std::size_t>(j)] : 0.0F;
+        }
+    }
+    out.eligible = true;
+    return out;
+}
+
+} // namespace dsmvc_gb

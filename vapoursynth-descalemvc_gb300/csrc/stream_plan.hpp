@@ -1,0 +1,38 @@
+// Host packing of an axis plan for the streaming kernels (stream_impl.cuh)
+// and the checks that admit a plan to them.
+#pragma once
+
+#include "planner.hpp"
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace dsmvc_gb {
+
+struct StreamPack {
+    bool eligible = false;          // the plan may use the streaming kernels
+    std::string reason;             // why not, when not
+    int window = 0;                 // dense gather window (multiple of 4)
+    int forward_stride = 0;         // floats per forward record
+    int backward_stride = 0;        // floats per backward record
+    // Ring capacity holds for 16-byte row loads of f32 (4 samples), u16 (8)
+    // and u8 (16) rows; column loads fetch 4 rows at a time (as f32 rows).
+    bool ring_ok_f32 = false;
+    bool ring_ok_u16 = false;
+    bool ring_ok_u8 = false;
+    double backward_transfer = 0.0; // max |carry -> state| over one chunk
+    std::vector<float> forward;     // destination_size * forward_stride
+    std::vector<float> backward;    // destination_size * backward_stride
+};
+
+// `chunk` destinations per register chunk, `ring` source samples held per
+// thread.  A plan is eligible when its half-bandwidth has a kernel, its
+// dense window fits the ring, the window starts never move backwards, and
+// the zero-carry backward warm-up over one chunk leaves a carry influence
+// below 2^-26 per carry slot (computed in double for every chunk of the
+// plan), which keeps the warm-up error within about one float ULP.
+StreamPack pack_stream_plan(const AxisPlan &plan, int chunk, int ring,
+                            bool half_bandwidth_supported);
+
+} // namespace dsmvc_gb

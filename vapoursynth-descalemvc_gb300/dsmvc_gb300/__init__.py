@@ -79,6 +79,14 @@ class PlaneTaskC(C.Structure):
                 ("conversion", ConversionC)]
 
 
+class StreamInfoC(C.Structure):
+    _fields_ = [("eligible", C.c_int32), ("window", C.c_int32),
+                ("forward_stride", C.c_int32), ("backward_stride", C.c_int32),
+                ("ring_ok_u16", C.c_int32), ("ring_ok_u8", C.c_int32),
+                ("chunk", C.c_int32), ("ring", C.c_int32),
+                ("backward_transfer", C.c_double), ("reason", C.c_char * 96)]
+
+
 class KernelTimeC(C.Structure):
     _fields_ = [("name", C.c_char * 64), ("launches", C.c_uint64),
                 ("milliseconds", C.c_double), ("bytes", C.c_uint64)]
@@ -101,6 +109,8 @@ SIGNATURES = {
                                  C.POINTER(C.c_uint64)], C.c_int),
     "dsmvc_gb_plan_hashes": ([C.c_void_p, C.POINTER(AxisRequestC), C.POINTER(C.c_uint64),
                               C.POINTER(C.c_uint64)], C.c_int),
+    "dsmvc_gb_plan_stream_info": ([C.c_void_p, C.POINTER(StreamInfoC), C.c_void_p, C.c_uint64,
+                                   C.c_void_p, C.c_uint64], C.c_int),
     "dsmvc_gb_planner_cache_stats": ([C.POINTER(PlannerStatsC)], C.c_int),
     "dsmvc_gb_clear_planner_caches": ([], None),
     "dsmvc_gb_executor_create": ([C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
@@ -229,6 +239,22 @@ class AxisPlan:
                 nbytes = count.value * np.dtype(dt).itemsize
                 return np.frombuffer((C.c_char * nbytes).from_address(ptr.value), dt).copy()
         raise KeyError(name)
+
+    def stream_info(self, records: bool = False) -> dict:
+        """Streaming-kernel eligibility and (optionally) packed records."""
+        info = StreamInfoC()
+        _check(lib().dsmvc_gb_plan_stream_info(self._h, C.byref(info), None, 0, None, 0))
+        out = {k: getattr(info, k) for k, _ in info._fields_}
+        out["reason"] = info.reason.decode()
+        if records and info.eligible:
+            n = self.destination_size
+            fwd = np.zeros(n * info.forward_stride, np.float32)
+            bwd = np.zeros(n * info.backward_stride, np.float32)
+            _check(lib().dsmvc_gb_plan_stream_info(self._h, C.byref(info), fwd.ctypes.data, fwd.size,
+                                                   bwd.ctypes.data, bwd.size))
+            out["forward"] = fwd.reshape(n, info.forward_stride)
+            out["backward"] = bwd.reshape(n, info.backward_stride)
+        return out
 
     def hashes(self):
         f, c = C.c_uint64(), C.c_uint64()
