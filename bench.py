@@ -254,8 +254,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--frames", type=int, default=FRAMES,
+                    help="frames per step (profiling runs use fewer; the benchmark line uses 64)")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="skip the end-to-end and CPU legs (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global FRAMES
+    FRAMES = args.frames
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -334,7 +340,7 @@ def main():
     # End to end: the synchronous host-frame calls of the C ABI, pinned host
     # planes, 8 caller threads (the plugin's frame-parallel requests).
     host_in, host_out, calls = [], [], []
-    for f in range(FRAMES):
+    for f in range(0 if args.kernels_only else FRAMES):
         for idx, plane in enumerate(frames[f % len(frames)]):
             hk, vk, conv = ("luma_h", "luma_v", luma_conv) if idx == 0 else \
                 ("chroma_h", "chroma_v", chroma_conv)
@@ -352,15 +358,17 @@ def main():
     def call(c):
         ex.inverse_2d(c[0], c[1], c[2], c[3], out=c[4])
 
-    with cf.ThreadPoolExecutor(max_workers=8) as pool:
-        list(pool.map(call, calls))  # warm-up
-        if dist is not None:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
-            list(pool.map(call, calls))
-        e2e_s = time.perf_counter() - t0
-    e2e = world * args.e2e_steps * pix_step / e2e_s / 1e6
+    e2e = None
+    if calls:
+        with cf.ThreadPoolExecutor(max_workers=8) as pool:
+            list(pool.map(call, calls))  # warm-up
+            if dist is not None:
+                dist.barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_steps):
+                list(pool.map(call, calls))
+            e2e_s = time.perf_counter() - t0
+        e2e = world * args.e2e_steps * pix_step / e2e_s / 1e6
 
     hbm, peak_kind = peaks()
     total_ms = sum(k["milliseconds"] for k in ktimes)
@@ -374,7 +382,7 @@ def main():
             dist.destroy_process_group()
         return
     cpu = None
-    if not args.no_cpu_baseline and world == 1:
+    if not args.no_cpu_baseline and not args.kernels_only and world == 1:
         cpu = cpu_baseline(frames, os.cpu_count() or 1, budget_s=args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,

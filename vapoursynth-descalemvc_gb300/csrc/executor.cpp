@@ -433,7 +433,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
     // byte buffer, each group's records contiguous and 256-byte aligned.
     constexpr int kSeqThreads = 128;
     const int stream_block = stream_threads();
-    struct Launch { GroupKey key; std::size_t offset; int count; int blocks; std::uint64_t bytes; };
+    struct Launch { GroupKey key; std::size_t offset; int count; int blocks; std::uint64_t bytes; int record_floats; };
     std::vector<Launch> launches;
     std::vector<char> &table = ws.host_table;
     table.clear();
@@ -441,7 +441,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
         const bool is_stream = key.kind == 2;
         const int per_block = is_stream ? stream_block : kSeqThreads;
         const std::size_t rec = is_stream ? sizeof(dev::StreamJob) : sizeof(dev::AxisJob);
-        int blocks = 0, count = 0;
+        int blocks = 0, count = 0, record_floats = 0;
         std::uint64_t bytes_moved = 0;
         const std::size_t offset = align_up(table.size());
         table.resize(offset);
@@ -451,12 +451,14 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
             if (is_stream) it.stream.first_block = blocks; else it.axis.first_block = blocks;
             blocks += (vectors + per_block - 1) / per_block;
             bytes_moved += it.bytes;
+            if (is_stream)
+                record_floats = std::max(record_floats, it.stream.plan.forward_stride + it.stream.plan.backward_stride);
             const char *src = is_stream ? reinterpret_cast<const char *>(&it.stream)
                                         : reinterpret_cast<const char *>(&it.axis);
             table.insert(table.end(), src, src + rec);
             ++count;
         }
-        if (count) launches.push_back({key, offset, count, blocks, bytes_moved});
+        if (count) launches.push_back({key, offset, count, blocks, bytes_moved, record_floats});
     }
     if (launches.empty()) return;
     ws.jobs.reserve(table.size());
@@ -478,7 +480,8 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
         int rc = 0;
         if (l.key.kind == 2) {
             rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
-                               l.key.hb, kStreamChunk, l.key.pass == 0, l.key.in, l.key.out, ws.stream);
+                               l.key.hb, kStreamChunk, l.key.pass == 0, l.key.in, l.key.out, l.record_floats,
+                               ws.stream);
         } else if (l.key.kind == 1) {
             rc = launch_axis_f64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
                                  kSeqThreads, l.key.hb, l.key.in, l.key.out, ws.status, ws.stream);

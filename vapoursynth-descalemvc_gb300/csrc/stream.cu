@@ -5,10 +5,10 @@
 
 namespace dsmvc_gb {
 
-int launch_stream_hb1(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
-int launch_stream_hb3(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
-int launch_stream_hb5(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
-int launch_stream_hb7(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, void *);
+int launch_stream_hb1(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, int, void *);
+int launch_stream_hb3(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, int, void *);
+int launch_stream_hb5(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, int, void *);
+int launch_stream_hb7(const dev::StreamJob *, int, int, bool, dev::Sample, dev::Sample, int, void *);
 
 int stream_threads() { return 128; }
 
@@ -17,13 +17,14 @@ bool stream_supports(int half_bandwidth) {
 }
 
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
-                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, void *stream) {
-    if (chunk != 32) return static_cast<int>(cudaErrorInvalidValue);
+                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, int record_floats,
+                  void *stream) {
+    if (chunk != kStreamChunk) return static_cast<int>(cudaErrorInvalidValue);
     switch (half_bandwidth) {
-    case 1: return launch_stream_hb1(jobs, job_count, total_blocks, contiguous, in, out, stream);
-    case 3: return launch_stream_hb3(jobs, job_count, total_blocks, contiguous, in, out, stream);
-    case 5: return launch_stream_hb5(jobs, job_count, total_blocks, contiguous, in, out, stream);
-    case 7: return launch_stream_hb7(jobs, job_count, total_blocks, contiguous, in, out, stream);
+    case 1: return launch_stream_hb1(jobs, job_count, total_blocks, contiguous, in, out, record_floats, stream);
+    case 3: return launch_stream_hb3(jobs, job_count, total_blocks, contiguous, in, out, record_floats, stream);
+    case 5: return launch_stream_hb5(jobs, job_count, total_blocks, contiguous, in, out, record_floats, stream);
+    case 7: return launch_stream_hb7(jobs, job_count, total_blocks, contiguous, in, out, record_floats, stream);
     default: return static_cast<int>(cudaErrorInvalidValue);
     }
 }

@@ -49,7 +49,9 @@ constexpr int kStreamChunk = 32;     // destinations per register chunk
 constexpr int kStreamRing = 32;      // source samples held per thread
 // `chunk` is 32 or 64; contiguous = the vector's samples are adjacent
 // (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
+// `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
-                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, void *stream);
+                  int chunk, bool contiguous, dev::Sample in, dev::Sample out, int record_floats,
+                  void *stream);
 
 } // namespace dsmvc_gb

@@ -5,9 +5,9 @@
 namespace dsmvc_gb {
 
 int launch_stream_hb3(const dev::StreamJob *jobs, int count, int blocks, bool contiguous,
-                        dev::Sample in, dev::Sample out, void *stream) {
-    return launch_hb<3, 32>(jobs, count, blocks, contiguous, in, out,
-                             static_cast<cudaStream_t>(stream));
+                        dev::Sample in, dev::Sample out, int record_floats, void *stream) {
+    return launch_hb<3, kStreamChunk>(jobs, count, blocks, contiguous, in, out, record_floats,
+                                       static_cast<cudaStream_t>(stream));
 }
 
 } // namespace dsmvc_gb

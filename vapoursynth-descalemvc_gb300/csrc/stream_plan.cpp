@@ -100,8 +100,11 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.window = window;
     out.forward_stride = 4 + window + low;
     out.backward_stride = std::max(4, low);
-    out.forward.assign(w * static_cast<std::size_t>(out.forward_stride), 0.0F);
-    out.backward.assign(w * static_cast<std::size_t>(out.backward_stride), 0.0F);
+    // Whole chunks of records (zeros past the last destination), so that
+    // every chunk copy of the kernel stays inside the arrays.
+    const auto padded = static_cast<std::size_t>((n + chunk - 1) / chunk) * static_cast<std::size_t>(chunk);
+    out.forward.assign(padded * static_cast<std::size_t>(out.forward_stride), 0.0F);
+    out.backward.assign(padded * static_cast<std::size_t>(out.backward_stride), 0.0F);
     for (int j = 0; j < n; ++j) {
         float *f = out.forward.data() + static_cast<std::size_t>(j) * out.forward_stride;
         std::memcpy(&f[0], &s0[j], sizeof(int));

@@ -22,8 +22,10 @@ struct StreamPack {
     bool ring_ok_u16 = false;
     bool ring_ok_u8 = false;
     double backward_transfer = 0.0; // max |carry -> state| over one chunk
-    std::vector<float> forward;     // destination_size * forward_stride
-    std::vector<float> backward;    // destination_size * backward_stride
+    // Records of ceil(destination_size / chunk) * chunk destinations (zero
+    // records past the end).
+    std::vector<float> forward;     // * forward_stride
+    std::vector<float> backward;    // * backward_stride
 };
 
 // `chunk` destinations per register chunk, `ring` source samples held per

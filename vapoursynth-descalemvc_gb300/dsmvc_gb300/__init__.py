@@ -247,7 +247,8 @@ class AxisPlan:
         out = {k: getattr(info, k) for k, _ in info._fields_}
         out["reason"] = info.reason.decode()
         if records and info.eligible:
-            n = self.destination_size
+            # Records cover whole chunks: zero records past the last destination.
+            n = -(-self.destination_size // info.chunk) * info.chunk
             fwd = np.zeros(n * info.forward_stride, np.float32)
             bwd = np.zeros(n * info.backward_stride, np.float32)
             _check(lib().dsmvc_gb_plan_stream_info(self._h, C.byref(info), fwd.ctypes.data, fwd.size,
