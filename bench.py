@@ -246,6 +246,7 @@ def workload_config():
 
 
 def main():
+    global FRAMES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -260,7 +261,6 @@ def main():
                     help="skip the end-to-end and CPU legs (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global FRAMES
     FRAMES = args.frames
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
