@@ -237,6 +237,30 @@ int dsmvc_gb_run_batch(dsmvc_gb_executor *executor,
                        void *stream, int32_t synchronize);
 int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream);
 
+/* Allocation-free 2D descale.  No counterpart in the reference.  For callers
+ * that cannot allocate device memory (code running inside another
+ * framework's memory pool, allocator-free real-time pipelines): the Float32
+ * route of the 2D descale on device pointers, enqueued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream), with no cudaMalloc,
+ * cudaFree or other allocating call.  Its scratch -- job table, both plans'
+ * coefficients, the Float32 intermediate plane (4 x vertical source size x
+ * horizontal destination size bytes) and, for integer output, a forward
+ * plane of the output's size -- lives in one file-scope device array of
+ * DSMVC_GB_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
+ * until the process exits.  Frames that need more, and plans that need
+ * Float64, are rejected with DSMVC_GB_INVALID_ARGUMENT.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race, so order them on one stream.  `sample` is an
+ * enum dsmvc_gb_sample; `conversion` is read for integer samples. */
+#define DSMVC_GB_NOALLOC_SCRATCH_BYTES (32u << 20)
+int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal,
+                                const dsmvc_gb_plan *vertical, int32_t sample,
+                                const void *input, int64_t input_stride,
+                                void *output, int64_t output_stride,
+                                const dsmvc_gb_conversion *conversion,
+                                void *stream);
+
 /* Kernel timing (the reference's NVTX ranges, src/cuda/nvtx.hpp:11-60, are
  * replaced by CUDA events): while enabled, every launch is bracketed by
  * events on its stream; dsmvc_gb_profile_read waits for them and returns one

@@ -3,6 +3,7 @@
 #include "../../include/dsmvc_gb300.h"
 
 #include "executor.hpp"
+#include "noalloc.hpp"
 #include "planner.hpp"
 #include "stream.cuh"
 #include "stream_plan.hpp"
@@ -340,6 +341,24 @@ int dsmvc_gb_run_batch(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task *t
 
 int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream) {
     return guarded([&] { exec_of(executor).check_status(stream); });
+}
+
+int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal, const dsmvc_gb_plan *vertical,
+                                int32_t sample, const void *input, int64_t input_stride,
+                                void *output, int64_t output_stride,
+                                const dsmvc_gb_conversion *conversion, void *stream) {
+    return guarded([&] {
+        if (sample < DSMVC_GB_FLOAT32 || sample > DSMVC_GB_UINT16)
+            throw std::invalid_argument("sample kind is invalid");
+        dsmvc_gb::dev::Conversion conv{0.0F, 1.0F, 1.0F, 0.0F, 255U};
+        if (sample != DSMVC_GB_FLOAT32) {
+            const auto c = to_conversion(conversion);
+            conv = {c.input_offset, c.input_scale, c.output_scale, c.output_offset, c.output_maximum};
+        }
+        dsmvc_gb::inverse_2d_noalloc(plan_of(horizontal), plan_of(vertical),
+                                     static_cast<dsmvc_gb::dev::Sample>(sample), input, input_stride,
+                                     output, output_stride, conv, stream);
+    });
 }
 
 int dsmvc_gb_profile(dsmvc_gb_executor *executor, int32_t enable) {

@@ -131,6 +131,9 @@ SIGNATURES = {
     "dsmvc_gb_run_batch": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_void_p,
                             C.c_int32], C.c_int),
     "dsmvc_gb_stream_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_inverse_2d_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
+                                     C.c_void_p, C.c_int64, C.POINTER(ConversionC), C.c_void_p],
+                                    C.c_int),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -395,6 +398,22 @@ class Executor:
         return [{"name": buf[i].name.decode(), "launches": buf[i].launches,
                  "milliseconds": buf[i].milliseconds, "bytes": buf[i].bytes}
                 for i in range(min(n.value, 64))]
+
+
+NOALLOC_SCRATCH_BYTES = 32 << 20
+
+
+def inverse_2d_noalloc(h: AxisPlan, v: AxisPlan, sample: int, input_ptr: int, input_stride: int,
+                       output_ptr: int, output_stride: int, conversion=None, stream: int = 0) -> None:
+    """Allocation-free 2D descale on device pointers (see the C header):
+    for callers that cannot allocate device memory.  Float32 route only;
+    frames whose scratch exceeds NOALLOC_SCRATCH_BYTES are rejected; calls
+    that overlap on the GPU race on the shared scratch array."""
+    conv = _conv(conversion)
+    _check(lib().dsmvc_gb_inverse_2d_noalloc(h.handle, v.handle, int(sample), C.c_void_p(input_ptr),
+                                             int(input_stride), C.c_void_p(output_ptr),
+                                             int(output_stride), C.byref(conv),
+                                             C.c_void_p(stream or None)))
 
 
 def integer_conversion(bits: int, chroma: bool, full_range: bool) -> tuple:
