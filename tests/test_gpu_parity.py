@@ -220,14 +220,37 @@ def test_full_size_frames_use_streaming_kernels(gb, executor, name, hq, vq, samp
     got = executor.inverse_2d(h, v, x, conv)
     names = {k["name"] for k in executor.kernel_times()}
     executor.profile(False)
-    assert any(n.startswith("stream_f32/rows") for n in names), names
-    assert any(n.startswith("stream_f32/columns") for n in names), names
+    assert any(n.startswith("tstream_f32/rows") for n in names), names
+    assert any(n.startswith("tstream_f32/columns") for n in names), names
     scalar = O.inverse_2d(oh, ov, x, conv)
     if sample == "f32":
         err = np.abs(got.astype(np.float64) - scalar)
         assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
     else:
         assert np.max(np.abs(got.astype(np.int64) - scalar.astype(np.int64))) <= INT_MAX_CODES
+
+
+ROW_COL_STREAM = [
+    ("lanczos3-rows", (400, 300, 300.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0)),
+    ("bicubic-odd", (333, 217, 216.5, 0.25, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)),
+    ("bilinear-zero", (250, 200, 200.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "zero", 0)),
+]
+
+
+@pytest.mark.parametrize("name,req", ROW_COL_STREAM, ids=[c[0] for c in ROW_COL_STREAM])
+def test_rows_and_columns_streaming(gb, executor, name, req):
+    """One-axis calls on the streaming kernels (rows: adjacent samples,
+    columns: strided), several chunks long."""
+    p, o = plans(gb, executor, req)
+    assert p.stream_info()["eligible"]
+    x = image(45, p.source_size, 51)
+    want = O.inverse_rows_gpu_order(o, x)
+    got = executor.inverse_rows(p, x)
+    assert np.max(np.abs(got - want)) <= STREAM_REL * np.max(np.abs(want))
+    xc = image(p.source_size, 47, 52)
+    wantc = O.inverse_columns_gpu_order(o, xc)
+    gotc = executor.inverse_columns(p, xc)
+    assert np.max(np.abs(gotc - wantc)) <= STREAM_REL * np.max(np.abs(wantc))
 
 
 def test_unprepared_plans_still_run(gb, executor):

@@ -81,6 +81,7 @@ struct DevicePlan {
     // Streaming-kernel records (when the plan qualifies, stream_plan.hpp).
     bool stream = false;
     bool stream_u16 = false, stream_u8 = false;
+    bool stream_t = false;          // transposing 2D kernels admitted
     dev::StreamPlanView stream_view{};
     std::size_t bytes = 0;
 };
@@ -135,6 +136,7 @@ std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
         dp->stream = true;
         dp->stream_u16 = pack.ring_ok_u16;
         dp->stream_u8 = pack.ring_ok_u8;
+        dp->stream_t = pack.ring_ok_transposed;
         auto &sv = dp->stream_view;
         sv.source_size = p.source_size;
         sv.destination_size = p.destination_size;
@@ -277,11 +279,14 @@ namespace {
 // half-bandwidth and sample kinds.
 struct GroupKey {
     int pass;        // 0 first pass (rows), 1 second pass (columns)
-    int kind;        // 0 sequential Float32, 1 sequential Float64, 2 streaming
+    int kind;        // 0 sequential Float32, 1 sequential Float64, 2 streaming,
+                     // 3 transposing streaming (2D)
     int hb;
     dev::Sample in, out;
+    int variant = 0; // kind 3: 1 when every job's window is 8
     bool operator<(const GroupKey &o) const {
-        return std::tie(pass, kind, hb, in, out) < std::tie(o.pass, o.kind, o.hb, o.in, o.out);
+        return std::tie(pass, kind, hb, in, out, variant)
+            < std::tie(o.pass, o.kind, o.hb, o.in, o.out, o.variant);
     }
 };
 
@@ -297,7 +302,7 @@ bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
 }
 
 std::string kernel_name(const GroupKey &k) {
-    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32"};
+    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -309,6 +314,10 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
     struct Route {
         const DevicePlan *h = nullptr, *v = nullptr;
         bool f64 = false, h_stream = false, v_stream = false;
+        // Float32 2D planes keep the intermediate transposed (destination
+        // column-major): both passes then read adjacent samples and write
+        // adjacent vectors.
+        bool transposed = false, h_t = false, v_t = false;
         std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0;
     };
     std::vector<Route> routes(tasks.size());
@@ -326,7 +335,21 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
             r.v_stream = r.v && r.v->stream;
         }
         const std::size_t es = r.f64 ? 8 : 4;
-        if (h && v) {
+        if (h && v && !r.f64) {
+            r.transposed = true;
+            r.h_t = allow_stream && r.h->stream && r.h->stream_t
+                && (task.sample == dev::Sample::f32 || task.sample == dev::Sample::u16
+                    || task.sample == dev::Sample::u8);
+            r.v_t = allow_stream && r.v->stream && r.v->stream_t;
+            r.mid_stride = (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4;
+            r.mid = bytes;
+            bytes += align_up(r.mid_stride * static_cast<std::size_t>(h->destination_size) * 4);
+            if (!r.v_t && task.sample != dev::Sample::f32) {
+                r.fwd_stride = static_cast<std::size_t>(h->destination_size);
+                r.fwd = bytes;
+                bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 4);
+            }
+        } else if (h && v) {
             r.mid_stride = static_cast<std::size_t>(h->destination_size);
             r.mid = bytes;
             bytes += align_up(r.mid_stride * static_cast<std::size_t>(v->source_size) * es);
@@ -359,6 +382,57 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
         const dev::Conversion conv = to_dev(task.conversion);
         const dev::Sample mid_kind = r.f64 ? dev::Sample::f64 : dev::Sample::f32;
         const int seq_kind = r.f64 ? 1 : 0;
+        if (r.transposed) {
+            float *mid = reinterpret_cast<float *>(base + r.mid);
+            const auto pitch = static_cast<std::int64_t>(r.mid_stride);
+            Item hi, vi;
+            hi.bytes = static_cast<std::uint64_t>(v->source_size) * h->source_size * sample_bytes(task.sample);
+            vi.bytes = static_cast<std::uint64_t>(h->destination_size) * v->destination_size
+                * sample_bytes(task.sample);
+            if (r.h_t) {
+                auto &j = hi.stream;
+                j.plan = r.h->stream_view;
+                j.in = task.input; j.in_elem = 1; j.in_vec = task.input_stride;
+                j.out = mid; j.out_elem = pitch; j.out_vec = 1;
+                j.vectors = v->source_size;
+                j.conv = conv;
+                groups[{0, 3, h->half_bandwidth, task.sample, dev::Sample::f32,
+                        j.plan.window == 8 ? 1 : 0}].push_back(hi);
+            } else {
+                auto &j = hi.axis;
+                j.plan = r.h->view;
+                j.in = task.input; j.in_elem = 1; j.in_vec = task.input_stride;
+                j.out = mid; j.out_elem = pitch; j.out_vec = 1;
+                j.fwd = mid; j.fwd_elem = pitch; j.fwd_vec = 1;
+                j.vectors = v->source_size;
+                j.conv = conv;
+                groups[{0, 0, h->half_bandwidth, task.sample, dev::Sample::f32}].push_back(hi);
+            }
+            if (r.v_t) {
+                auto &j = vi.stream;
+                j.plan = r.v->stream_view;
+                j.in = mid; j.in_elem = 1; j.in_vec = pitch;
+                j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
+                j.vectors = h->destination_size;
+                j.conv = conv;
+                groups[{1, 3, v->half_bandwidth, dev::Sample::f32, task.sample,
+                        j.plan.window == 8 ? 1 : 0}].push_back(vi);
+            } else {
+                auto &j = vi.axis;
+                j.plan = r.v->view;
+                j.in = mid; j.in_elem = 1; j.in_vec = pitch;
+                j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
+                if (r.fwd_stride) {
+                    j.fwd = base + r.fwd; j.fwd_elem = static_cast<std::int64_t>(r.fwd_stride); j.fwd_vec = 1;
+                } else {
+                    j.fwd = task.output; j.fwd_elem = task.output_stride; j.fwd_vec = 1;
+                }
+                j.vectors = h->destination_size;
+                j.conv = conv;
+                groups[{1, 0, v->half_bandwidth, dev::Sample::f32, task.sample}].push_back(vi);
+            }
+            continue;
+        }
         if (h) {
             // Rows: source rows of the input, into the intermediate (2D) or
             // the output (rows only).
@@ -438,7 +512,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
     std::vector<char> &table = ws.host_table;
     table.clear();
     for (auto &[key, items] : groups) {
-        const bool is_stream = key.kind == 2;
+        const bool is_stream = key.kind >= 2;
         const int per_block = is_stream ? stream_block : kSeqThreads;
         const std::size_t rec = is_stream ? sizeof(dev::StreamJob) : sizeof(dev::AxisJob);
         int blocks = 0, count = 0, record_floats = 0;
@@ -478,7 +552,11 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
         }
         const char *dev_table = ws.jobs.data() + l.offset;
         int rc = 0;
-        if (l.key.kind == 2) {
+        if (l.key.kind == 3) {
+            rc = launch_tstream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
+                                l.key.hb, l.key.variant ? 8 : 0, l.key.in, l.key.out, l.record_floats,
+                                ws.stream);
+        } else if (l.key.kind == 2) {
             rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
                                l.key.hb, kStreamChunk, l.key.pass == 0, l.key.in, l.key.out, l.record_floats,
                                ws.stream);

@@ -49,6 +49,12 @@ constexpr int kStreamChunk = 32;     // destinations per register chunk
 constexpr int kStreamRing = 32;      // source samples held per thread
 // `chunk` is 32 or 64; contiguous = the vector's samples are adjacent
 // (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
+// Transposing 2D passes (tstream_impl.cuh): vectors with adjacent samples
+// in, destination-major output with the vectors adjacent.  Every job of one
+// launch has the same window when window == 8 (unrolled gather).
+int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
+                   int window, dev::Sample in, dev::Sample out, int record_floats, void *stream);
+
 // `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
                   int chunk, bool contiguous, dev::Sample in, dev::Sample out, int record_floats,

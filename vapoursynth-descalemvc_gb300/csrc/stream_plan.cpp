@@ -23,6 +23,23 @@ bool ring_fits(const std::vector<int> &s0, int window, int size, int granule, in
     return true;
 }
 
+// The transposing kernels feed a warp's ring in blocks of 16 samples once
+// per group of 4 destinations (up to the window end of the group's last
+// destination, single samples past the last whole block).  True when every
+// destination's window is still resident.
+bool ring_fits_grouped(const std::vector<int> &s0, int window, int size, int ring) {
+    int have = 0;
+    const int n = static_cast<int>(s0.size());
+    for (int g = 0; g < n; g += 4) {
+        const int last = std::min(g + 3, n - 1);
+        const int need = std::min(size, std::max(s0[g], s0[last]) + window);
+        while (have < need) have += (have + 16 <= size) ? 16 : 1;
+        for (int j = g; j <= last; ++j)
+            if (have - s0[j] > ring) return false;
+    }
+    return true;
+}
+
 } // namespace
 
 StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supported) {
@@ -63,6 +80,7 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.ring_ok_f32 = ring_fits(s0, window, m, 4, ring);
     out.ring_ok_u16 = ring_fits(s0, window, m, 8, ring);
     out.ring_ok_u8 = ring_fits(s0, window, m, 16, ring);
+    out.ring_ok_transposed = ring_fits_grouped(s0, window, m, ring);
     if (!out.ring_ok_f32) {
         out.reason = "gather windows advance faster than the ring";
         return out;

@@ -21,6 +21,8 @@ struct StreamPack {
     bool ring_ok_f32 = false;
     bool ring_ok_u16 = false;
     bool ring_ok_u8 = false;
+    // The transposing 2D kernels' warp-wide block feeding fits the ring.
+    bool ring_ok_transposed = false;
     double backward_transfer = 0.0; // max |carry -> state| over one chunk
     // Records of ceil(destination_size / chunk) * chunk destinations (zero
     // records past the end).

@@ -1,0 +1,402 @@
+// Transposing streaming kernels: the two passes of a 2D descale.
+//
+// Both passes read vectors whose samples are contiguous (rows of the input
+// plane; columns of the transposed intermediate) and write their results
+// transposed, destination-major with the vectors contiguous (the first pass
+// writes the intermediate column-major, the second writes the output plane
+// row-major).  A warp owns 32 vectors, one per lane:
+//
+//  * Loads: blocks of 16 source samples of all 32 vectors are fetched by the
+//    whole warp with 16-byte coalesced loads (2 lanes per u16 vector, 4 per
+//    f32 vector, 1 per u8 vector), converted to float and scattered into a
+//    shared ring of 32 sample rows, stored twice so that any window of up to
+//    32 consecutive samples is contiguous.  Ring rows are 34 floats apart:
+//    the scatter of every load pattern and the per-lane reads of one sample
+//    row are both free of bank conflicts.  The next block is in flight while
+//    the current one is consumed.
+//  * Stores: destination j of the 32 vectors is one coalesced store.
+//  * Records: the CTA's four warps work on the same destinations, so one
+//    chunk of 32 destination records is copied (cp.async) into shared memory
+//    for all of them, three chunks deep, behind a barrier per chunk.
+//  * Arithmetic: as in stream_impl.cuh -- exact forward substitution in the
+//    reference CUDA order, chunk-delayed backward substitution with a
+//    zero-carry warm-up over the following chunk (admitted per plan by the
+//    host), no forward value written to memory.  The destination loop of a
+//    chunk is branch-free: samples are fetched once per four destinations
+//    and destinations past the end are computed as zeros and not stored.
+#pragma once
+
+#include "kernels.cuh"
+#include "stream.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace dsmvc_gb {
+namespace {
+
+using dev::Conversion;
+using dev::StreamJob;
+
+constexpr int kTRing = kStreamRing;        // sample rows per ring
+constexpr int kTPitch = 34;                // floats between ring rows
+constexpr int kTRingFloats = 2 * kTRing * kTPitch;
+constexpr int kTChunk = kStreamChunk;
+constexpr int kTThreads = 128;
+constexpr int kTWarps = kTThreads / 32;
+constexpr int kTBlock = 16;                // samples per warp load block
+
+__device__ __forceinline__ int find_tjob(const StreamJob *jobs, int count, int block) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].first_block <= block) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void tcp_async16(float *smem, const float *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void tcp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void tcp_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <class T> __device__ __forceinline__ float tin(T v, const Conversion &c) {
+    return (static_cast<float>(v) - c.in_offset) * c.in_scale;
+}
+template <> __device__ __forceinline__ float tin<float>(float v, const Conversion &) { return v; }
+
+template <class T> __device__ __forceinline__ T tout(float v, const Conversion &c) {
+    float s = __fadd_rn(__fmul_rn(v, c.out_scale), c.out_offset);
+    s = fminf(fmaxf(s, 0.0f), static_cast<float>(c.out_max));
+    return static_cast<T>(__float2uint_rn(s));
+}
+template <> __device__ __forceinline__ float tout<float>(float v, const Conversion &) { return v; }
+
+__device__ __forceinline__ float4 tlds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// Cooperative ring feeder of one warp.  Block b covers samples
+// [16 b, 16 b + 16) of the warp's 32 vectors.
+template <class In>
+struct WarpFeeder {
+    static constexpr int SPL = 16 / static_cast<int>(sizeof(In));   // samples per lane load
+    static constexpr int LPV = kTBlock / SPL;                       // lanes per vector
+    static constexpr int VPI = 32 / LPV;                            // vectors per load
+    static constexpr int NI = 32 / VPI;                             // loads per block
+    const In *base;          // vector 0 of the warp
+    std::int64_t stride;     // samples between vectors
+    int size;                // samples per vector
+    int have;                // samples in the ring
+    int vectors;             // valid vectors of the warp (>= 1)
+    bool vec_ok;             // 16-byte aligned vectors
+    int lane;
+    float *ring;             // warp ring, ring[row * kTPitch + vector]
+    Conversion conv;
+    uint4 pend[NI];
+    bool pend_ok;
+
+    __device__ __forceinline__ void put(int s, int v, float x) {
+        float *r = ring + (s & (kTRing - 1)) * kTPitch + v;
+        r[0] = x;
+        r[kTRing * kTPitch] = x;
+    }
+
+    __device__ __forceinline__ void issue() {
+        pend_ok = vec_ok && have + kTBlock <= size;
+        if (!pend_ok) return;
+#pragma unroll
+        for (int i = 0; i < NI; ++i) {
+            int v = i * VPI + lane / LPV;
+            v = v < vectors ? v : vectors - 1;
+            const In *p = base + v * stride + have + (lane % LPV) * SPL;
+            pend[i] = __ldg(reinterpret_cast<const uint4 *>(p));
+        }
+    }
+
+    __device__ __forceinline__ void start() {
+        have = 0;
+        issue();
+    }
+
+    // Makes samples [0, need) resident (need <= size) and visible warp-wide.
+    __device__ __forceinline__ void ensure(int need) {
+        if (have >= need) return;
+        while (have < need) {
+            if (pend_ok) {
+#pragma unroll
+                for (int i = 0; i < NI; ++i) {
+                    const int v = i * VPI + lane / LPV;
+                    const In *vals = reinterpret_cast<const In *>(&pend[i]);
+#pragma unroll
+                    for (int k = 0; k < SPL; ++k) put(have + (lane % LPV) * SPL + k, v, tin(vals[k], conv));
+                }
+                have += kTBlock;
+                issue();
+            } else {
+                // Unaligned vectors or the tail: each lane loads its own
+                // vector's next sample.
+                const int v = lane < vectors ? lane : vectors - 1;
+                put(have, lane, tin(__ldg(base + v * stride + have), conv));
+                have += 1;
+            }
+        }
+        __syncwarp();
+    }
+};
+
+__device__ __forceinline__ void tstage(float *buf, const dev::StreamPlanView &p, int chunk, int tid) {
+    const int fs = p.forward_stride, bs = p.backward_stride;
+    const float *gf = p.forward + static_cast<std::int64_t>(chunk) * kTChunk * fs;
+    const float *gb = p.backward + static_cast<std::int64_t>(chunk) * kTChunk * bs;
+    for (int i = tid * 4; i < kTChunk * fs; i += kTThreads * 4) tcp_async16(buf + i, gf + i);
+    float *bb = buf + kTChunk * fs;
+    for (int i = tid * 4; i < kTChunk * bs; i += kTThreads * 4) tcp_async16(bb + i, gb + i);
+}
+
+// Forward substitution of chunk destinations [j0, j0 + LC) into y[LC + t].
+template <int HB, int LC, int K, class Feed>
+__device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::StreamPlanView &p,
+                                         const float *fwd, Feed &feed, int lane) {
+    const int fs = p.forward_stride;
+    const int kw = K > 0 ? K : p.window;
+    const int n = p.destination_size;
+#pragma unroll
+    for (int t = 0; t < LC; ++t) {
+        if (t % 4 == 0) {
+            // Window end of the group's last destination (records past the
+            // end of the vector hold s0 = 0).
+            const int s_last = __float_as_int(fwd[(t + 3) * fs]);
+            const int need = max(s_last, __float_as_int(fwd[t * fs])) + kw;
+            feed.ensure(min(need, p.source_size));
+        }
+        const float *rec = fwd + t * fs;
+        const float4 hdr = tlds4(rec);
+        const int s0 = __float_as_int(hdr.x);
+        const float *win = feed.ring + (s0 & (kTRing - 1)) * kTPitch + lane;
+        float sum = 0.0f;
+        if constexpr (K > 0) {
+#pragma unroll
+            for (int k = 0; k < K; k += 4) {
+                const float4 w = tlds4(rec + 4 + k);
+                sum = fmaf(w.x, win[(k + 0) * kTPitch], sum);
+                sum = fmaf(w.y, win[(k + 1) * kTPitch], sum);
+                sum = fmaf(w.z, win[(k + 2) * kTPitch], sum);
+                sum = fmaf(w.w, win[(k + 3) * kTPitch], sum);
+            }
+        } else {
+            for (int k = 0; k < kw; k += 4) {
+                const float4 w = tlds4(rec + 4 + k);
+                sum = fmaf(w.x, win[(k + 0) * kTPitch], sum);
+                sum = fmaf(w.y, win[(k + 1) * kTPitch], sum);
+                sum = fmaf(w.z, win[(k + 2) * kTPitch], sum);
+                sum = fmaf(w.w, win[(k + 3) * kTPitch], sum);
+            }
+        }
+        const float *low = rec + 4 + kw;
+#pragma unroll
+        for (int q = 0; q < HB; q += 4) {
+            const float4 l = tlds4(low + q);
+            const float lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int d = HB - (q + e);
+                if (d >= 1) sum = fmaf(lv[e], y[LC + t - d], sum);
+            }
+        }
+        y[LC + t] = j0 + t < n ? sum * hdr.y : 0.0f;
+    }
+}
+
+// Zero-carry backward warm-up over the chunk held in y[LC, 2 LC); leaves the
+// state entering the preceding chunk in `carry`.
+template <int HB, int LC>
+__device__ __forceinline__ void twarmup(const float (&y)[2 * LC], float (&carry)[HB],
+                                        const dev::StreamPlanView &p, const float *bwd) {
+    const int bs = p.backward_stride;
+    float w[HB];
+#pragma unroll
+    for (int d = 0; d < HB; ++d) w[d] = 0.0f;
+#pragma unroll
+    for (int t = LC - 1; t >= 0; --t) {
+        const float *rec = bwd + t * bs;
+        float sum = 0.0f;
+#pragma unroll
+        for (int q = 0; q < HB; q += 4) {
+            const float4 u = tlds4(rec + q);
+            const float uv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int pos = q + e;
+                if (pos < HB) {
+                    const int d = HB == 3 ? pos + 1 : HB - pos;
+                    // x_{t+d} beyond the chunk is the zero carry.
+                    const float xd = (t + d < LC) ? w[(t + d) % HB] : 0.0f;
+                    sum = fmaf(uv[e], xd, sum);
+                }
+            }
+        }
+        w[t % HB] = y[LC + t] - sum;
+    }
+#pragma unroll
+    for (int d = 0; d < HB; ++d) carry[d] = w[d];
+}
+
+// Final backward substitution of the chunk held in y[B, B + LC) from
+// `carry` (x after the chunk); each x is stored as soon as it is known.
+// Leaves the chunk's first HB x values in `carry`.
+template <int HB, int LC, int B, class Out>
+__device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB], int j0,
+                                          const dev::StreamPlanView &p, const float *bwd, Out *out,
+                                          std::int64_t out_elem, bool active, const Conversion &conv) {
+    const int bs = p.backward_stride;
+    const int n = p.destination_size;
+#pragma unroll
+    for (int t = LC - 1; t >= 0; --t) {
+        const float *rec = bwd + t * bs;
+        float sum = 0.0f;
+#pragma unroll
+        for (int q = 0; q < HB; q += 4) {
+            const float4 u = tlds4(rec + q);
+            const float uv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int pos = q + e;
+                if (pos < HB) {
+                    const int d = HB == 3 ? pos + 1 : HB - pos;
+                    const float xd = (t + d < LC) ? y[B + (t + d < LC ? t + d : 0)]
+                                                  : carry[t + d >= LC ? t + d - LC : 0];
+                    sum = fmaf(uv[e], xd, sum);
+                }
+            }
+        }
+        const float x = y[B + t] - sum;
+        y[B + t] = x;
+        if (active && j0 + t < n) out[static_cast<std::int64_t>(j0 + t) * out_elem] = tout<Out>(x, conv);
+    }
+#pragma unroll
+    for (int d = 0; d < HB; ++d) carry[d] = y[B + d];
+}
+
+template <int HB, int LC, int K, class In, class Out>
+__global__ void __launch_bounds__(kTThreads)
+tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats) {
+    static_assert(LC == kTChunk, "record chunks and register chunks coincide");
+    extern __shared__ __align__(16) float smem[];
+    const int jidx = find_tjob(jobs, job_count, static_cast<int>(blockIdx.x));
+    const StreamJob &job = jobs[jidx];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const dev::StreamPlanView p = job.plan;
+    const int n = p.destination_size;
+    const int per_buffer = kTChunk * record_floats;
+    float *bufs = smem;
+    float *ring = smem + 3 * per_buffer + warp * kTRingFloats;
+
+    // The warp's vectors; a warp past the last vector still takes part in
+    // the CTA's record copies and barriers, on a clamped vector.
+    const int block_first = (static_cast<int>(blockIdx.x) - job.first_block) * kTThreads;
+    int warp_first = block_first + warp * 32;
+    int warp_vectors = job.vectors - warp_first;
+    if (warp_vectors <= 0) {
+        warp_first = job.vectors - 1;
+        warp_vectors = 1;
+    } else if (warp_vectors > 32) {
+        warp_vectors = 32;
+    }
+    const bool active = block_first + warp * 32 + lane < job.vectors;
+
+    WarpFeeder<In> feed;
+    feed.base = static_cast<const In *>(job.in) + warp_first * job.in_vec;
+    feed.stride = job.in_vec;
+    feed.size = p.source_size;
+    feed.vectors = warp_vectors;
+    feed.lane = lane;
+    feed.ring = ring;
+    feed.conv = job.conv;
+    feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
+        && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
+    feed.start();
+
+    Out *out = static_cast<Out *>(job.out) + (warp_first + (lane < warp_vectors ? lane : 0));
+
+    const int chunks = (n + LC - 1) / LC;
+    tstage(bufs, p, 0, tid);
+    tcp_commit();
+    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid);
+    tcp_commit();
+
+    float y[2 * LC];
+    float carry[HB];
+#pragma unroll
+    for (int t = 0; t < LC; ++t) y[t] = 0.0f;
+    for (int c = 0; c < chunks; ++c) {
+        tcp_wait_one();
+        __syncthreads();
+        const float *cur = bufs + (c % 3) * per_buffer;
+        const float *prev = bufs + ((c + 2) % 3) * per_buffer;
+        tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
+        const float *cur_b = cur + kTChunk * p.forward_stride;
+        const bool last = c + 1 == chunks;
+        if (last) {
+#pragma unroll
+            for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
+            tbackward<HB, LC, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
+        } else {
+            twarmup<HB, LC>(y, carry, p, cur_b);
+        }
+        if (c > 0) {
+            tbackward<HB, LC, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * p.forward_stride, out,
+                                 job.out_elem, active, job.conv);
+        }
+        if (last) break;
+        // Every warp is done with chunk c-1's records: fetch chunk c+2.
+        __syncthreads();
+        if (c + 2 < chunks) tstage(const_cast<float *>(prev), p, c + 2, tid);
+        tcp_commit();
+#pragma unroll
+        for (int t = 0; t < LC; ++t) y[t] = y[LC + t];
+    }
+}
+
+template <int HB, int LC, int K, class In, class Out>
+int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int record_floats, cudaStream_t s) {
+    const int smem = (3 * kTChunk * record_floats + kTWarps * kTRingFloats) * static_cast<int>(sizeof(float));
+    auto kernel = tstream_kernel<HB, LC, K, In, Out>;
+    static int configured = 0;
+    if (smem > configured) {
+        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return static_cast<int>(e);
+        configured = smem;
+    }
+    kernel<<<blocks, kTThreads, smem, s>>>(jobs, count, record_floats);
+    return static_cast<int>(cudaGetLastError());
+}
+
+template <int HB, int LC, int K>
+int tlaunch_k(const StreamJob *jobs, int count, int blocks, dev::Sample in, dev::Sample out,
+              int record_floats, cudaStream_t s) {
+    using dev::Sample;
+    if (in == Sample::f32 && out == Sample::f32)
+        return tlaunch_typed<HB, LC, K, float, float>(jobs, count, blocks, record_floats, s);
+    if (in == Sample::u16 && out == Sample::f32)
+        return tlaunch_typed<HB, LC, K, std::uint16_t, float>(jobs, count, blocks, record_floats, s);
+    if (in == Sample::u8 && out == Sample::f32)
+        return tlaunch_typed<HB, LC, K, std::uint8_t, float>(jobs, count, blocks, record_floats, s);
+    if (in == Sample::f32 && out == Sample::u16)
+        return tlaunch_typed<HB, LC, K, float, std::uint16_t>(jobs, count, blocks, record_floats, s);
+    if (in == Sample::f32 && out == Sample::u8)
+        return tlaunch_typed<HB, LC, K, float, std::uint8_t>(jobs, count, blocks, record_floats, s);
+    return static_cast<int>(cudaErrorInvalidValue);
+}
+
+// window == 8 has an unrolled gather; other windows loop.
+template <int HB>
+int tlaunch_hb(const StreamJob *jobs, int count, int blocks, int window, dev::Sample in,
+               dev::Sample out, int record_floats, cudaStream_t s) {
+    if (window == 8) return tlaunch_k<HB, kTChunk, 8>(jobs, count, blocks, in, out, record_floats, s);
+    return tlaunch_k<HB, kTChunk, 0>(jobs, count, blocks, in, out, record_floats, s);
+}
+
+} // namespace
+} // namespace dsmvc_gb
