@@ -163,6 +163,33 @@ struct Workspace {
     std::uint32_t *status = nullptr;      // device
     std::uint32_t *status_host = nullptr; // pinned
     std::vector<char> host_table;
+    // Job tables travel through two pinned slots, each reused only after
+    // its previous copy has finished; an unchanged table is not copied.
+    char *pinned[2] = {nullptr, nullptr};
+    std::size_t pinned_bytes[2] = {0, 0};
+    cudaEvent_t pinned_done[2] = {nullptr, nullptr};
+    int pinned_next = 0;
+    std::vector<char> device_table;   // what ws.jobs holds
+
+    void upload_table(const std::vector<char> &table) {
+        if (table == device_table) return;
+        const int k = pinned_next;
+        pinned_next ^= 1;
+        if (pinned_done[k]) cuda_check(cudaEventSynchronize(pinned_done[k]), "waiting for a job table slot");
+        else cuda_check(cudaEventCreateWithFlags(&pinned_done[k], cudaEventDisableTiming), "creating event");
+        if (pinned_bytes[k] < table.size()) {
+            if (pinned[k]) cudaFreeHost(pinned[k]);
+            pinned[k] = nullptr;
+            cuda_check(cudaMallocHost(&pinned[k], table.size()), "allocating a pinned job table");
+            pinned_bytes[k] = table.size();
+        }
+        std::memcpy(pinned[k], table.data(), table.size());
+        jobs.reserve(table.size());
+        cuda_check(cudaMemcpyAsync(jobs.data(), pinned[k], table.size(), cudaMemcpyHostToDevice, stream),
+                   "uploading job table");
+        cuda_check(cudaEventRecord(pinned_done[k], stream), "recording event");
+        device_table = table;
+    }
 
     explicit Workspace(cudaStream_t s) : stream(s) {
         if (!stream) {
@@ -175,6 +202,10 @@ struct Workspace {
     }
     ~Workspace() {
         if (stream) cudaStreamSynchronize(stream);
+        for (int k = 0; k < 2; ++k) {
+            if (pinned[k]) cudaFreeHost(pinned[k]);
+            if (pinned_done[k]) cudaEventDestroy(pinned_done[k]);
+        }
         if (status) cudaFree(status);
         if (status_host) cudaFreeHost(status_host);
         if (owns_stream) cudaStreamDestroy(stream);
@@ -216,6 +247,18 @@ struct Executor::Impl {
         std::uint64_t bytes = 0;
     };
     bool profiling = false;
+    std::vector<cudaEvent_t> event_pool;   // reused across profiling sessions
+    std::size_t events_used = 0;
+
+    // Caller holds `mutex`.
+    cudaEvent_t pooled_event() {
+        if (events_used == event_pool.size()) {
+            cudaEvent_t e = nullptr;
+            cuda_check(cudaEventCreate(&e), "creating event");
+            event_pool.push_back(e);
+        }
+        return event_pool[events_used++];
+    }
     // DSMVC_GB_STREAM=0 keeps every plan on the sequential kernels (the
     // counterpart of the reference's DSMVC_GPU_SOLVE_PARTITION switch).
     bool allow_stream = true;
@@ -535,9 +578,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
         if (count) launches.push_back({key, offset, count, blocks, bytes_moved, record_floats});
     }
     if (launches.empty()) return;
-    ws.jobs.reserve(table.size());
-    cuda_check(cudaMemcpyAsync(ws.jobs.data(), table.data(), table.size(), cudaMemcpyHostToDevice, ws.stream),
-               "uploading job table");
+    ws.upload_table(table);
     for (const auto &l : launches) {
         Record *rec = nullptr;
         if (profiling) {
@@ -546,8 +587,8 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
             rec = &records.back();
             rec->name = kernel_name(l.key);
             rec->bytes = l.bytes;
-            cuda_check(cudaEventCreate(&rec->start), "creating event");
-            cuda_check(cudaEventCreate(&rec->stop), "creating event");
+            rec->start = pooled_event();
+            rec->stop = pooled_event();
             cuda_check(cudaEventRecord(rec->start, ws.stream), "recording event");
         }
         const char *dev_table = ws.jobs.data() + l.offset;
@@ -614,6 +655,7 @@ Executor::~Executor() {
     impl_->slots.clear();
     impl_->stream_spaces.clear();
     impl_->plans.clear();
+    for (auto e : impl_->event_pool) cudaEventDestroy(e);
 }
 
 int Executor::device() const noexcept { return impl_->device; }
@@ -805,11 +847,8 @@ void Executor::check_status(void *stream) {
 void Executor::set_profiling(bool enable) {
     DeviceGuard guard(impl_->device);
     std::scoped_lock lock(impl_->mutex);
-    for (auto &r : impl_->records) {
-        if (r.start) cudaEventDestroy(r.start);
-        if (r.stop) cudaEventDestroy(r.stop);
-    }
     impl_->records.clear();
+    impl_->events_used = 0;
     impl_->profiling = enable;
 }
 

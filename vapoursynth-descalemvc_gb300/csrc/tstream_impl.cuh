@@ -77,6 +77,15 @@ template <> __device__ __forceinline__ float tout<float>(float v, const Conversi
 
 __device__ __forceinline__ float4 tlds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
+// Record strides (floats).  With a compile-time window they are constants,
+// so every record read is an immediate offset from the chunk's base.
+template <int HB, int K> __device__ __forceinline__ int fwd_stride(const dev::StreamPlanView &p) {
+    return K > 0 ? 4 + K + (HB + 3) / 4 * 4 : p.forward_stride;
+}
+template <int HB, int K> __device__ __forceinline__ int bwd_stride(const dev::StreamPlanView &p) {
+    return K > 0 ? ((HB + 3) / 4 * 4 < 4 ? 4 : (HB + 3) / 4 * 4) : p.backward_stride;
+}
+
 // Cooperative ring feeder of one warp.  Block b covers samples
 // [16 b, 16 b + 16) of the warp's 32 vectors.
 template <class In>
@@ -159,7 +168,7 @@ __device__ __forceinline__ void tstage(float *buf, const dev::StreamPlanView &p,
 template <int HB, int LC, int K, class Feed>
 __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::StreamPlanView &p,
                                          const float *fwd, Feed &feed, int lane) {
-    const int fs = p.forward_stride;
+    const int fs = fwd_stride<HB, K>(p);
     const int kw = K > 0 ? K : p.window;
     const int n = p.destination_size;
 #pragma unroll
@@ -211,10 +220,10 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
 
 // Zero-carry backward warm-up over the chunk held in y[LC, 2 LC); leaves the
 // state entering the preceding chunk in `carry`.
-template <int HB, int LC>
+template <int HB, int LC, int K>
 __device__ __forceinline__ void twarmup(const float (&y)[2 * LC], float (&carry)[HB],
                                         const dev::StreamPlanView &p, const float *bwd) {
-    const int bs = p.backward_stride;
+    const int bs = bwd_stride<HB, K>(p);
     float w[HB];
 #pragma unroll
     for (int d = 0; d < HB; ++d) w[d] = 0.0f;
@@ -246,11 +255,11 @@ __device__ __forceinline__ void twarmup(const float (&y)[2 * LC], float (&carry)
 // Final backward substitution of the chunk held in y[B, B + LC) from
 // `carry` (x after the chunk); each x is stored as soon as it is known.
 // Leaves the chunk's first HB x values in `carry`.
-template <int HB, int LC, int B, class Out>
+template <int HB, int LC, int K, int B, class Out>
 __device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB], int j0,
                                           const dev::StreamPlanView &p, const float *bwd, Out *out,
                                           std::int64_t out_elem, bool active, const Conversion &conv) {
-    const int bs = p.backward_stride;
+    const int bs = bwd_stride<HB, K>(p);
     const int n = p.destination_size;
 #pragma unroll
     for (int t = LC - 1; t >= 0; --t) {
@@ -336,18 +345,18 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
         const float *cur = bufs + (c % 3) * per_buffer;
         const float *prev = bufs + ((c + 2) % 3) * per_buffer;
         tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
-        const float *cur_b = cur + kTChunk * p.forward_stride;
+        const float *cur_b = cur + kTChunk * fwd_stride<HB, K>(p);
         const bool last = c + 1 == chunks;
         if (last) {
 #pragma unroll
             for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
-            tbackward<HB, LC, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
+            tbackward<HB, LC, K, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
         } else {
-            twarmup<HB, LC>(y, carry, p, cur_b);
+            twarmup<HB, LC, K>(y, carry, p, cur_b);
         }
         if (c > 0) {
-            tbackward<HB, LC, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * p.forward_stride, out,
-                                 job.out_elem, active, job.conv);
+            tbackward<HB, LC, K, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * fwd_stride<HB, K>(p), out,
+                                    job.out_elem, active, job.conv);
         }
         if (last) break;
         // Every warp is done with chunk c-1's records: fetch chunk c+2.
