@@ -237,6 +237,27 @@ int dsmvc_gb_run_batch(dsmvc_gb_executor *executor,
                        void *stream, int32_t synchronize);
 int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream);
 
+/* Prepared batch: the task list of dsmvc_gb_run_batch routed, packed and
+ * uploaded once (job table, intermediate planes and a status word owned by
+ * the batch), then launched any number of times.  No counterpart in the
+ * reference, whose launch layer rebuilds its launch parameters for every
+ * plane (src/cuda/cuda_launch.hpp:11-149).  dsmvc_gb_batch_launch issues
+ * kernels only -- no copy, allocation or host synchronisation -- so it may
+ * be captured into a CUDA graph; launches of one batch must be ordered (one
+ * stream or a graph) because they share the batch's scratch.
+ * dsmvc_gb_batch_check waits for `stream` and reports Float64 non-finite
+ * data seen by any earlier launch.  The tasks' buffers, their plans and the
+ * executor must outlive the batch. */
+typedef struct dsmvc_gb_batch dsmvc_gb_batch;
+int dsmvc_gb_batch_create(dsmvc_gb_executor *executor,
+                          const dsmvc_gb_plane_task *tasks, int32_t count,
+                          dsmvc_gb_batch **out);
+int dsmvc_gb_batch_launch(dsmvc_gb_batch *batch, void *stream);
+int dsmvc_gb_batch_check(dsmvc_gb_batch *batch, void *stream);
+int dsmvc_gb_batch_info(const dsmvc_gb_batch *batch, int64_t *kernel_launches,
+                        int64_t *scratch_bytes, int64_t *table_bytes);
+void dsmvc_gb_batch_destroy(dsmvc_gb_batch *batch);
+
 /* Allocation-free 2D descale.  No counterpart in the reference.  For callers
  * that cannot allocate device memory (code running inside another
  * framework's memory pool, allocator-free real-time pipelines): the Float32

@@ -1,0 +1,121 @@
+"""Prepared batches (dsmvc_gb_batch_*): packed once, launched many times,
+captured into a CUDA graph.  Bar: every launch writes exactly the bytes that
+dsmvc_gb_run_batch writes for the same task list (same routing, same
+kernels), and those match the oracle within the parity bars of
+test_gpu_parity.py."""
+import numpy as np
+import pytest
+
+import oracle as O
+from common import INT_MAX_CODES, make_input, oracle_request, product_request
+
+pytestmark = pytest.mark.gpu
+
+# Luma and chroma axes of the 1080p -> 810p Lanczos-3 descale, at full size
+# (streaming kernels) and a small bicubic pair (sequential kernels).
+LUMA_H = (1920, 1440, 1440.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "symmetric", 1)
+LUMA_V = (1080, 810, 810.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "symmetric", 1)
+CHROMA_H = (960, 720, 720.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "symmetric", 1)
+CHROMA_V = (540, 405, 405.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "symmetric", 1)
+SMALL_H = (240, 160, 160.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)
+SMALL_V = (135, 90, 90.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1)
+
+
+def _plan(gb, executor, req):
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    executor.prepare(p)
+    return p
+
+
+def _tasks(gb, executor, torch, copies=2):
+    geoms = [(LUMA_H, LUMA_V, "u16"), (CHROMA_H, CHROMA_V, "u16"), (SMALL_H, SMALL_V, "f32")]
+    plans = {}
+    tasks, inputs, outputs, meta = [], [], [], []
+    for i, (hq, vq, sample) in enumerate(geoms * copies):
+        h = plans.setdefault(hq, _plan(gb, executor, hq))
+        v = plans.setdefault(vq, _plan(gb, executor, vq))
+        x = make_input(v.source_size, h.source_size, sample, 300 + i)
+        conv = gb.integer_conversion(16, i % 3 == 1, False) if sample == "u16" else None
+        dx = torch.from_numpy(x.view(np.int16) if sample == "u16" else x).cuda()
+        dy = torch.zeros((v.destination_size, h.destination_size), dtype=dx.dtype, device="cuda")
+        inputs.append(dx)
+        outputs.append(dy)
+        meta.append((hq, vq, x, conv, sample))
+        tasks.append(gb.PlaneTask(h, v, dx.data_ptr(), h.source_size, dy.data_ptr(),
+                                  h.destination_size, 2 if sample == "u16" else 0, 0, conv))
+    return tasks, inputs, outputs, meta
+
+
+def _snapshot(outputs):
+    return [y.cpu().numpy().copy() for y in outputs]
+
+
+def test_prepared_batch_matches_run_batch(gb, executor):
+    torch = pytest.importorskip("torch")
+    tasks, _inputs, outputs, meta = _tasks(gb, executor, torch)
+    sid = torch.cuda.current_stream().cuda_stream
+    executor.run_batch(tasks, stream=sid, synchronize=True)
+    want = _snapshot(outputs)
+    batch = executor.prepare_batch(tasks)
+    info = batch.info()
+    assert info["kernel_launches"] >= 2 and info["scratch_bytes"] > 0 and info["table_bytes"] > 0
+    for _ in range(3):
+        for y in outputs:
+            y.zero_()
+        batch.launch(sid)
+        batch.check(sid)
+        for got, exp in zip(_snapshot(outputs), want):
+            assert np.array_equal(got, exp)
+    # One plane of each kind against the oracle's CPU scalar route.
+    for (hq, vq, x, conv, sample), got in list(zip(meta, want))[:3]:
+        oh, ov = O.Plan(oracle_request(hq)), O.Plan(oracle_request(vq))
+        ref = O.inverse_2d(oh, ov, x, conv)
+        if sample == "u16":
+            diff = np.abs(got.view(np.uint16).astype(np.int64) - ref.astype(np.int64))
+            assert diff.max() <= INT_MAX_CODES
+        else:
+            assert np.abs(got - ref).max() <= 2e-5
+
+
+def test_prepared_batch_graph_replay(gb, executor):
+    torch = pytest.importorskip("torch")
+    tasks, _inputs, outputs, _meta = _tasks(gb, executor, torch, copies=1)
+    batch = executor.prepare_batch(tasks)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        batch.launch(side.cuda_stream)       # warm launch outside the capture
+    torch.cuda.synchronize()
+    want = _snapshot(outputs)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        batch.launch(side.cuda_stream)
+    for _ in range(2):
+        for y in outputs:
+            y.zero_()
+        torch.cuda.synchronize()
+        graph.replay()
+        torch.cuda.synchronize()
+        for got, exp in zip(_snapshot(outputs), want):
+            assert np.array_equal(got, exp)
+    batch.check(side.cuda_stream)
+
+
+def test_prepared_batch_float64_status(gb, executor):
+    torch = pytest.importorskip("torch")
+    req = (40, 30, 30.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2)
+    p = _plan(gb, executor, req)
+    x = np.random.default_rng(5).random((40, 40), dtype=np.float32)
+    x[3, 7] = np.inf
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.empty((30, 30), dtype=torch.float32, device="cuda")
+    batch = executor.prepare_batch([gb.PlaneTask(p, p, dx.data_ptr(), 40, dy.data_ptr(), 30, 0, 0, None)])
+    sid = torch.cuda.current_stream().cuda_stream
+    batch.launch(sid)
+    with pytest.raises(gb.DescaleError):
+        batch.check(sid)
+    # The status is cleared by the check; finite input then passes.
+    dx.copy_(torch.from_numpy(np.random.default_rng(6).random((40, 40), dtype=np.float32)))
+    batch.launch(sid)
+    batch.check(sid)
+    assert torch.isfinite(dy).all()

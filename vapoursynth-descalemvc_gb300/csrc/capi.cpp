@@ -314,30 +314,76 @@ int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor, const dsmvc_gb_plan *ho
     });
 }
 
+namespace {
+
+std::vector<dsmvc_gb::PlaneTask> task_list(const dsmvc_gb_plane_task *tasks, int32_t count) {
+    if (count < 0 || (count > 0 && !tasks)) throw std::invalid_argument("invalid task list");
+    std::vector<dsmvc_gb::PlaneTask> list(static_cast<std::size_t>(count));
+    for (int32_t i = 0; i < count; ++i) {
+        const auto &t = tasks[i];
+        if (t.sample < DSMVC_GB_FLOAT32 || t.sample > DSMVC_GB_UINT16)
+            throw std::invalid_argument("sample kind is invalid");
+        auto &d = list[static_cast<std::size_t>(i)];
+        d.horizontal = t.horizontal ? &plan_of(t.horizontal) : nullptr;
+        d.vertical = t.vertical ? &plan_of(t.vertical) : nullptr;
+        d.input = t.input;
+        d.input_stride = t.input_stride;
+        d.output = t.output;
+        d.output_stride = t.output_stride;
+        d.sample = static_cast<dsmvc_gb::dev::Sample>(t.sample);
+        d.vectors = t.vectors;
+        d.conversion = to_conversion(&t.conversion);
+    }
+    return list;
+}
+
+} // namespace
+
 int dsmvc_gb_run_batch(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task *tasks, int32_t count,
                        void *stream, int32_t synchronize) {
+    return guarded([&] { exec_of(executor).run_batch(task_list(tasks, count), stream, synchronize != 0); });
+}
+
+struct dsmvc_gb_batch {
+    std::unique_ptr<dsmvc_gb::PreparedBatch> batch;
+};
+
+int dsmvc_gb_batch_create(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task *tasks, int32_t count,
+                          dsmvc_gb_batch **out) {
     return guarded([&] {
-        auto &ex = exec_of(executor);
-        if (count < 0 || (count > 0 && !tasks)) throw std::invalid_argument("invalid task list");
-        std::vector<dsmvc_gb::PlaneTask> list(static_cast<std::size_t>(count));
-        for (int32_t i = 0; i < count; ++i) {
-            const auto &t = tasks[i];
-            if (t.sample < DSMVC_GB_FLOAT32 || t.sample > DSMVC_GB_UINT16)
-                throw std::invalid_argument("sample kind is invalid");
-            auto &d = list[static_cast<std::size_t>(i)];
-            d.horizontal = t.horizontal ? &plan_of(t.horizontal) : nullptr;
-            d.vertical = t.vertical ? &plan_of(t.vertical) : nullptr;
-            d.input = t.input;
-            d.input_stride = t.input_stride;
-            d.output = t.output;
-            d.output_stride = t.output_stride;
-            d.sample = static_cast<dsmvc_gb::dev::Sample>(t.sample);
-            d.vectors = t.vectors;
-            d.conversion = to_conversion(&t.conversion);
-        }
-        ex.run_batch(list, stream, synchronize != 0);
+        if (!out) throw std::invalid_argument("output pointer is null");
+        *out = nullptr;
+        auto b = std::make_unique<dsmvc_gb_batch>();
+        b->batch = exec_of(executor).prepare_batch(task_list(tasks, count));
+        *out = b.release();
     });
 }
+
+int dsmvc_gb_batch_launch(dsmvc_gb_batch *batch, void *stream) {
+    return guarded([&] {
+        if (!batch) throw std::invalid_argument("batch is null");
+        batch->batch->launch(stream);
+    });
+}
+
+int dsmvc_gb_batch_check(dsmvc_gb_batch *batch, void *stream) {
+    return guarded([&] {
+        if (!batch) throw std::invalid_argument("batch is null");
+        batch->batch->check_status(stream);
+    });
+}
+
+int dsmvc_gb_batch_info(const dsmvc_gb_batch *batch, int64_t *kernel_launches, int64_t *scratch_bytes,
+                        int64_t *table_bytes) {
+    return guarded([&] {
+        if (!batch) throw std::invalid_argument("batch is null");
+        if (kernel_launches) *kernel_launches = static_cast<int64_t>(batch->batch->kernel_launches());
+        if (scratch_bytes) *scratch_bytes = static_cast<int64_t>(batch->batch->scratch_bytes());
+        if (table_bytes) *table_bytes = static_cast<int64_t>(batch->batch->table_bytes());
+    });
+}
+
+void dsmvc_gb_batch_destroy(dsmvc_gb_batch *batch) { delete batch; }
 
 int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream) {
     return guarded([&] { exec_of(executor).check_status(stream); });

@@ -26,6 +26,7 @@
 #include <string>
 #include <tuple>
 #include <cstdlib>
+#include <functional>
 #include <unordered_map>
 
 namespace dsmvc_gb {
@@ -38,6 +39,7 @@ void cuda_check(cudaError_t e, const char *what) {
 void cuda_check(int e, const char *what) { cuda_check(static_cast<cudaError_t>(e), what); }
 
 constexpr std::size_t kAlign = 256;
+constexpr int kSeqThreads = 128;   // threads per block of the sequential kernels
 std::size_t align_up(std::size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 std::size_t sample_bytes(dev::Sample s) {
@@ -312,6 +314,26 @@ struct Executor::Impl {
         return *ws;
     }
 
+    // A routed, packed submission: launch groups over one job table.
+    struct Launch {
+        int pass, kind, hb;
+        dev::Sample in, out;
+        int variant;
+        std::size_t offset;
+        int count, blocks;
+        std::uint64_t bytes;
+        int record_floats;
+    };
+    struct Compiled {
+        std::vector<std::unique_ptr<DevicePlan>> temporaries;
+        std::vector<char> table;
+        std::vector<Launch> launches;
+        std::size_t scratch_bytes = 0;
+        std::size_t tasks = 0;
+    };
+    void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
+                 const std::function<char *(std::size_t)> &scratch);
+    void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
     void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks);
     void finish(Workspace &ws);
 };
@@ -351,8 +373,9 @@ std::string kernel_name(const GroupKey &k) {
 
 } // namespace
 
-void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks) {
-    std::vector<std::unique_ptr<DevicePlan>> temporaries;
+void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
+                             const std::function<char *(std::size_t)> &scratch) {
+    auto &temporaries = out.temporaries;
     // Per task: which kernels run each pass, and the scratch they need.
     struct Route {
         const DevicePlan *h = nullptr, *v = nullptr;
@@ -409,8 +432,8 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
             bytes += align_up(r.fwd_stride * lines * 8);
         }
     }
-    ws.scratch.reserve(std::max<std::size_t>(bytes, kAlign));
-    char *base = ws.scratch.data();
+    out.scratch_bytes = bytes;
+    char *base = scratch(std::max<std::size_t>(bytes, kAlign));
 
     struct Item {
         dev::AxisJob axis{};
@@ -548,12 +571,11 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
 
     // One job table for every group: AxisJob and StreamJob records share a
     // byte buffer, each group's records contiguous and 256-byte aligned.
-    constexpr int kSeqThreads = 128;
     const int stream_block = stream_threads();
-    struct Launch { GroupKey key; std::size_t offset; int count; int blocks; std::uint64_t bytes; int record_floats; };
-    std::vector<Launch> launches;
-    std::vector<char> &table = ws.host_table;
+    std::vector<Launch> &launches = out.launches;
+    std::vector<char> &table = out.table;
     table.clear();
+    launches.clear();
     for (auto &[key, items] : groups) {
         const bool is_stream = key.kind >= 2;
         const int per_block = is_stream ? stream_block : kSeqThreads;
@@ -575,48 +597,62 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
             table.insert(table.end(), src, src + rec);
             ++count;
         }
-        if (count) launches.push_back({key, offset, count, blocks, bytes_moved, record_floats});
+        if (count)
+            launches.push_back({key.pass, key.kind, key.hb, key.in, key.out, key.variant, offset, count, blocks,
+                                bytes_moved, record_floats});
     }
-    if (launches.empty()) return;
-    ws.upload_table(table);
-    for (const auto &l : launches) {
+    out.tasks = tasks.size();
+}
+
+void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStream_t stream,
+                            std::uint32_t *status) {
+    for (const auto &l : c.launches) {
         Record *rec = nullptr;
         if (profiling) {
             std::scoped_lock lock(mutex);
             records.emplace_back();
             rec = &records.back();
-            rec->name = kernel_name(l.key);
+            rec->name = kernel_name({l.pass, l.kind, l.hb, l.in, l.out, l.variant});
             rec->bytes = l.bytes;
             rec->start = pooled_event();
             rec->stop = pooled_event();
-            cuda_check(cudaEventRecord(rec->start, ws.stream), "recording event");
+            cuda_check(cudaEventRecord(rec->start, stream), "recording event");
         }
-        const char *dev_table = ws.jobs.data() + l.offset;
+        const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.key.kind == 3) {
+        if (l.kind == 3) {
             rc = launch_tstream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
-                                l.key.hb, l.key.variant ? 8 : 0, l.key.in, l.key.out, l.record_floats,
-                                ws.stream);
-        } else if (l.key.kind == 2) {
+                                l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats,
+                                stream);
+        } else if (l.kind == 2) {
             rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
-                               l.key.hb, kStreamChunk, l.key.pass == 0, l.key.in, l.key.out, l.record_floats,
-                               ws.stream);
-        } else if (l.key.kind == 1) {
+                               l.hb, kStreamChunk, l.pass == 0, l.in, l.out, l.record_floats,
+                               stream);
+        } else if (l.kind == 1) {
             rc = launch_axis_f64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
-                                 kSeqThreads, l.key.hb, l.key.in, l.key.out, ws.status, ws.stream);
+                                 kSeqThreads, l.hb, l.in, l.out, status, stream);
         } else {
             rc = launch_axis_f32(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
-                                 kSeqThreads, l.key.hb, l.key.in, l.key.out, ws.stream);
+                                 kSeqThreads, l.hb, l.in, l.out, stream);
         }
         cuda_check(rc, "launching axis kernel");
-        if (rec) cuda_check(cudaEventRecord(rec->stop, ws.stream), "recording event");
+        if (rec) cuda_check(cudaEventRecord(rec->stop, stream), "recording event");
     }
-    {
-        std::scoped_lock lock(mutex);
-        stats.launches += launches.size();
-        stats.plane_tasks += tasks.size();
-    }
-    if (!temporaries.empty()) {
+    std::scoped_lock lock(mutex);
+    stats.launches += c.launches.size();
+    stats.plane_tasks += c.tasks;
+}
+
+void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks) {
+    Compiled c;
+    compile(tasks, c, [&](std::size_t bytes) {
+        ws.scratch.reserve(bytes);
+        return ws.scratch.data();
+    });
+    if (c.launches.empty()) return;
+    ws.upload_table(c.table);
+    launch(c, ws.jobs.data(), ws.stream, ws.status);
+    if (!c.temporaries.empty()) {
         // Private plan copies must outlive the kernels that read them.
         cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
     }
@@ -815,8 +851,9 @@ void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample samp
     impl_->release_slot(slot);
 }
 
-void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize) {
-    DeviceGuard guard(impl_->device);
+namespace {
+
+void validate_tasks(const std::vector<PlaneTask> &tasks) {
     for (const auto &t : tasks) {
         const AxisPlan *h = t.horizontal, *v = t.vertical;
         if ((!h && !v) || !t.input || !t.output || (h && !h->valid()) || (v && !v->valid()))
@@ -834,9 +871,84 @@ void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool
                 throw std::invalid_argument("invalid batch column task");
         }
     }
+}
+
+} // namespace
+
+void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize) {
+    DeviceGuard guard(impl_->device);
+    validate_tasks(tasks);
     Workspace &ws = impl_->stream_space(static_cast<cudaStream_t>(stream));
     impl_->enqueue(ws, tasks);
     if (synchronize) impl_->finish(ws);
+}
+
+struct PreparedBatch::Impl {
+    Executor::Impl *owner = nullptr;
+    Executor::Impl::Compiled compiled;
+    DeviceBuffer scratch;
+    DeviceBuffer table;
+    std::uint32_t *status = nullptr;       // device
+    std::uint32_t *status_host = nullptr;  // pinned
+    ~Impl() {
+        if (status) cudaFree(status);
+        if (status_host) cudaFreeHost(status_host);
+    }
+};
+
+PreparedBatch::PreparedBatch(std::unique_ptr<Impl> impl) : impl_(std::move(impl)) {}
+
+PreparedBatch::~PreparedBatch() {
+    if (!impl_) return;
+    DeviceGuard guard(impl_->owner->device);
+    // Kernels of an earlier launch may still read the table and scratch.
+    cudaDeviceSynchronize();
+    impl_.reset();
+}
+
+void PreparedBatch::launch(void *stream) {
+    DeviceGuard guard(impl_->owner->device);
+    impl_->owner->launch(impl_->compiled, impl_->table.data(), static_cast<cudaStream_t>(stream),
+                         impl_->status);
+}
+
+void PreparedBatch::check_status(void *stream) {
+    DeviceGuard guard(impl_->owner->device);
+    auto s = static_cast<cudaStream_t>(stream);
+    cuda_check(cudaMemcpyAsync(impl_->status_host, impl_->status, sizeof(std::uint32_t),
+                               cudaMemcpyDeviceToHost, s), "reading status");
+    cuda_check(cudaStreamSynchronize(s), "synchronizing");
+    const std::uint32_t status = *impl_->status_host;
+    if (status) {
+        cuda_check(cudaMemset(impl_->status, 0, sizeof(std::uint32_t)), "clearing status");
+        if (status & dev::kStatusNonFiniteInput)
+            throw std::runtime_error("Float64 input contains NaN or infinity");
+        throw std::runtime_error("Float64 execution produced NaN or infinity");
+    }
+}
+
+std::size_t PreparedBatch::kernel_launches() const { return impl_->compiled.launches.size(); }
+std::size_t PreparedBatch::scratch_bytes() const { return impl_->compiled.scratch_bytes; }
+std::size_t PreparedBatch::table_bytes() const { return impl_->compiled.table.size(); }
+
+std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks) {
+    DeviceGuard guard(impl_->device);
+    validate_tasks(tasks);
+    auto b = std::make_unique<PreparedBatch::Impl>();
+    b->owner = impl_.get();
+    impl_->compile(tasks, b->compiled, [&](std::size_t bytes) {
+        b->scratch.reserve(bytes);
+        return b->scratch.data();
+    });
+    const auto &table = b->compiled.table;
+    b->table.reserve(std::max<std::size_t>(table.size(), 1));
+    if (!table.empty())
+        cuda_check(cudaMemcpy(b->table.data(), table.data(), table.size(), cudaMemcpyHostToDevice),
+                   "uploading job table");
+    cuda_check(cudaMalloc(&b->status, sizeof(std::uint32_t)), "allocating status");
+    cuda_check(cudaMallocHost(&b->status_host, sizeof(std::uint32_t)), "allocating status");
+    cuda_check(cudaMemset(b->status, 0, sizeof(std::uint32_t)), "clearing status");
+    return std::make_unique<PreparedBatch>(std::move(b));
 }
 
 void Executor::check_status(void *stream) {

@@ -63,6 +63,32 @@ struct ExecutorStats {
     std::size_t workspace_bytes = 0;
 };
 
+class Executor;
+
+// A batch routed and packed once, with its own job table, scratch and status
+// word on the device, then launched any number of times.  launch() issues
+// kernels only (no copies, no allocation, no host synchronisation), so it
+// can be captured into a CUDA graph.  The tasks' buffers and plans, and the
+// executor, must outlive the batch.
+class PreparedBatch {
+public:
+    struct Impl;
+    explicit PreparedBatch(std::unique_ptr<Impl> impl);
+    ~PreparedBatch();
+    PreparedBatch(const PreparedBatch &) = delete;
+    PreparedBatch &operator=(const PreparedBatch &) = delete;
+
+    void launch(void *stream);
+    // Waits for `stream` and raises on a Float64 non-finite status (clears it).
+    void check_status(void *stream);
+    [[nodiscard]] std::size_t kernel_launches() const;
+    [[nodiscard]] std::size_t scratch_bytes() const;
+    [[nodiscard]] std::size_t table_bytes() const;
+
+private:
+    std::unique_ptr<Impl> impl_;
+};
+
 class Executor {
 public:
     explicit Executor(int device = -1);
@@ -91,6 +117,8 @@ public:
     // Float64 non-finite status; otherwise check_status() does that later.
     void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize);
     void check_status(void *stream);
+    // Validates, routes and uploads `tasks` once (see PreparedBatch).
+    [[nodiscard]] std::unique_ptr<PreparedBatch> prepare_batch(const std::vector<PlaneTask> &tasks);
 
     [[nodiscard]] ExecutorStats stats() const;
 

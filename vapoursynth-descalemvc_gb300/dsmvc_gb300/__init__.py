@@ -131,6 +131,13 @@ SIGNATURES = {
     "dsmvc_gb_run_batch": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_void_p,
                             C.c_int32], C.c_int),
     "dsmvc_gb_stream_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_batch_create": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32,
+                               C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_batch_launch": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_batch_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_batch_info": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                             C.POINTER(C.c_int64)], C.c_int),
+    "dsmvc_gb_batch_destroy": ([C.c_void_p], None),
     "dsmvc_gb_inverse_2d_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                      C.c_void_p, C.c_int64, C.POINTER(ConversionC), C.c_void_p],
                                     C.c_int),
@@ -374,15 +381,14 @@ class Executor:
 
     # -- device-resident batches ------------------------------------------
     def run_batch(self, tasks: Sequence[PlaneTask], stream: int = 0, synchronize: bool = True):
-        arr = (PlaneTaskC * len(tasks))()
-        for i, t in enumerate(tasks):
-            arr[i] = PlaneTaskC(t.horizontal.handle if t.horizontal else None,
-                                t.vertical.handle if t.vertical else None,
-                                int(t.input), int(t.input_stride), int(t.output),
-                                int(t.output_stride), int(t.sample), int(t.vectors),
-                                _conv(t.conversion))
+        arr = _task_array(tasks)
         _check(lib().dsmvc_gb_run_batch(self._h, arr, len(tasks), C.c_void_p(stream or None),
                                         1 if synchronize else 0))
+
+    def prepare_batch(self, tasks: Sequence[PlaneTask]) -> "PreparedBatch":
+        """Routes and uploads `tasks` once; PreparedBatch.launch() then
+        issues only the kernels (capturable into a CUDA graph)."""
+        return PreparedBatch(self, tasks)
 
     def stream_check(self, stream: int = 0) -> None:
         _check(lib().dsmvc_gb_stream_check(self._h, C.c_void_p(stream or None)))
@@ -398,6 +404,47 @@ class Executor:
         return [{"name": buf[i].name.decode(), "launches": buf[i].launches,
                  "milliseconds": buf[i].milliseconds, "bytes": buf[i].bytes}
                 for i in range(min(n.value, 64))]
+
+
+def _task_array(tasks: Sequence[PlaneTask]):
+    arr = (PlaneTaskC * len(tasks))()
+    for i, t in enumerate(tasks):
+        arr[i] = PlaneTaskC(t.horizontal.handle if t.horizontal else None,
+                            t.vertical.handle if t.vertical else None,
+                            int(t.input), int(t.input_stride), int(t.output),
+                            int(t.output_stride), int(t.sample), int(t.vectors),
+                            _conv(t.conversion))
+    return arr
+
+
+class PreparedBatch:
+    """A task list packed once (dsmvc_gb_batch_create); keeps its executor
+    and plans alive.  The task buffers must outlive it."""
+
+    def __init__(self, executor: Executor, tasks: Sequence[PlaneTask]):
+        h = C.c_void_p()
+        _check(lib().dsmvc_gb_batch_create(executor._h, _task_array(tasks), len(tasks), C.byref(h)))
+        self._h = h
+        self._executor = executor
+        self._plans = [p for t in tasks for p in (t.horizontal, t.vertical) if p is not None]
+
+    def launch(self, stream: int = 0) -> None:
+        _check(lib().dsmvc_gb_batch_launch(self._h, C.c_void_p(stream or None)))
+
+    def check(self, stream: int = 0) -> None:
+        _check(lib().dsmvc_gb_batch_check(self._h, C.c_void_p(stream or None)))
+
+    def info(self) -> dict:
+        k, s, t = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().dsmvc_gb_batch_info(self._h, C.byref(k), C.byref(s), C.byref(t)))
+        return {"kernel_launches": k.value, "scratch_bytes": s.value, "table_bytes": t.value}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
+            _lib.dsmvc_gb_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
 
 
 NOALLOC_SCRATCH_BYTES = 32 << 20
