@@ -342,7 +342,7 @@ def main():
     value = world * args.steps * pix_step / (elapsed_ms / 1e3) / 1e6
 
     # End to end: the synchronous host-frame calls of the C ABI, pinned host
-    # planes, 8 caller threads (the plugin's frame-parallel requests).
+    # planes, 16 caller threads (the plugin's frame-parallel requests).
     host_in, host_out, calls = [], [], []
     for f in range(0 if args.kernels_only else FRAMES):
         for idx, plane in enumerate(frames[f % len(frames)]):
@@ -364,7 +364,7 @@ def main():
 
     e2e = None
     if calls:
-        with cf.ThreadPoolExecutor(max_workers=8) as pool:
+        with cf.ThreadPoolExecutor(max_workers=16) as pool:
             list(pool.map(call, calls))  # warm-up
             if dist is not None:
                 dist.barrier()

@@ -238,6 +238,11 @@ struct Executor::Impl {
     // execution slots, src/cuda/cuda_executor.cpp:1102-1160).
     std::vector<std::unique_ptr<Workspace>> slots;
     std::vector<bool> slot_busy;
+    // At most this many host calls run at once, each on its own stream
+    // (DSMVC_GB_STREAMS=1..16, the counterpart of DSMVC_CUDA_STREAMS,
+    // src/cuda/cuda_executor.cpp:105-118).  A single plane fills only a few
+    // SMs, so concurrent calls are what keeps the GPU busy.
+    std::size_t max_slots = 16;
     std::condition_variable slot_free;
     std::map<cudaStream_t, std::unique_ptr<Workspace>> stream_spaces;
     ExecutorStats stats;
@@ -289,7 +294,7 @@ struct Executor::Impl {
                     return *slots[i];
                 }
             }
-            if (slots.size() < 4) {
+            if (slots.size() < max_slots) {
                 slots.push_back(std::make_unique<Workspace>(nullptr));
                 slot_busy.push_back(true);
                 index = slots.size() - 1;
@@ -681,6 +686,11 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     impl_->device = device;
     if (const char *env = std::getenv("DSMVC_GB_STREAM"); env && std::string(env) == "0")
         impl_->allow_stream = false;
+    if (const char *env = std::getenv("DSMVC_GB_STREAMS")) {
+        char *end = nullptr;
+        const long v = std::strtol(env, &end, 10);
+        if (end && *end == '\0' && v >= 1 && v <= 16) impl_->max_slots = static_cast<std::size_t>(v);
+    }
     DeviceGuard guard(device);
     cuda_check(cudaFree(nullptr), "initialising the primary context");
 }
