@@ -37,6 +37,10 @@ SRC_W, SRC_H, DST_W, DST_H = 1920, 1080, 1440, 810
 FRAMES = 64
 KERNEL = dict(kernel="lanczos", taps=3, b=0.0, c=0.5, blur=1.0, border="repeat", f64_mode=0)
 METRIC = "descale Mpix/s (source pixels, Delanczos YUV420P16 1920x1080->1440x810)"
+# DRAM bytes (read + write) per frame of both passes, from one ncu capture of
+# the 24-frame cut of this workload (profiles/tstream_c1_24frames_full.md:
+# 614.6 MB per 24 frames; traffic grows with the frame count).
+DRAM_BYTES_PER_FRAME = 614.6e6 / 24
 
 
 def peaks():
@@ -237,6 +241,121 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+SWEEP_W, SWEEP_H = 1920, 1080
+SWEEP_HEIGHTS = range(500, 1001)
+SWEEP_METRIC = "candidate solves/s (1920x1080 GRAYS sweep, heights 500..1000, 3 kernels)"
+
+
+def run_sweep(args, rank, world):
+    """Batched candidate sweep: one 1920x1080 GRAYS float32 frame built from a
+    hidden base height drawn from the seed in [600, 900], descaled to every
+    height 500..1000 (width round(16 h / 9), even) with Debicubic(0, 0.5),
+    Debilinear and Delanczos(3), each result re-upscaled and scored by mean
+    absolute error: 1503 candidates per step, one CUDA graph per step.  Warm
+    = plans resident; cold = host planning + sweep preparation + one run;
+    plain = the same candidates one at a time, each waited for."""
+    import torch
+    import dsmvc_gb300 as gb
+    from dsmvc_gb300 import synthetic
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    base_h = int(rng.integers(600, 901))
+    frame = synthetic.gray_frame(SWEEP_W, SWEEP_H, synthetic.sweep_width(base_h, SWEEP_W / SWEEP_H),
+                                 base_h, seed=args.seed + 1)
+    cands = synthetic.native_resolution_candidates(SWEEP_W, SWEEP_H, SWEEP_HEIGHTS)
+    reqs = [r for c in cands for r in (c[3], c[4])]
+    dframe = torch.from_numpy(frame).cuda()
+    ex = gb.Executor(local)
+    stream = torch.cuda.Stream()
+    sid = stream.cuda_stream
+    torch.cuda.synchronize()
+
+    t0 = time.perf_counter()
+    plans = gb.build_plans(reqs, threads=0)
+    t_plan = time.perf_counter() - t0
+    pairs = [(plans[2 * i], plans[2 * i + 1]) for i in range(len(cands))]
+    for p in plans:
+        ex.prepare(p)
+    t1 = time.perf_counter()
+    sweep = gb.Sweep(ex, pairs, dframe.data_ptr(), SWEEP_W, autotune=True, graph=True)
+    sweep.run(sid)
+    scores = sweep.scores(sid)
+    t_cold = time.perf_counter() - t0
+    t_prepare = time.perf_counter() - t1
+    info = sweep.info()
+
+    for _ in range(args.warmup):
+        sweep.run(sid)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                sweep.run(sid)
+            stop.record(stream)
+        stream.synchronize()
+    ms = start.elapsed_time(stop) / args.steps
+    warm = len(cands) / (ms / 1e3)
+
+    # End to end: the frame uploaded from pinned host memory and the scores
+    # read back every step.
+    pinned = torch.from_numpy(frame).pin_memory()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            dframe.copy_(pinned, non_blocking=True)
+        sweep.run(sid)
+        scores = sweep.scores(sid)
+    e2e = e2e_steps * len(cands) / (time.perf_counter() - t2)
+
+    t3 = time.perf_counter()
+    sweep.run_plain(sid)
+    plain_scores = sweep.scores(sid)
+    plain = len(cands) / (time.perf_counter() - t3)
+    best = int(np.argmin(scores))
+
+    hbm, peak_kind = peaks()
+    out_bytes = sum(c[1] * c[2] * 4 for c in cands)
+    plan_bytes = sum(int(p.storage_bytes) for p in plans)
+    algo = out_bytes + plan_bytes + frame.nbytes
+    achieved = algo / (ms / 1e3) / 1e9
+    if rank != 0:
+        return
+    line = {
+        "metric": SWEEP_METRIC, "value": warm, "unit": "candidates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C3 sweep: 1920x1080 GRAYS f32, heights 500..1000, "
+                               "bicubic(0,0.5)/bilinear/lanczos3, mean-L1 score",
+                   "candidates": len(cands), "hidden_base_height": base_h,
+                   "l2": "per-step outputs (6.2 GB) larger than L2; no flush",
+                   "parallelism": "replicas"},
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e, "unit": "candidates/s", "h2d_bytes_per_step": frame.nbytes,
+                "d2h_bytes_per_step": 4 * len(cands)},
+        "gpu_launches": info["kernel_launches"] * args.steps,
+        "plain_per_candidate": {"value": plain, "unit": "candidates/s",
+                                "speedup_batched": warm / plain,
+                                "scores_identical": bool(np.array_equal(plain_scores, scores))},
+        "cold": {"value": len(cands) / t_cold, "unit": "candidates/s", "planning_s": t_plan,
+                 "prepare_s": t_prepare, "seconds": t_cold},
+        "sweep": {"waves": info["waves"], "device_bytes": info["device_bytes"],
+                  "tune_ms": info["tune_milliseconds"], "segment_rows": info["segment_rows"],
+                  "best": {"kernel": cands[best][0], "width": cands[best][1],
+                           "height": cands[best][2], "score": float(scores[best])},
+                  "found_base_height": cands[best][2] == base_h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes": algo,
+                     "kernel": "whole sweep graph (descale passes + scoring)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def workload_config():
     return {"workload": "Delanczos(taps=3) YUV420P16 1920x1080->1440x810, 64 frames, "
                         "f64mode=0, padding=1",
@@ -257,6 +376,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per step (profiling runs use fewer; the benchmark line uses 64)")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
+                    help="c1: Delanczos YUV420P16 frames (default); c3: candidate sweep")
+    ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--kernels-only", action="store_true",
                     help="skip the end-to-end and CPU legs (profiling runs)")
     args = ap.parse_args()
@@ -272,6 +394,12 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+    if args.workload == "c3" and args.impl != "reference":
+        run_sweep(args, rank, world)
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         if dist is not None:
@@ -398,7 +526,9 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
+                     "frac": achieved / hbm,
+                     "traffic": DRAM_BYTES_PER_FRAME * FRAMES,
+                     "algorithmic_bytes": total_bytes / max(1, args.steps),
                      "peak_source": peak_kind,
                      "kernel": "2D descale (horizontal + vertical passes per step)",
                      "kernels": [dict(k, share=k["milliseconds"] / total_ms) for k in ktimes],

@@ -148,6 +148,13 @@ int dsmvc_gb_plan_get_or_build(const dsmvc_gb_axis_request *request,
                                dsmvc_gb_custom_kernel custom, void *user,
                                dsmvc_gb_plan **out);
 void dsmvc_gb_plan_release(dsmvc_gb_plan *plan);
+/* Builds `count` plans (no custom kernels) on up to `threads` host threads
+ * (0 = one per hardware thread); the reference builds a sweep's plans one
+ * Descale call at a time.  On failure no plan is returned and the message
+ * names the first failing index. */
+int dsmvc_gb_plan_build_many(const dsmvc_gb_axis_request *requests,
+                             int32_t count, int32_t threads,
+                             dsmvc_gb_plan **out);
 int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out);
 /* Read-only view of one plan array: 0 transpose_offsets (u32),
  * 1 transpose_indices (i32), 2 transpose_weights (f32), 3 lower_ld (f32),
@@ -281,6 +288,47 @@ int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal,
                                 void *output, int64_t output_stride,
                                 const dsmvc_gb_conversion *conversion,
                                 void *stream);
+
+/* Batched candidate sweep (the reference's native-resolution scan, where
+ * each candidate is a Descale call, a resize back to the source size and a
+ * PlaneStats average, docs/release-benchmark.md "getfnative"): every
+ * candidate (a horizontal and a vertical plan over the same source size) is
+ * descaled from one device frame, re-upscaled with its plans' forward
+ * operators and scored by the mean absolute error against the frame.  The
+ * candidates run in waves within `memory_budget` bytes (0 = 32 GiB), one
+ * prepared batch per wave, the whole sweep captured into one CUDA graph
+ * (`graph`), with CTA sizes and the scoring row segment chosen by timing the
+ * alternatives on the first wave (`autotune`).  dsmvc_gb_sweep_run enqueues
+ * the sweep on `stream`; dsmvc_gb_sweep_run_plain runs the same candidates one
+ * at a time, each waited for (the per-frame baseline); dsmvc_gb_sweep_scores
+ * waits and copies `count` scores in candidate order.  The frame and the
+ * plans must outlive the sweep (the sweep keeps its own plan references). */
+typedef struct dsmvc_gb_sweep dsmvc_gb_sweep;
+typedef struct dsmvc_gb_sweep_options {
+    int64_t memory_budget;
+    int32_t autotune;
+    int32_t graph;
+} dsmvc_gb_sweep_options;
+typedef struct dsmvc_gb_sweep_info {
+    int32_t candidates;
+    int32_t waves;
+    int64_t device_bytes;
+    int64_t kernel_launches;      /* per dsmvc_gb_sweep_run */
+    double tune_milliseconds;
+    int32_t segment_rows;
+    int32_t tuned_groups;
+} dsmvc_gb_sweep_info;
+int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor,
+                          const dsmvc_gb_plan *const *horizontal,
+                          const dsmvc_gb_plan *const *vertical, int32_t count,
+                          const float *frame, int64_t frame_stride,
+                          const dsmvc_gb_sweep_options *options,
+                          dsmvc_gb_sweep **out);
+int dsmvc_gb_sweep_run(dsmvc_gb_sweep *sweep, void *stream);
+int dsmvc_gb_sweep_run_plain(dsmvc_gb_sweep *sweep, void *stream);
+int dsmvc_gb_sweep_scores(dsmvc_gb_sweep *sweep, float *scores, void *stream);
+int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *out);
+void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep);
 
 /* Kernel timing (the reference's NVTX ranges, src/cuda/nvtx.hpp:11-60, are
  * replaced by CUDA events): while enabled, every launch is bracketed by

@@ -4,11 +4,15 @@
 
 #include "executor.hpp"
 #include "noalloc.hpp"
+#include "sweep.hpp"
 #include "planner.hpp"
 #include "stream.cuh"
 #include "stream_plan.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -144,6 +148,41 @@ int dsmvc_gb_plan_get_or_build(const dsmvc_gb_axis_request *request, dsmvc_gb_cu
 }
 
 void dsmvc_gb_plan_release(dsmvc_gb_plan *plan) { delete plan; }
+
+int dsmvc_gb_plan_build_many(const dsmvc_gb_axis_request *requests, int32_t count, int32_t threads,
+                             dsmvc_gb_plan **out) {
+    return guarded([&] {
+        if (count < 0 || (count > 0 && (!requests || !out))) throw std::invalid_argument("invalid plan list");
+        std::vector<dsmvc_gb::AxisRequest> qs;
+        qs.reserve(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) qs.push_back(to_request(&requests[i]));
+        for (int32_t i = 0; i < count; ++i) out[i] = nullptr;
+        std::vector<std::shared_ptr<const dsmvc_gb::AxisPlan>> built(static_cast<std::size_t>(count));
+        std::vector<std::string> errors(static_cast<std::size_t>(count));
+        std::atomic<int32_t> next{0};
+        auto worker = [&] {
+            for (int32_t i = next++; i < count; i = next++) {
+                try {
+                    built[static_cast<std::size_t>(i)] = std::make_shared<const dsmvc_gb::AxisPlan>(
+                        dsmvc_gb::build_axis_plan(qs[static_cast<std::size_t>(i)]));
+                } catch (const std::exception &e) {
+                    errors[static_cast<std::size_t>(i)] = e.what();
+                }
+            }
+        };
+        unsigned n = threads > 0 ? static_cast<unsigned>(threads) : std::thread::hardware_concurrency();
+        n = std::max(1U, std::min<unsigned>(n, static_cast<unsigned>(std::max(count, 1))));
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < n; ++t) pool.emplace_back(worker);
+        worker();
+        for (auto &t : pool) t.join();
+        for (int32_t i = 0; i < count; ++i)
+            if (!errors[static_cast<std::size_t>(i)].empty())
+                throw std::invalid_argument("plan " + std::to_string(i) + ": " + errors[static_cast<std::size_t>(i)]);
+        for (int32_t i = 0; i < count; ++i)
+            out[i] = new dsmvc_gb_plan{std::move(built[static_cast<std::size_t>(i)]), qs[static_cast<std::size_t>(i)]};
+    });
+}
 
 int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out) {
     return guarded([&] {
@@ -427,5 +466,74 @@ int dsmvc_gb_profile_read(dsmvc_gb_executor *executor, dsmvc_gb_kernel_time *out
         }
     });
 }
+
+struct dsmvc_gb_sweep {
+    std::vector<std::shared_ptr<const dsmvc_gb::AxisPlan>> keep;
+    std::unique_ptr<dsmvc_gb::Sweep> sweep;
+};
+
+int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor, const dsmvc_gb_plan *const *horizontal,
+                          const dsmvc_gb_plan *const *vertical, int32_t count, const float *frame,
+                          int64_t frame_stride, const dsmvc_gb_sweep_options *options, dsmvc_gb_sweep **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        if (count <= 0 || !horizontal || !vertical) throw std::invalid_argument("invalid candidate list");
+        auto s = std::make_unique<dsmvc_gb_sweep>();
+        std::vector<std::pair<const dsmvc_gb::AxisPlan *, const dsmvc_gb::AxisPlan *>> list;
+        for (int32_t i = 0; i < count; ++i) {
+            if (!horizontal[i] || !vertical[i]) throw std::invalid_argument("candidate plan is null");
+            s->keep.push_back(horizontal[i]->plan);
+            s->keep.push_back(vertical[i]->plan);
+            list.emplace_back(horizontal[i]->plan.get(), vertical[i]->plan.get());
+        }
+        dsmvc_gb::SweepOptions o;
+        if (options) {
+            if (options->memory_budget < 0) throw std::invalid_argument("negative memory budget");
+            o.memory_budget = static_cast<std::size_t>(options->memory_budget);
+            o.autotune = options->autotune != 0;
+            o.graph = options->graph != 0;
+        }
+        s->sweep = std::make_unique<dsmvc_gb::Sweep>(exec_of(executor), list, frame, frame_stride, o);
+        *out = s.release();
+    });
+}
+
+int dsmvc_gb_sweep_run(dsmvc_gb_sweep *sweep, void *stream) {
+    return guarded([&] {
+        if (!sweep) throw std::invalid_argument("sweep is null");
+        sweep->sweep->run(stream);
+    });
+}
+
+int dsmvc_gb_sweep_run_plain(dsmvc_gb_sweep *sweep, void *stream) {
+    return guarded([&] {
+        if (!sweep) throw std::invalid_argument("sweep is null");
+        sweep->sweep->run_plain(stream);
+    });
+}
+
+int dsmvc_gb_sweep_scores(dsmvc_gb_sweep *sweep, float *scores, void *stream) {
+    return guarded([&] {
+        if (!sweep || !scores) throw std::invalid_argument("sweep or score buffer is null");
+        sweep->sweep->read_scores(scores, stream);
+    });
+}
+
+int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *out) {
+    return guarded([&] {
+        if (!sweep || !out) throw std::invalid_argument("sweep or output is null");
+        const auto i = sweep->sweep->info();
+        out->candidates = i.candidates;
+        out->waves = i.waves;
+        out->device_bytes = static_cast<int64_t>(i.device_bytes);
+        out->kernel_launches = static_cast<int64_t>(i.kernel_launches);
+        out->tune_milliseconds = i.tune_milliseconds;
+        out->segment_rows = i.segment_rows;
+        out->tuned_groups = static_cast<int32_t>(i.tuning.size());
+    });
+}
+
+void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep) { delete sweep; }
 
 } // extern "C"

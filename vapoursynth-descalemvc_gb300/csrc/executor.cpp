@@ -328,7 +328,12 @@ struct Executor::Impl {
         int count, blocks;
         std::uint64_t bytes;
         int record_floats;
+        int threads;
     };
+    // CTA size per launch group, keyed by (pass, kind, hb, in, out, variant);
+    // groups not listed take the default size of their kernel.
+    using GroupTuple = std::tuple<int, int, int, int, int, int>;
+    using Tuning = std::map<GroupTuple, int>;
     struct Compiled {
         std::vector<std::unique_ptr<DevicePlan>> temporaries;
         std::vector<char> table;
@@ -337,7 +342,7 @@ struct Executor::Impl {
         std::size_t tasks = 0;
     };
     void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                 const std::function<char *(std::size_t)> &scratch);
+                 const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr);
     void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
     void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks);
     void finish(Workspace &ws);
@@ -379,7 +384,7 @@ std::string kernel_name(const GroupKey &k) {
 } // namespace
 
 void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                             const std::function<char *(std::size_t)> &scratch) {
+                             const std::function<char *(std::size_t)> &scratch, const Tuning *tuning) {
     auto &temporaries = out.temporaries;
     // Per task: which kernels run each pass, and the scratch they need.
     struct Route {
@@ -583,7 +588,12 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     launches.clear();
     for (auto &[key, items] : groups) {
         const bool is_stream = key.kind >= 2;
-        const int per_block = is_stream ? stream_block : kSeqThreads;
+        int per_block = key.kind == 2 ? stream_block : key.kind == 3 ? kTStreamThreads : kSeqThreads;
+        if (tuning && key.kind != 2) {
+            const GroupTuple g{key.pass, key.kind, key.hb, static_cast<int>(key.in), static_cast<int>(key.out),
+                               key.variant};
+            if (auto it = tuning->find(g); it != tuning->end()) per_block = it->second;
+        }
         const std::size_t rec = is_stream ? sizeof(dev::StreamJob) : sizeof(dev::AxisJob);
         int blocks = 0, count = 0, record_floats = 0;
         std::uint64_t bytes_moved = 0;
@@ -604,7 +614,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         }
         if (count)
             launches.push_back({key.pass, key.kind, key.hb, key.in, key.out, key.variant, offset, count, blocks,
-                                bytes_moved, record_floats});
+                                bytes_moved, record_floats, per_block});
     }
     out.tasks = tasks.size();
 }
@@ -613,7 +623,9 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
                             std::uint32_t *status) {
     for (const auto &l : c.launches) {
         Record *rec = nullptr;
-        if (profiling) {
+        cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(stream, &capturing);
+        if (profiling && capturing == cudaStreamCaptureStatusNone) {
             std::scoped_lock lock(mutex);
             records.emplace_back();
             rec = &records.back();
@@ -627,7 +639,7 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         int rc = 0;
         if (l.kind == 3) {
             rc = launch_tstream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
-                                l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats,
+                                l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats,
                                 stream);
         } else if (l.kind == 2) {
             rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
@@ -635,10 +647,10 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
                                stream);
         } else if (l.kind == 1) {
             rc = launch_axis_f64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
-                                 kSeqThreads, l.hb, l.in, l.out, status, stream);
+                                 l.threads, l.hb, l.in, l.out, status, stream);
         } else {
             rc = launch_axis_f32(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks,
-                                 kSeqThreads, l.hb, l.in, l.out, stream);
+                                 l.threads, l.hb, l.in, l.out, stream);
         }
         cuda_check(rc, "launching axis kernel");
         if (rec) cuda_check(cudaEventRecord(rec->stop, stream), "recording event");
@@ -896,7 +908,7 @@ void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool
 struct PreparedBatch::Impl {
     Executor::Impl *owner = nullptr;
     Executor::Impl::Compiled compiled;
-    DeviceBuffer scratch;
+    DeviceBuffer scratch;                 // unused with caller-owned scratch
     DeviceBuffer table;
     std::uint32_t *status = nullptr;       // device
     std::uint32_t *status_host = nullptr;  // pinned
@@ -922,6 +934,29 @@ void PreparedBatch::launch(void *stream) {
                          impl_->status);
 }
 
+void PreparedBatch::launch_group(std::size_t index, void *stream) {
+    DeviceGuard guard(impl_->owner->device);
+    if (index >= impl_->compiled.launches.size()) throw std::out_of_range("launch group index");
+    Executor::Impl::Compiled one;
+    one.launches.push_back(impl_->compiled.launches[index]);
+    impl_->owner->launch(one, impl_->table.data(), static_cast<cudaStream_t>(stream), impl_->status);
+}
+
+std::vector<BatchGroup> PreparedBatch::groups() const {
+    std::vector<BatchGroup> out;
+    for (const auto &l : impl_->compiled.launches) {
+        BatchGroup g;
+        g.key = {l.pass, l.kind, l.hb, static_cast<int>(l.in), static_cast<int>(l.out), l.variant};
+        g.kind = l.kind;
+        g.threads = l.threads;
+        g.blocks = l.blocks;
+        g.jobs = l.count;
+        g.name = kernel_name({l.pass, l.kind, l.hb, l.in, l.out, l.variant});
+        out.push_back(g);
+    }
+    return out;
+}
+
 void PreparedBatch::check_status(void *stream) {
     DeviceGuard guard(impl_->owner->device);
     auto s = static_cast<cudaStream_t>(stream);
@@ -941,15 +976,48 @@ std::size_t PreparedBatch::kernel_launches() const { return impl_->compiled.laun
 std::size_t PreparedBatch::scratch_bytes() const { return impl_->compiled.scratch_bytes; }
 std::size_t PreparedBatch::table_bytes() const { return impl_->compiled.table.size(); }
 
-std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks) {
+std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
+    // Per task: the intermediate plane (destinations of the first pass x
+    // sources of the second, rows padded to 4) plus a forward plane of the
+    // output's size, in the route's sample width.
+    std::size_t bytes = kAlign;
+    for (const auto &t : tasks) {
+        const AxisPlan *h = t.horizontal, *v = t.vertical;
+        if (!h && !v) continue;
+        const bool f64 = (h && h->requires_float64()) || (v && v->requires_float64());
+        const std::size_t es = f64 ? 8 : 4;
+        const std::size_t hd = h ? static_cast<std::size_t>(h->destination_size) : static_cast<std::size_t>(t.vectors);
+        const std::size_t vs = v ? (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4 : static_cast<std::size_t>(t.vectors);
+        const std::size_t vd = v ? static_cast<std::size_t>(v->destination_size) : static_cast<std::size_t>(t.vectors);
+        bytes += align_up(hd * vs * es) + align_up(hd * vd * es);
+    }
+    return bytes;
+}
+
+std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks,
+                                                       const BatchTuning *tuning, void *scratch,
+                                                       std::size_t scratch_capacity) {
     DeviceGuard guard(impl_->device);
     validate_tasks(tasks);
+    for (const auto &[key, threads] : tuning ? *tuning : BatchTuning{}) {
+        const int kind = key[1];
+        const int most = kind == 3 ? 256 : 128;
+        if (kind == 2 || threads < 32 || threads > most || threads % 32)
+            throw std::invalid_argument("invalid CTA size in batch tuning");
+    }
+    Executor::Impl::Tuning t;
+    if (tuning)
+        for (const auto &[k, v] : *tuning) t[{k[0], k[1], k[2], k[3], k[4], k[5]}] = v;
     auto b = std::make_unique<PreparedBatch::Impl>();
     b->owner = impl_.get();
     impl_->compile(tasks, b->compiled, [&](std::size_t bytes) {
+        if (scratch) {
+            if (bytes > scratch_capacity) throw std::length_error("batch scratch exceeds the caller's buffer");
+            return static_cast<char *>(scratch);
+        }
         b->scratch.reserve(bytes);
         return b->scratch.data();
-    });
+    }, &t);
     const auto &table = b->compiled.table;
     b->table.reserve(std::max<std::size_t>(table.size(), 1));
     if (!table.empty())

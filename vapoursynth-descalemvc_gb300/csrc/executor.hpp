@@ -14,8 +14,10 @@
 #include "kernels.cuh"
 #include "planner.hpp"
 
+#include <array>
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -65,6 +67,25 @@ struct ExecutorStats {
 
 class Executor;
 
+// One launch group of a batch: every job of the group runs in one kernel
+// launch.  `key` identifies the kernel variant (pass, kind, half-bandwidth,
+// input and output sample kinds, window variant); `kind` 0/1 are the
+// sequential Float32/Float64 kernels, 2 the streaming 1D kernels, 3 the
+// transposing streaming 2D kernels.
+struct BatchGroup {
+    std::array<int, 6> key{};
+    int kind = 0;
+    int threads = 0;      // CTA size
+    int blocks = 0;
+    int jobs = 0;
+    std::string name;
+};
+
+// CTA sizes chosen per launch-group key (an autotuner's output); groups not
+// listed keep their kernel's default.  Kinds 0/1 accept 32..128, kind 3
+// 32..256 (multiples of 32); kind 2 has a fixed size.
+using BatchTuning = std::map<std::array<int, 6>, int>;
+
 // A batch routed and packed once, with its own job table, scratch and status
 // word on the device, then launched any number of times.  launch() issues
 // kernels only (no copies, no allocation, no host synchronisation), so it
@@ -79,6 +100,9 @@ public:
     PreparedBatch &operator=(const PreparedBatch &) = delete;
 
     void launch(void *stream);
+    // Launches group `index` alone (for timing one group).
+    void launch_group(std::size_t index, void *stream);
+    [[nodiscard]] std::vector<BatchGroup> groups() const;
     // Waits for `stream` and raises on a Float64 non-finite status (clears it).
     void check_status(void *stream);
     [[nodiscard]] std::size_t kernel_launches() const;
@@ -117,8 +141,16 @@ public:
     // Float64 non-finite status; otherwise check_status() does that later.
     void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize);
     void check_status(void *stream);
-    // Validates, routes and uploads `tasks` once (see PreparedBatch).
-    [[nodiscard]] std::unique_ptr<PreparedBatch> prepare_batch(const std::vector<PlaneTask> &tasks);
+    // Validates, routes and uploads `tasks` once (see PreparedBatch).  With
+    // `scratch` the batch's intermediate planes live in that caller-owned
+    // device buffer of `scratch_capacity` bytes (batches launched one after
+    // another may share it); otherwise the batch allocates its own.
+    [[nodiscard]] std::unique_ptr<PreparedBatch> prepare_batch(const std::vector<PlaneTask> &tasks,
+                                                             const BatchTuning *tuning = nullptr,
+                                                             void *scratch = nullptr,
+                                                             std::size_t scratch_capacity = 0);
+    // Upper bound of the scratch bytes prepare_batch needs for `tasks`.
+    [[nodiscard]] static std::size_t batch_scratch_bound(const std::vector<PlaneTask> &tasks);
 
     [[nodiscard]] ExecutorStats stats() const;
 

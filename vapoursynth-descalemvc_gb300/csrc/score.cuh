@@ -1,0 +1,58 @@
+// Candidate scoring of a descale sweep (score.cu): re-upscale each descaled
+// plane with its plans' forward operators and reduce the mean absolute error
+// against the source frame.
+//
+// The forward operator of an axis is A (source x destination), the matrix
+// whose transpose the plan stores as a CSR by destination.  Upscaling a
+// descaled plane Y (rows x cols) back to the source size is A_v * Y * A_h^T:
+// a row pass Z = Y * A_h^T (rows x width), then a column pass A_v * Z fused
+// with |. - frame| and a per-CTA partial sum.  Partial sums are reduced in a
+// fixed order, so a score does not depend on launch shapes or on the other
+// candidates of the sweep.
+#pragma once
+
+#include <cstdint>
+
+namespace dsmvc_gb::dev {
+
+// A as a CSR by source sample: entries (destination index, weight) in
+// ascending destination order.
+struct ForwardCsr {
+    const std::uint32_t *offsets;   // source_size + 1
+    const std::int32_t *indices;
+    const float *weights;
+};
+
+struct ScoreJob {
+    const float *descaled;          // rows x cols
+    std::int64_t descaled_stride;
+    std::int32_t rows, cols;
+    float *upscaled_rows;           // rows x width scratch
+    std::int64_t upscaled_stride;
+    const float *frame;             // height x width source plane
+    std::int64_t frame_stride;
+    std::int32_t width, height;
+    ForwardCsr h, v;                // forward operators of the two axes
+    float *partials;                // column tiles x row segments
+    std::int32_t first_block_rows;  // row-pass blocks before this job
+    std::int32_t first_block_cols;  // column-pass blocks before this job
+    std::int32_t segment_rows;      // source rows per column-pass block
+    std::int32_t column_tiles;      // ceil(width / threads of the column pass)
+};
+
+} // namespace dsmvc_gb::dev
+
+namespace dsmvc_gb {
+
+constexpr int kScoreThreads = 256;
+
+// Row pass: one block per descaled row; `max_cols` bounds every job's cols
+// (the row is staged in shared memory).
+int launch_upscale_rows(const dev::ScoreJob *jobs, int job_count, int total_blocks, int max_cols,
+                        void *stream);
+// Column pass + absolute error: one block per (column tile, row segment).
+int launch_upscale_columns_l1(const dev::ScoreJob *jobs, int job_count, int total_blocks, void *stream);
+// scores[i] = sum of job i's partials / (width * height), one block per job.
+int launch_score_finalize(const dev::ScoreJob *jobs, int job_count, float *scores, void *stream);
+
+} // namespace dsmvc_gb

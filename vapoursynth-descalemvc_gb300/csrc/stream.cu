@@ -33,18 +33,18 @@ int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, i
 
 namespace dsmvc_gb {
 
-int launch_tstream_hb1(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
-int launch_tstream_hb3(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
-int launch_tstream_hb5(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
-int launch_tstream_hb7(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_hb1(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_hb3(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_hb5(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_hb7(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
 
-int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
+int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
                    int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
     switch (half_bandwidth) {
-    case 1: return launch_tstream_hb1(jobs, job_count, total_blocks, window, in, out, record_floats, stream);
-    case 3: return launch_tstream_hb3(jobs, job_count, total_blocks, window, in, out, record_floats, stream);
-    case 5: return launch_tstream_hb5(jobs, job_count, total_blocks, window, in, out, record_floats, stream);
-    case 7: return launch_tstream_hb7(jobs, job_count, total_blocks, window, in, out, record_floats, stream);
+    case 1: return launch_tstream_hb1(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 3: return launch_tstream_hb3(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 5: return launch_tstream_hb5(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 7: return launch_tstream_hb7(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
     default: return static_cast<int>(cudaErrorInvalidValue);
     }
 }

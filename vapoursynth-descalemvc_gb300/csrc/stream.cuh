@@ -51,9 +51,12 @@ constexpr int kStreamRing = 32;      // source samples held per thread
 // (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
 // Transposing 2D passes (tstream_impl.cuh): vectors with adjacent samples
 // in, destination-major output with the vectors adjacent.  Every job of one
-// launch has the same window when window == 8 (unrolled gather).
-int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
-                   int window, dev::Sample in, dev::Sample out, int record_floats, void *stream);
+// launch has the same window when window == 8 (unrolled gather).  `threads`
+// per CTA: 32..256, a multiple of 32 (one warp per 32 vectors).
+constexpr int kTStreamThreads = 128;   // default CTA size
+int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
+                   int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
+                   void *stream);
 
 // `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,

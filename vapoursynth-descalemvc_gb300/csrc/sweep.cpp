@@ -1,0 +1,437 @@
+// Batched candidate sweep (sweep.hpp).
+#include "sweep.hpp"
+
+#include "score.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+
+namespace dsmvc_gb {
+namespace {
+
+void check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA ") + what + ": " + cudaGetErrorString(e));
+}
+void check(int e, const char *what) { check(static_cast<cudaError_t>(e), what); }
+
+constexpr std::size_t kAlign = 256;
+std::size_t align_up(std::size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+struct Buffer {
+    void *ptr = nullptr;
+    std::size_t bytes = 0;
+    Buffer() = default;
+    Buffer(const Buffer &) = delete;
+    Buffer &operator=(const Buffer &) = delete;
+    ~Buffer() { if (ptr) cudaFree(ptr); }
+    void allocate(std::size_t n) {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        check(cudaMalloc(&ptr, std::max<std::size_t>(n, kAlign)), "allocating sweep buffer");
+        bytes = n;
+    }
+    [[nodiscard]] char *data() const { return static_cast<char *>(ptr); }
+};
+
+// A (source x destination) as a CSR by source sample, from the plan's CSR
+// of A^T: entries keep ascending destination order.
+struct HostForward {
+    std::vector<std::uint32_t> offsets;
+    std::vector<std::int32_t> indices;
+    std::vector<float> weights;
+};
+
+HostForward forward_csr(const AxisPlan &p) {
+    HostForward f;
+    const auto n = static_cast<std::size_t>(p.source_size);
+    f.offsets.assign(n + 1, 0);
+    for (std::size_t j = 0; j < static_cast<std::size_t>(p.destination_size); ++j)
+        for (std::uint32_t e = p.transpose_offsets[j]; e < p.transpose_offsets[j + 1]; ++e)
+            ++f.offsets[static_cast<std::size_t>(p.transpose_indices[e]) + 1];
+    for (std::size_t s = 0; s < n; ++s) f.offsets[s + 1] += f.offsets[s];
+    f.indices.resize(f.offsets[n]);
+    f.weights.resize(f.offsets[n]);
+    std::vector<std::uint32_t> fill(f.offsets.begin(), f.offsets.end() - 1);
+    for (std::size_t j = 0; j < static_cast<std::size_t>(p.destination_size); ++j) {
+        for (std::uint32_t e = p.transpose_offsets[j]; e < p.transpose_offsets[j + 1]; ++e) {
+            const auto s = static_cast<std::size_t>(p.transpose_indices[e]);
+            f.indices[fill[s]] = static_cast<std::int32_t>(j);
+            f.weights[fill[s]] = p.transpose_weights[e];
+            ++fill[s];
+        }
+    }
+    return f;
+}
+
+} // namespace
+
+constexpr int kMinSegment = 16;
+constexpr int kSegments[] = {16, 32, 64, 128, 256};
+
+struct Sweep::Impl {
+    Executor *executor = nullptr;
+    std::vector<std::pair<const AxisPlan *, const AxisPlan *>> candidates;
+    const float *frame = nullptr;
+    std::ptrdiff_t frame_stride = 0;
+    int width = 0, height = 0;
+    SweepOptions options;
+    cudaStream_t stream = nullptr;          // tuning and capture
+
+    struct Wave {
+        int first = 0, count = 0;
+        std::vector<PlaneTask> tasks;
+        std::unique_ptr<PreparedBatch> batch;
+        int row_blocks = 0, column_blocks = 0, max_cols = 0;
+    };
+    std::vector<Wave> waves;
+    std::vector<std::size_t> y_offset, z_offset, partial_offset;   // within a wave's buffers
+    Buffer forward_mem, y_mem, z_mem, partial_mem, scratch_mem, job_mem, plain_job_mem, score_mem;
+    std::size_t scratch_capacity = 0;
+    std::map<const AxisPlan *, dev::ForwardCsr> forward;
+    int segment_rows = 64;
+    BatchTuning tuning;
+    double tune_ms = 0.0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    ~Impl() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void upload_forward() {
+        std::map<const AxisPlan *, HostForward> host;
+        std::size_t bytes = 0;
+        for (const auto &[h, v] : candidates) {
+            for (const AxisPlan *p : {h, v}) {
+                if (host.count(p)) continue;
+                auto f = forward_csr(*p);
+                bytes += align_up(f.offsets.size() * 4) + align_up(f.indices.size() * 4)
+                    + align_up(f.weights.size() * 4);
+                host.emplace(p, std::move(f));
+            }
+        }
+        std::vector<char> blob(std::max<std::size_t>(bytes, kAlign), 0);
+        forward_mem.allocate(blob.size());
+        std::size_t at = 0;
+        for (auto &[p, f] : host) {
+            dev::ForwardCsr c{};
+            auto put = [&](const void *src, std::size_t n) {
+                std::memcpy(blob.data() + at, src, n);
+                const char *d = forward_mem.data() + at;
+                at += align_up(n);
+                return d;
+            };
+            c.offsets = reinterpret_cast<const std::uint32_t *>(put(f.offsets.data(), f.offsets.size() * 4));
+            c.indices = reinterpret_cast<const std::int32_t *>(put(f.indices.data(), f.indices.size() * 4));
+            c.weights = reinterpret_cast<const float *>(put(f.weights.data(), f.weights.size() * 4));
+            forward[p] = c;
+        }
+        check(cudaMemcpy(forward_mem.data(), blob.data(), blob.size(), cudaMemcpyHostToDevice),
+              "uploading forward operators");
+    }
+
+    [[nodiscard]] int column_tiles() const { return (width + kScoreThreads - 1) / kScoreThreads; }
+    [[nodiscard]] int segments(int seg) const { return (height + seg - 1) / seg; }
+
+    // Splits the candidates into waves within the memory budget and lays
+    // out each wave's descaled planes, row-pass planes and partial sums.
+    void plan_waves() {
+        const std::size_t budget = options.memory_budget ? options.memory_budget : (32ULL << 30);
+        // Room for the partial sums of the finest row segment the tuner tries.
+        const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kMinSegment) * 4);
+        std::size_t y_bytes = 0, z_bytes = 0, p_bytes = 0, s_bytes = 0;
+        std::size_t y_max = 0, z_max = 0, p_max = 0, s_max = 0;
+        y_offset.resize(candidates.size());
+        z_offset.resize(candidates.size());
+        partial_offset.resize(candidates.size());
+        Wave cur;
+        for (std::size_t i = 0; i < candidates.size(); ++i) {
+            const auto &[h, v] = candidates[i];
+            const std::size_t y = align_up(static_cast<std::size_t>(h->destination_size) * v->destination_size * 4);
+            const std::size_t z = align_up(static_cast<std::size_t>(v->destination_size) * width * 4);
+            PlaneTask probe;
+            probe.horizontal = h;
+            probe.vertical = v;
+            const std::size_t s = Executor::batch_scratch_bound({probe});
+            if (cur.count > 0 && y_bytes + z_bytes + p_bytes + s_bytes + y + z + partials + s > budget) {
+                waves.push_back(std::move(cur));
+                cur = Wave{};
+                y_bytes = z_bytes = p_bytes = s_bytes = 0;
+            }
+            if (cur.count == 0) cur.first = static_cast<int>(i);
+            ++cur.count;
+            y_offset[i] = y_bytes;
+            z_offset[i] = z_bytes;
+            partial_offset[i] = p_bytes;
+            y_bytes += y;
+            z_bytes += z;
+            p_bytes += partials;
+            s_bytes += s;
+            y_max = std::max(y_max, y_bytes);
+            z_max = std::max(z_max, z_bytes);
+            p_max = std::max(p_max, p_bytes);
+            s_max = std::max(s_max, s_bytes);
+        }
+        if (cur.count > 0) waves.push_back(std::move(cur));
+        y_mem.allocate(y_max);
+        z_mem.allocate(z_max);
+        partial_mem.allocate(p_max);
+        scratch_mem.allocate(s_max);
+        scratch_capacity = s_max;
+        for (auto &w : waves) {
+            for (int k = 0; k < w.count; ++k) {
+                const std::size_t i = static_cast<std::size_t>(w.first + k);
+                PlaneTask t;
+                t.horizontal = candidates[i].first;
+                t.vertical = candidates[i].second;
+                t.input = frame;
+                t.input_stride = frame_stride;
+                t.output = y_mem.data() + y_offset[i];
+                t.output_stride = candidates[i].first->destination_size;
+                t.sample = dev::Sample::f32;
+                w.tasks.push_back(t);
+            }
+        }
+    }
+
+    // Score jobs of every candidate with `seg` source rows per column-pass
+    // block; block numbering restarts at each wave (`plain`: at each job).
+    std::vector<dev::ScoreJob> score_jobs(int seg, bool plain) {
+        std::vector<dev::ScoreJob> jobs(candidates.size());
+        for (auto &w : waves) {
+            int rows = 0, cols = 0;
+            w.max_cols = 0;
+            for (int k = 0; k < w.count; ++k) {
+                const std::size_t i = static_cast<std::size_t>(w.first + k);
+                const AxisPlan *h = candidates[i].first, *v = candidates[i].second;
+                auto &j = jobs[i];
+                j.descaled = reinterpret_cast<const float *>(y_mem.data() + y_offset[i]);
+                j.descaled_stride = h->destination_size;
+                j.rows = v->destination_size;
+                j.cols = h->destination_size;
+                j.upscaled_rows = reinterpret_cast<float *>(z_mem.data() + z_offset[i]);
+                j.upscaled_stride = width;
+                j.frame = frame;
+                j.frame_stride = frame_stride;
+                j.width = width;
+                j.height = height;
+                j.h = forward.at(h);
+                j.v = forward.at(v);
+                j.partials = reinterpret_cast<float *>(partial_mem.data() + partial_offset[i]);
+                j.segment_rows = seg;
+                j.column_tiles = column_tiles();
+                j.first_block_rows = plain ? 0 : rows;
+                j.first_block_cols = plain ? 0 : cols;
+                rows += j.rows;
+                cols += j.column_tiles * segments(seg);
+                w.max_cols = std::max(w.max_cols, j.cols);
+            }
+            w.row_blocks = rows;
+            w.column_blocks = cols;
+        }
+        return jobs;
+    }
+
+    void upload_jobs(Buffer &mem, const std::vector<dev::ScoreJob> &jobs) {
+        const std::size_t n = jobs.size() * sizeof(dev::ScoreJob);
+        if (mem.bytes < n) mem.allocate(n);
+        check(cudaMemcpy(mem.data(), jobs.data(), n, cudaMemcpyHostToDevice), "uploading score jobs");
+    }
+
+    [[nodiscard]] const dev::ScoreJob *wave_jobs(const Wave &w) const {
+        return reinterpret_cast<const dev::ScoreJob *>(job_mem.data()) + w.first;
+    }
+
+    void enqueue_scoring(const Wave &w, cudaStream_t s) {
+        check(launch_upscale_rows(wave_jobs(w), w.count, w.row_blocks, w.max_cols, s), "launching upscale rows");
+        check(launch_upscale_columns_l1(wave_jobs(w), w.count, w.column_blocks, s), "launching upscale columns");
+    }
+
+    void enqueue_all(cudaStream_t s) {
+        for (auto &w : waves) {
+            w.batch->launch(s);
+            enqueue_scoring(w, s);
+        }
+        check(launch_score_finalize(reinterpret_cast<const dev::ScoreJob *>(job_mem.data()),
+                                    static_cast<int>(candidates.size()),
+                                    reinterpret_cast<float *>(score_mem.data()), s),
+              "launching score finalize");
+    }
+
+    template <class F> float time_ms(F &&f, int reps) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        check(cudaEventCreate(&a), "creating event");
+        check(cudaEventCreate(&b), "creating event");
+        f();   // warm
+        check(cudaEventRecord(a, stream), "recording event");
+        for (int r = 0; r < reps; ++r) f();
+        check(cudaEventRecord(b, stream), "recording event");
+        check(cudaEventSynchronize(b), "waiting for event");
+        float ms = 0.0F;
+        check(cudaEventElapsedTime(&ms, a, b), "reading event");
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return ms / static_cast<float>(reps);
+    }
+
+    // Times every launch group of the first wave at each candidate CTA size
+    // and the scoring column pass at each row segment; keeps the fastest.
+    void autotune() {
+        const auto t0 = std::chrono::steady_clock::now();
+        Wave &w = waves.front();
+        std::map<std::array<int, 6>, std::pair<float, int>> best;
+        const auto keys = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity)->groups();
+        for (const int threads : {32, 64, 128, 256}) {
+            BatchTuning all;
+            for (const auto &g : keys) {
+                const int most = g.kind == 3 ? 256 : 128;
+                if (g.kind != 2 && threads <= most) all[g.key] = threads;
+            }
+            if (all.empty()) continue;
+            auto batch = executor->prepare_batch(w.tasks, &all, scratch_mem.data(), scratch_capacity);
+            const auto groups = batch->groups();
+            for (std::size_t gi = 0; gi < groups.size(); ++gi) {
+                if (!all.count(groups[gi].key)) continue;
+                const float ms = time_ms([&] { batch->launch_group(gi, stream); }, 3);
+                auto it = best.find(groups[gi].key);
+                if (it == best.end() || ms < it->second.first) best[groups[gi].key] = {ms, threads};
+            }
+            check(cudaStreamSynchronize(stream), "synchronizing");
+        }
+        tuning.clear();
+        for (const auto &[k, v] : best) tuning[k] = v.second;
+        float best_ms = 0.0F;
+        for (const int seg : kSegments) {
+            upload_jobs(job_mem, score_jobs(seg, false));
+            const float ms = time_ms([&] {
+                check(launch_upscale_columns_l1(wave_jobs(w), w.count, w.column_blocks, stream), "launching");
+            }, 3);
+            if (seg == kSegments[0] || ms < best_ms) {
+                best_ms = ms;
+                segment_rows = seg;
+            }
+        }
+        tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    void build() {
+        check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "creating stream");
+        upload_forward();
+        plan_waves();
+        score_mem.allocate(candidates.size() * sizeof(float));
+        if (options.autotune) autotune();
+        for (auto &w : waves)
+            w.batch = executor->prepare_batch(w.tasks, &tuning, scratch_mem.data(), scratch_capacity);
+        upload_jobs(plain_job_mem, score_jobs(segment_rows, true));
+        upload_jobs(job_mem, score_jobs(segment_rows, false));
+        if (options.graph) {
+            check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "beginning capture");
+            try {
+                enqueue_all(stream);
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            check(cudaStreamEndCapture(stream, &graph), "ending capture");
+            check(cudaGraphInstantiate(&graph_exec, graph, 0), "instantiating graph");
+        }
+        check(cudaStreamSynchronize(stream), "synchronizing");
+    }
+};
+
+Sweep::Sweep(Executor &executor, const std::vector<std::pair<const AxisPlan *, const AxisPlan *>> &candidates,
+             const float *frame, std::ptrdiff_t frame_stride, const SweepOptions &options)
+    : impl_(std::make_unique<Impl>()) {
+    if (candidates.empty() || !frame) throw std::invalid_argument("a sweep needs candidates and a frame");
+    const AxisPlan *h0 = candidates.front().first, *v0 = candidates.front().second;
+    if (!h0 || !v0) throw std::invalid_argument("sweep candidate without a plan");
+    for (const auto &[h, v] : candidates) {
+        if (!h || !v || !h->valid() || !v->valid() || h->source_size != h0->source_size
+            || v->source_size != v0->source_size)
+            throw std::invalid_argument("sweep candidates must share the frame's source size");
+    }
+    if (frame_stride < h0->source_size) throw std::invalid_argument("invalid frame stride");
+    auto &m = *impl_;
+    m.executor = &executor;
+    m.candidates = candidates;
+    m.frame = frame;
+    m.frame_stride = frame_stride;
+    m.width = h0->source_size;
+    m.height = v0->source_size;
+    m.options = options;
+    int previous = -1;
+    cudaGetDevice(&previous);
+    if (previous != executor.device()) check(cudaSetDevice(executor.device()), "selecting device");
+    try {
+        m.build();
+    } catch (...) {
+        if (previous >= 0 && previous != executor.device()) cudaSetDevice(previous);
+        throw;
+    }
+    if (previous >= 0 && previous != executor.device()) cudaSetDevice(previous);
+}
+
+Sweep::~Sweep() = default;
+
+void Sweep::run(void *stream) {
+    auto s = static_cast<cudaStream_t>(stream);
+    if (impl_->graph_exec) check(cudaGraphLaunch(impl_->graph_exec, s), "launching sweep graph");
+    else impl_->enqueue_all(s);
+}
+
+void Sweep::run_plain(void *stream) {
+    auto &m = *impl_;
+    auto s = static_cast<cudaStream_t>(stream);
+    const auto *jobs = reinterpret_cast<const dev::ScoreJob *>(m.plain_job_mem.data());
+    for (const auto &w : m.waves) {
+        for (int k = 0; k < w.count; ++k) {
+            const std::size_t i = static_cast<std::size_t>(w.first + k);
+            const AxisPlan *h = m.candidates[i].first, *v = m.candidates[i].second;
+            m.executor->run_batch({w.tasks[static_cast<std::size_t>(k)]}, stream, false);
+            const int col_blocks = m.column_tiles() * m.segments(m.segment_rows);
+            check(launch_upscale_rows(jobs + i, 1, v->destination_size, h->destination_size, s), "launching");
+            check(launch_upscale_columns_l1(jobs + i, 1, col_blocks, s), "launching");
+            check(launch_score_finalize(jobs + i, 1, reinterpret_cast<float *>(m.score_mem.data()) + i, s),
+                  "launching");
+            check(cudaStreamSynchronize(s), "synchronizing");
+        }
+    }
+}
+
+void Sweep::read_scores(float *host, void *stream) {
+    auto s = static_cast<cudaStream_t>(stream);
+    check(cudaMemcpyAsync(host, impl_->score_mem.data(), impl_->candidates.size() * sizeof(float),
+                          cudaMemcpyDeviceToHost, s), "reading scores");
+    check(cudaStreamSynchronize(s), "synchronizing");
+}
+
+const float *Sweep::device_scores() const { return reinterpret_cast<const float *>(impl_->score_mem.data()); }
+
+SweepInfo Sweep::info() const {
+    const auto &m = *impl_;
+    SweepInfo i;
+    i.candidates = static_cast<int>(m.candidates.size());
+    i.waves = static_cast<int>(m.waves.size());
+    i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.z_mem.bytes + m.partial_mem.bytes
+        + m.scratch_mem.bytes + m.job_mem.bytes + m.plain_job_mem.bytes + m.score_mem.bytes;
+    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 2;
+    i.kernel_launches += 1;
+    i.tune_milliseconds = m.tune_ms;
+    i.segment_rows = m.segment_rows;
+    i.tuning = m.tuning;
+    return i;
+}
+
+} // namespace dsmvc_gb

@@ -4,9 +4,9 @@
 
 namespace dsmvc_gb {
 
-int launch_tstream_hb7(const dev::StreamJob *jobs, int count, int blocks, int window,
+int launch_tstream_hb7(const dev::StreamJob *jobs, int count, int blocks, int threads, int window,
                         dev::Sample in, dev::Sample out, int record_floats, void *stream) {
-    return tlaunch_hb<7>(jobs, count, blocks, window, in, out, record_floats,
+    return tlaunch_hb<7>(jobs, count, blocks, threads, window, in, out, record_floats,
                           static_cast<cudaStream_t>(stream));
 }
 

@@ -15,7 +15,7 @@
 //    row are both free of bank conflicts.  The next block is in flight while
 //    the current one is consumed.
 //  * Stores: destination j of the 32 vectors is one coalesced store.
-//  * Records: the CTA's four warps work on the same destinations, so one
+//  * Records: the CTA's warps work on the same destinations, so one
 //    chunk of 32 destination records is copied (cp.async) into shared memory
 //    for all of them, three chunks deep, behind a barrier per chunk.
 //  * Arithmetic: as in stream_impl.cuh -- exact forward substitution in the
@@ -43,8 +43,7 @@ constexpr int kTRing = kStreamRing;        // sample rows per ring
 constexpr int kTPitch = 34;                // floats between ring rows
 constexpr int kTRingFloats = 2 * kTRing * kTPitch;
 constexpr int kTChunk = kStreamChunk;
-constexpr int kTThreads = 128;
-constexpr int kTWarps = kTThreads / 32;
+constexpr int kTMaxThreads = 256;         // CTA sizes 32..256 (a multiple of 32)
 constexpr int kTBlock = 16;                // samples per warp load block
 
 __device__ __forceinline__ int find_tjob(const StreamJob *jobs, int count, int block) {
@@ -155,13 +154,14 @@ struct WarpFeeder {
     }
 };
 
-__device__ __forceinline__ void tstage(float *buf, const dev::StreamPlanView &p, int chunk, int tid) {
+__device__ __forceinline__ void tstage(float *buf, const dev::StreamPlanView &p, int chunk, int tid,
+                                       int nthreads) {
     const int fs = p.forward_stride, bs = p.backward_stride;
     const float *gf = p.forward + static_cast<std::int64_t>(chunk) * kTChunk * fs;
     const float *gb = p.backward + static_cast<std::int64_t>(chunk) * kTChunk * bs;
-    for (int i = tid * 4; i < kTChunk * fs; i += kTThreads * 4) tcp_async16(buf + i, gf + i);
+    for (int i = tid * 4; i < kTChunk * fs; i += nthreads * 4) tcp_async16(buf + i, gf + i);
     float *bb = buf + kTChunk * fs;
-    for (int i = tid * 4; i < kTChunk * bs; i += kTThreads * 4) tcp_async16(bb + i, gb + i);
+    for (int i = tid * 4; i < kTChunk * bs; i += nthreads * 4) tcp_async16(bb + i, gb + i);
 }
 
 // Forward substitution of chunk destinations [j0, j0 + LC) into y[LC + t].
@@ -289,13 +289,14 @@ __device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB]
 }
 
 template <int HB, int LC, int K, class In, class Out>
-__global__ void __launch_bounds__(kTThreads)
+__global__ void __launch_bounds__(kTMaxThreads)
 tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats) {
     static_assert(LC == kTChunk, "record chunks and register chunks coincide");
     extern __shared__ __align__(16) float smem[];
     const int jidx = find_tjob(jobs, job_count, static_cast<int>(blockIdx.x));
     const StreamJob &job = jobs[jidx];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthreads = static_cast<int>(blockDim.x);
     const dev::StreamPlanView p = job.plan;
     const int n = p.destination_size;
     const int per_buffer = kTChunk * record_floats;
@@ -304,7 +305,7 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
 
     // The warp's vectors; a warp past the last vector still takes part in
     // the CTA's record copies and barriers, on a clamped vector.
-    const int block_first = (static_cast<int>(blockIdx.x) - job.first_block) * kTThreads;
+    const int block_first = (static_cast<int>(blockIdx.x) - job.first_block) * nthreads;
     int warp_first = block_first + warp * 32;
     int warp_vectors = job.vectors - warp_first;
     if (warp_vectors <= 0) {
@@ -330,9 +331,9 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     Out *out = static_cast<Out *>(job.out) + (warp_first + (lane < warp_vectors ? lane : 0));
 
     const int chunks = (n + LC - 1) / LC;
-    tstage(bufs, p, 0, tid);
+    tstage(bufs, p, 0, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid);
+    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid, nthreads);
     tcp_commit();
 
     float y[2 * LC];
@@ -361,7 +362,7 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
         if (last) break;
         // Every warp is done with chunk c-1's records: fetch chunk c+2.
         __syncthreads();
-        if (c + 2 < chunks) tstage(const_cast<float *>(prev), p, c + 2, tid);
+        if (c + 2 < chunks) tstage(const_cast<float *>(prev), p, c + 2, tid, nthreads);
         tcp_commit();
 #pragma unroll
         for (int t = 0; t < LC; ++t) y[t] = y[LC + t];
@@ -369,8 +370,9 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
 }
 
 template <int HB, int LC, int K, class In, class Out>
-int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int record_floats, cudaStream_t s) {
-    const int smem = (3 * kTChunk * record_floats + kTWarps * kTRingFloats) * static_cast<int>(sizeof(float));
+int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int threads, int record_floats, cudaStream_t s) {
+    if (threads < 32 || threads > kTMaxThreads || threads % 32) return static_cast<int>(cudaErrorInvalidValue);
+    const int smem = (3 * kTChunk * record_floats + threads / 32 * kTRingFloats) * static_cast<int>(sizeof(float));
     auto kernel = tstream_kernel<HB, LC, K, In, Out>;
     static int configured = 0;
     if (smem > configured) {
@@ -378,33 +380,33 @@ int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int record_float
         if (e != cudaSuccess) return static_cast<int>(e);
         configured = smem;
     }
-    kernel<<<blocks, kTThreads, smem, s>>>(jobs, count, record_floats);
+    kernel<<<blocks, threads, smem, s>>>(jobs, count, record_floats);
     return static_cast<int>(cudaGetLastError());
 }
 
 template <int HB, int LC, int K>
-int tlaunch_k(const StreamJob *jobs, int count, int blocks, dev::Sample in, dev::Sample out,
+int tlaunch_k(const StreamJob *jobs, int count, int blocks, int threads, dev::Sample in, dev::Sample out,
               int record_floats, cudaStream_t s) {
     using dev::Sample;
     if (in == Sample::f32 && out == Sample::f32)
-        return tlaunch_typed<HB, LC, K, float, float>(jobs, count, blocks, record_floats, s);
+        return tlaunch_typed<HB, LC, K, float, float>(jobs, count, blocks, threads, record_floats, s);
     if (in == Sample::u16 && out == Sample::f32)
-        return tlaunch_typed<HB, LC, K, std::uint16_t, float>(jobs, count, blocks, record_floats, s);
+        return tlaunch_typed<HB, LC, K, std::uint16_t, float>(jobs, count, blocks, threads, record_floats, s);
     if (in == Sample::u8 && out == Sample::f32)
-        return tlaunch_typed<HB, LC, K, std::uint8_t, float>(jobs, count, blocks, record_floats, s);
+        return tlaunch_typed<HB, LC, K, std::uint8_t, float>(jobs, count, blocks, threads, record_floats, s);
     if (in == Sample::f32 && out == Sample::u16)
-        return tlaunch_typed<HB, LC, K, float, std::uint16_t>(jobs, count, blocks, record_floats, s);
+        return tlaunch_typed<HB, LC, K, float, std::uint16_t>(jobs, count, blocks, threads, record_floats, s);
     if (in == Sample::f32 && out == Sample::u8)
-        return tlaunch_typed<HB, LC, K, float, std::uint8_t>(jobs, count, blocks, record_floats, s);
+        return tlaunch_typed<HB, LC, K, float, std::uint8_t>(jobs, count, blocks, threads, record_floats, s);
     return static_cast<int>(cudaErrorInvalidValue);
 }
 
 // window == 8 has an unrolled gather; other windows loop.
 template <int HB>
-int tlaunch_hb(const StreamJob *jobs, int count, int blocks, int window, dev::Sample in,
+int tlaunch_hb(const StreamJob *jobs, int count, int blocks, int threads, int window, dev::Sample in,
                dev::Sample out, int record_floats, cudaStream_t s) {
-    if (window == 8) return tlaunch_k<HB, kTChunk, 8>(jobs, count, blocks, in, out, record_floats, s);
-    return tlaunch_k<HB, kTChunk, 0>(jobs, count, blocks, in, out, record_floats, s);
+    if (window == 8) return tlaunch_k<HB, kTChunk, 8>(jobs, count, blocks, threads, in, out, record_floats, s);
+    return tlaunch_k<HB, kTChunk, 0>(jobs, count, blocks, threads, in, out, record_floats, s);
 }
 
 } // namespace

@@ -87,6 +87,16 @@ class StreamInfoC(C.Structure):
                 ("backward_transfer", C.c_double), ("reason", C.c_char * 96)]
 
 
+class SweepOptionsC(C.Structure):
+    _fields_ = [("memory_budget", C.c_int64), ("autotune", C.c_int32), ("graph", C.c_int32)]
+
+
+class SweepInfoC(C.Structure):
+    _fields_ = [("candidates", C.c_int32), ("waves", C.c_int32), ("device_bytes", C.c_int64),
+                ("kernel_launches", C.c_int64), ("tune_milliseconds", C.c_double),
+                ("segment_rows", C.c_int32), ("tuned_groups", C.c_int32)]
+
+
 class KernelTimeC(C.Structure):
     _fields_ = [("name", C.c_char * 64), ("launches", C.c_uint64),
                 ("milliseconds", C.c_double), ("bytes", C.c_uint64)]
@@ -141,6 +151,16 @@ SIGNATURES = {
     "dsmvc_gb_inverse_2d_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                      C.c_void_p, C.c_int64, C.POINTER(ConversionC), C.c_void_p],
                                     C.c_int),
+    "dsmvc_gb_plan_build_many": ([C.POINTER(AxisRequestC), C.c_int32, C.c_int32,
+                                  C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_sweep_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int32,
+                               C.c_void_p, C.c_int64, C.POINTER(SweepOptionsC),
+                               C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_sweep_run": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_sweep_run_plain": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_sweep_scores": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_sweep_get_info": ([C.c_void_p, C.POINTER(SweepInfoC)], C.c_int),
+    "dsmvc_gb_sweep_destroy": ([C.c_void_p], None),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -221,13 +241,16 @@ class AxisPlan:
                ("ldlt_bands_f64", np.float64), ("inverse_diagonal_f64", np.float64)]
 
     def __init__(self, request: AxisRequest, custom: Optional[Callable[[float], float]] = None,
-                 cached: bool = True):
+                 cached: bool = True, _handle=None):
         self.request = request
         self._req_c = request.to_c()
         self._custom = CUSTOM_FN(lambda x, _u: float(custom(x))) if custom else CUSTOM_FN()
         h = C.c_void_p()
-        fn = lib().dsmvc_gb_plan_get_or_build if cached else lib().dsmvc_gb_plan_build
-        _check(fn(C.byref(self._req_c), self._custom, None, C.byref(h)))
+        if _handle is not None:
+            h = C.c_void_p(_handle)
+        else:
+            fn = lib().dsmvc_gb_plan_get_or_build if cached else lib().dsmvc_gb_plan_build
+            _check(fn(C.byref(self._req_c), self._custom, None, C.byref(h)))
         self._h = h
         info = PlanInfoC()
         _check(lib().dsmvc_gb_plan_get_info(h, C.byref(info)))
@@ -277,6 +300,15 @@ class AxisPlan:
         if h is not None and h.value and _lib is not None:
             _lib.dsmvc_gb_plan_release(h)
             self._h = None
+
+
+def build_plans(requests: Sequence[AxisRequest], threads: int = 0) -> list:
+    """dsmvc_gb_plan_build_many: uncached plans built on `threads` host
+    threads (0 = all hardware threads)."""
+    reqs = (AxisRequestC * len(requests))(*[r.to_c() for r in requests])
+    out = (C.c_void_p * len(requests))()
+    _check(lib().dsmvc_gb_plan_build_many(reqs, len(requests), int(threads), out))
+    return [AxisPlan(r, _handle=out[i]) for i, r in enumerate(requests)]
 
 
 def planner_cache_stats() -> dict:
@@ -442,6 +474,48 @@ class PreparedBatch:
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
             _lib.dsmvc_gb_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+
+class Sweep:
+    """dsmvc_gb_sweep_*: candidates (h, v) descaled from one device frame,
+    re-upscaled and scored (mean absolute error), one CUDA graph per run."""
+
+    def __init__(self, executor: Executor, candidates: Sequence[tuple], frame_ptr: int,
+                 frame_stride: int, memory_budget: int = 0, autotune: bool = True,
+                 graph: bool = True):
+        n = len(candidates)
+        hs = (C.c_void_p * n)(*[h.handle.value for h, _ in candidates])
+        vs = (C.c_void_p * n)(*[v.handle.value for _, v in candidates])
+        opts = SweepOptionsC(int(memory_budget), 1 if autotune else 0, 1 if graph else 0)
+        h = C.c_void_p()
+        _check(lib().dsmvc_gb_sweep_create(executor._h, hs, vs, n, C.c_void_p(frame_ptr),
+                                           int(frame_stride), C.byref(opts), C.byref(h)))
+        self._h = h
+        self._executor = executor
+        self.count = n
+
+    def run(self, stream: int = 0) -> None:
+        _check(lib().dsmvc_gb_sweep_run(self._h, C.c_void_p(stream or None)))
+
+    def run_plain(self, stream: int = 0) -> None:
+        _check(lib().dsmvc_gb_sweep_run_plain(self._h, C.c_void_p(stream or None)))
+
+    def scores(self, stream: int = 0) -> np.ndarray:
+        out = np.empty(self.count, np.float32)
+        _check(lib().dsmvc_gb_sweep_scores(self._h, out.ctypes.data, C.c_void_p(stream or None)))
+        return out
+
+    def info(self) -> dict:
+        i = SweepInfoC()
+        _check(lib().dsmvc_gb_sweep_get_info(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
+            _lib.dsmvc_gb_sweep_destroy(self._h)
             self._h = None
 
     __del__ = close
