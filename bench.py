@@ -316,7 +316,14 @@ def run_sweep(args, rank, world):
     sweep.run_plain(sid)
     plain_scores = sweep.scores(sid)
     plain = len(cands) / (time.perf_counter() - t3)
-    best = int(np.argmin(scores))
+    # The native resolution shows as the sharpest dip of a kernel's score
+    # against its neighbouring heights.
+    dips = {}
+    for k in synthetic.SWEEP_KERNELS:
+        idx = [i for i, c in enumerate(cands) if c[0] == k]
+        for a, b, c in zip(idx, idx[1:], idx[2:]):
+            dips[b] = float(scores[b] / min(scores[a], scores[c]))
+    best = min(dips, key=dips.get)
 
     hbm, peak_kind = peaks()
     out_bytes = sum(c[1] * c[2] * 4 for c in cands)
@@ -345,8 +352,9 @@ def run_sweep(args, rank, world):
                  "prepare_s": t_prepare, "seconds": t_cold},
         "sweep": {"waves": info["waves"], "device_bytes": info["device_bytes"],
                   "tune_ms": info["tune_milliseconds"], "segment_rows": info["segment_rows"],
-                  "best": {"kernel": cands[best][0], "width": cands[best][1],
-                           "height": cands[best][2], "score": float(scores[best])},
+                  "detected": {"kernel": cands[best][0], "width": cands[best][1],
+                               "height": cands[best][2], "score": float(scores[best]),
+                               "dip": dips[best]},
                   "found_base_height": cands[best][2] == base_h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,

@@ -181,6 +181,7 @@ typedef struct dsmvc_gb_stream_info {
     int32_t ring;                /* source samples per thread ring */
     double backward_transfer;    /* carry influence after one chunk */
     char reason[96];             /* why not eligible */
+    int32_t ring_ok_transposed;  /* the 2D passes' warp-wide block feed fits */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,

@@ -92,6 +92,48 @@ def test_2d_float32(gb, executor, seq_executor, name, hq, vq):
         assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
 
 
+def _random_geometries(count, seed):
+    """Seeded 2D geometries over every kernel family, border and ratios
+    1.0-2.4: gather windows of 4 to 16 samples, partial last chunks and
+    half-bandwidths 1 to 7 (the Debilinear 192x108 -> 112x63 shape among
+    them)."""
+    rng = np.random.default_rng(seed)
+    kernels = [("bilinear", 3, 0, 0.5), ("bicubic", 3, 0, 0.5), ("bicubic", 3, 1 / 3, 1 / 3),
+               ("lanczos", 3, 0, 0.5), ("lanczos", 4, 0, 0.5), ("spline16", 3, 0, 0.5),
+               ("spline36", 3, 0, 0.5)]
+    borders = ["zero", "repeat", "reflect101", "symmetric", "mirror"]
+    out = [((192, 112, 112.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "mirror", 0),
+            (108, 63, 63.0, 0.0, "bilinear", 3, 0, 0.5, 1.0, "mirror", 0))]
+    for i in range(count):
+        k, taps, b, c = kernels[i % len(kernels)]
+        border = borders[int(rng.integers(len(borders)))]
+        axes = []
+        for src in (int(rng.integers(40, 420)), int(rng.integers(24, 260))):
+            dst = max(8, min(src, int(round(src / rng.uniform(1.0, 2.4)))))
+            axes.append((src, dst, float(dst), 0.0, k, taps, b, c, 1.0, border, 0))
+        out.append(tuple(axes))
+    return out
+
+
+RANDOM_2D = _random_geometries(28, 99)
+
+
+@pytest.mark.parametrize("hq,vq", RANDOM_2D, ids=[f"g{i}" for i in range(len(RANDOM_2D))])
+def test_2d_random_geometries(gb, executor, hq, vq):
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = image(v.source_size, h.source_size, 11)
+    scalar = O.inverse_2d(oh, ov, x)
+    got = executor.inverse_2d(h, v, x)
+    err = np.abs(got.astype(np.float64) - scalar)
+    assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS, (hq, vq, err.max())
+    xi = make_input(v.source_size, h.source_size, "u16", 12)
+    conv = gb.integer_conversion(16, False, False)
+    goti = executor.inverse_2d(h, v, xi, conv)
+    wanti = O.inverse_2d(oh, ov, xi, conv)
+    assert np.abs(goti.astype(np.int64) - wanti.astype(np.int64)).max() <= INT_MAX_CODES
+
+
 @pytest.mark.parametrize("sample", ["u8", "u16"])
 @pytest.mark.parametrize("name,hq,vq", CASES_2D[:3], ids=[c[0] for c in CASES_2D[:3]])
 def test_2d_integer(gb, executor, seq_executor, sample, name, hq, vq):

@@ -248,6 +248,7 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->backward_stride = pack.backward_stride;
         info->ring_ok_u16 = pack.ring_ok_u16 ? 1 : 0;
         info->ring_ok_u8 = pack.ring_ok_u8 ? 1 : 0;
+        info->ring_ok_transposed = pack.ring_ok_transposed ? 1 : 0;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;
         info->backward_transfer = pack.backward_transfer;

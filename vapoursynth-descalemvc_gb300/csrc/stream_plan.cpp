@@ -118,11 +118,17 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.window = window;
     out.forward_stride = 4 + window + low;
     out.backward_stride = std::max(4, low);
-    // Whole chunks of records (zeros past the last destination), so that
-    // every chunk copy of the kernel stays inside the arrays.
+    // Whole chunks of records, so that every chunk copy of the kernel stays
+    // inside the arrays.  Records past the last destination are zero except
+    // for their window start, which repeats the last destination's: the
+    // kernels size each ring refill by the window starts of a group's first
+    // and last records, and a padding record must not hide the windows of
+    // the valid destinations before it in its group.
     const auto padded = static_cast<std::size_t>((n + chunk - 1) / chunk) * static_cast<std::size_t>(chunk);
     out.forward.assign(padded * static_cast<std::size_t>(out.forward_stride), 0.0F);
     out.backward.assign(padded * static_cast<std::size_t>(out.backward_stride), 0.0F);
+    for (std::size_t j = static_cast<std::size_t>(n); j < padded; ++j)
+        std::memcpy(&out.forward[j * static_cast<std::size_t>(out.forward_stride)], &s0.back(), sizeof(int));
     for (int j = 0; j < n; ++j) {
         float *f = out.forward.data() + static_cast<std::size_t>(j) * out.forward_stride;
         std::memcpy(&f[0], &s0[j], sizeof(int));

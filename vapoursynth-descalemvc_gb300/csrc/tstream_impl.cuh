@@ -174,8 +174,9 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
 #pragma unroll
     for (int t = 0; t < LC; ++t) {
         if (t % 4 == 0) {
-            // Window end of the group's last destination (records past the
-            // end of the vector hold s0 = 0).
+            // Window end of the group's last destination: window starts
+            // never decrease, and records past the end of the vector repeat
+            // the last destination's start.
             const int s_last = __float_as_int(fwd[(t + 3) * fs]);
             const int need = max(s_last, __float_as_int(fwd[t * fs])) + kw;
             feed.ensure(min(need, p.source_size));
