@@ -312,6 +312,7 @@ def run_sweep(args, rank, world):
         scores = sweep.scores(sid)
     e2e = e2e_steps * len(cands) / (time.perf_counter() - t2)
 
+    stages = sweep.profile(sid)
     t3 = time.perf_counter()
     sweep.run_plain(sid)
     plain_scores = sweep.scores(sid)
@@ -324,6 +325,7 @@ def run_sweep(args, rank, world):
         for a, b, c in zip(idx, idx[1:], idx[2:]):
             dips[b] = float(scores[b] / min(scores[a], scores[c]))
     best = min(dips, key=dips.get)
+    base_idx = [i for i, c in enumerate(cands) if c[0] == "bicubic" and c[2] == base_h][0]
 
     hbm, peak_kind = peaks()
     out_bytes = sum(c[1] * c[2] * 4 for c in cands)
@@ -355,7 +357,9 @@ def run_sweep(args, rank, world):
                   "detected": {"kernel": cands[best][0], "width": cands[best][1],
                                "height": cands[best][2], "score": float(scores[best]),
                                "dip": dips[best]},
-                  "found_base_height": cands[best][2] == base_h},
+                  "found_base_height": cands[best][2] == base_h,
+                  "dip_at_base_bicubic": dips.get(base_idx),
+                  "stages_ms": stages},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
                      "algorithmic_bytes": algo,

@@ -535,6 +535,14 @@ int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *ou
     });
 }
 
+int dsmvc_gb_sweep_profile(dsmvc_gb_sweep *sweep, void *stream, double *milliseconds) {
+    return guarded([&] {
+        if (!sweep || !milliseconds) throw std::invalid_argument("sweep or output is null");
+        const auto t = sweep->sweep->stage_milliseconds(stream);
+        std::copy(t.begin(), t.end(), milliseconds);
+    });
+}
+
 void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep) { delete sweep; }
 
 } // extern "C"

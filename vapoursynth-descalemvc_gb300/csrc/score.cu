@@ -38,7 +38,10 @@ upscale_rows_kernel(const ScoreJob *__restrict__ jobs, int count) {
 }
 
 // For one column tile and one segment of source rows: the upscaled sample
-// sum_e A_v[r, e] * Z[e][s] against frame[r][s], summed per CTA.
+// sum_e A_v[r, e] * Z[e][s] against frame[r][s].  Absolute errors are summed
+// per block of kScoreRowBlock rows (one partial per column tile and row
+// block, whatever the segment length), so the partial sums -- and the
+// score -- do not depend on the segment a launch uses.
 __global__ void __launch_bounds__(kScoreThreads)
 upscale_columns_l1_kernel(const ScoreJob *__restrict__ jobs, int count) {
     __shared__ float warp_sums[kScoreThreads / 32];
@@ -47,29 +50,34 @@ upscale_columns_l1_kernel(const ScoreJob *__restrict__ jobs, int count) {
     const int local = b - job.first_block_cols;
     const int tile = local % job.column_tiles, segment = local / job.column_tiles;
     const int s = tile * static_cast<int>(blockDim.x) + static_cast<int>(threadIdx.x);
-    const int r0 = segment * job.segment_rows;
-    const int r1 = min(job.height, r0 + job.segment_rows);
-    float sum = 0.0f;
-    if (s < job.width) {
-        const float *z = job.upscaled_rows + s;
-        const float *f = job.frame + s;
-        for (int r = r0; r < r1; ++r) {
-            const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
-            float acc = 0.0f;
-            for (std::uint32_t e = e0; e < e1; ++e)
-                acc = fmaf(job.v.weights[e], z[static_cast<std::int64_t>(job.v.indices[e]) * job.upscaled_stride], acc);
-            sum += fabsf(acc - f[static_cast<std::int64_t>(r) * job.frame_stride]);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) warp_sums[warp] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float total = 0.0f;
-        for (int w = 0; w < static_cast<int>(blockDim.x) / 32; ++w) total += warp_sums[w];
-        job.partials[local] = total;
+    const int row_blocks = (job.height + kScoreRowBlock - 1) / kScoreRowBlock;
+    const int seg_blocks = job.segment_rows / kScoreRowBlock;
+    const float *z = job.upscaled_rows + s;
+    const float *f = job.frame + s;
+    for (int rb = segment * seg_blocks; rb < min(row_blocks, (segment + 1) * seg_blocks); ++rb) {
+        const int r0 = rb * kScoreRowBlock, r1 = min(job.height, r0 + kScoreRowBlock);
+        float sum = 0.0f;
+        if (s < job.width) {
+            for (int r = r0; r < r1; ++r) {
+                const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
+                float acc = 0.0f;
+                for (std::uint32_t e = e0; e < e1; ++e)
+                    acc = fmaf(job.v.weights[e], z[static_cast<std::int64_t>(job.v.indices[e]) * job.upscaled_stride],
+                               acc);
+                sum += fabsf(acc - f[static_cast<std::int64_t>(r) * job.frame_stride]);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) warp_sums[warp] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float total = 0.0f;
+            for (int w = 0; w < static_cast<int>(blockDim.x) / 32; ++w) total += warp_sums[w];
+            job.partials[static_cast<std::int64_t>(rb) * job.column_tiles + tile] = total;
+        }
+        __syncthreads();
     }
 }
 
@@ -77,7 +85,7 @@ __global__ void __launch_bounds__(kScoreThreads)
 score_finalize_kernel(const ScoreJob *__restrict__ jobs, float *scores) {
     __shared__ double sums[kScoreThreads];
     const ScoreJob &job = jobs[blockIdx.x];
-    const int n = job.column_tiles * ((job.height + job.segment_rows - 1) / job.segment_rows);
+    const int n = job.column_tiles * ((job.height + kScoreRowBlock - 1) / kScoreRowBlock);
     double acc = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) acc += static_cast<double>(job.partials[i]);
     sums[threadIdx.x] = acc;

@@ -33,10 +33,10 @@ struct ScoreJob {
     std::int64_t frame_stride;
     std::int32_t width, height;
     ForwardCsr h, v;                // forward operators of the two axes
-    float *partials;                // column tiles x row segments
+    float *partials;                // row blocks x column tiles
     std::int32_t first_block_rows;  // row-pass blocks before this job
     std::int32_t first_block_cols;  // column-pass blocks before this job
-    std::int32_t segment_rows;      // source rows per column-pass block
+    std::int32_t segment_rows;      // source rows per column-pass block (a multiple of kScoreRowBlock)
     std::int32_t column_tiles;      // ceil(width / threads of the column pass)
 };
 
@@ -45,6 +45,7 @@ struct ScoreJob {
 namespace dsmvc_gb {
 
 constexpr int kScoreThreads = 256;
+constexpr int kScoreRowBlock = 16;   // rows per partial sum
 
 // Row pass: one block per descaled row; `max_cols` bounds every job's cols
 // (the row is staged in shared memory).
@@ -52,7 +53,8 @@ int launch_upscale_rows(const dev::ScoreJob *jobs, int job_count, int total_bloc
                         void *stream);
 // Column pass + absolute error: one block per (column tile, row segment).
 int launch_upscale_columns_l1(const dev::ScoreJob *jobs, int job_count, int total_blocks, void *stream);
-// scores[i] = sum of job i's partials / (width * height), one block per job.
+// scores[i] = sum of job i's partials / (width * height), one block per job,
+// in a fixed order.
 int launch_score_finalize(const dev::ScoreJob *jobs, int job_count, float *scores, void *stream);
 
 } // namespace dsmvc_gb

@@ -72,8 +72,7 @@ HostForward forward_csr(const AxisPlan &p) {
 
 } // namespace
 
-constexpr int kMinSegment = 16;
-constexpr int kSegments[] = {16, 32, 64, 128, 256};
+constexpr int kSegments[] = {16, 32, 64, 128, 256};   // multiples of kScoreRowBlock
 
 struct Sweep::Impl {
     Executor *executor = nullptr;
@@ -147,8 +146,7 @@ struct Sweep::Impl {
     // out each wave's descaled planes, row-pass planes and partial sums.
     void plan_waves() {
         const std::size_t budget = options.memory_budget ? options.memory_budget : (32ULL << 30);
-        // Room for the partial sums of the finest row segment the tuner tries.
-        const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kMinSegment) * 4);
+        const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kScoreRowBlock) * 4);
         std::size_t y_bytes = 0, z_bytes = 0, p_bytes = 0, s_bytes = 0;
         std::size_t y_max = 0, z_max = 0, p_max = 0, s_max = 0;
         y_offset.resize(candidates.size());
@@ -408,6 +406,46 @@ void Sweep::run_plain(void *stream) {
             check(cudaStreamSynchronize(s), "synchronizing");
         }
     }
+}
+
+std::array<double, 4> Sweep::stage_milliseconds(void *stream) {
+    auto &m = *impl_;
+    auto s = static_cast<cudaStream_t>(stream);
+    std::array<cudaEvent_t, 8> ev{};
+    for (auto &e : ev) check(cudaEventCreate(&e), "creating event");
+    std::array<double, 4> out{};
+    try {
+        for (const auto &w : m.waves) {
+            check(cudaEventRecord(ev[0], s), "recording event");
+            w.batch->launch(s);
+            check(cudaEventRecord(ev[1], s), "recording event");
+            check(launch_upscale_rows(m.wave_jobs(w), w.count, w.row_blocks, w.max_cols, s), "launching");
+            check(cudaEventRecord(ev[2], s), "recording event");
+            check(launch_upscale_columns_l1(m.wave_jobs(w), w.count, w.column_blocks, s), "launching");
+            check(cudaEventRecord(ev[3], s), "recording event");
+            check(cudaEventSynchronize(ev[3]), "waiting for event");
+            for (int k = 0; k < 3; ++k) {
+                float ms = 0.0F;
+                check(cudaEventElapsedTime(&ms, ev[static_cast<std::size_t>(k)], ev[static_cast<std::size_t>(k + 1)]),
+                      "reading event");
+                out[static_cast<std::size_t>(k)] += ms;
+            }
+        }
+        check(cudaEventRecord(ev[4], s), "recording event");
+        check(launch_score_finalize(reinterpret_cast<const dev::ScoreJob *>(m.job_mem.data()),
+                                    static_cast<int>(m.candidates.size()),
+                                    reinterpret_cast<float *>(m.score_mem.data()), s), "launching");
+        check(cudaEventRecord(ev[5], s), "recording event");
+        check(cudaEventSynchronize(ev[5]), "waiting for event");
+        float ms = 0.0F;
+        check(cudaEventElapsedTime(&ms, ev[4], ev[5]), "reading event");
+        out[3] = ms;
+    } catch (...) {
+        for (auto &e : ev) cudaEventDestroy(e);
+        throw;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return out;
 }
 
 void Sweep::read_scores(float *host, void *stream) {

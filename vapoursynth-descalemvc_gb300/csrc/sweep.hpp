@@ -18,6 +18,7 @@
 #include "executor.hpp"
 #include "planner.hpp"
 
+#include <array>
 #include <cstddef>
 #include <memory>
 #include <utility>
@@ -60,6 +61,10 @@ public:
     void run_plain(void *stream);
     // Waits for `stream` and copies the scores (candidate order) to `host`.
     void read_scores(float *host, void *stream);
+    // Runs the sweep once without the graph, with CUDA events between its
+    // stages, and returns their milliseconds: descale passes, row
+    // re-upscale, column re-upscale with the error sums, score reduction.
+    [[nodiscard]] std::array<double, 4> stage_milliseconds(void *stream);
     [[nodiscard]] const float *device_scores() const;
     [[nodiscard]] SweepInfo info() const;
 

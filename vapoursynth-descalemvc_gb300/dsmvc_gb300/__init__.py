@@ -161,6 +161,7 @@ SIGNATURES = {
     "dsmvc_gb_sweep_run_plain": ([C.c_void_p, C.c_void_p], C.c_int),
     "dsmvc_gb_sweep_scores": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "dsmvc_gb_sweep_get_info": ([C.c_void_p, C.POINTER(SweepInfoC)], C.c_int),
+    "dsmvc_gb_sweep_profile": ([C.c_void_p, C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "dsmvc_gb_sweep_destroy": ([C.c_void_p], None),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
@@ -508,6 +509,12 @@ class Sweep:
         out = np.empty(self.count, np.float32)
         _check(lib().dsmvc_gb_sweep_scores(self._h, out.ctypes.data, C.c_void_p(stream or None)))
         return out
+
+    def profile(self, stream: int = 0) -> dict:
+        """Stage milliseconds of one ungraphed run."""
+        ms = (C.c_double * 4)()
+        _check(lib().dsmvc_gb_sweep_profile(self._h, C.c_void_p(stream or None), ms))
+        return dict(zip(("descale", "upscale_rows", "upscale_columns_l1", "finalize"), list(ms)))
 
     def info(self) -> dict:
         i = SweepInfoC()
