@@ -250,9 +250,16 @@ struct Sweep::Impl {
         return reinterpret_cast<const dev::ScoreJob *>(job_mem.data()) + w.first;
     }
 
+    [[nodiscard]] float *wave_scores(const Wave &w) const {
+        return reinterpret_cast<float *>(score_mem.data()) + w.first;
+    }
+
+    // A wave's scores are reduced before the next wave reuses its buffers
+    // (descaled planes, row-pass planes and partial sums).
     void enqueue_scoring(const Wave &w, cudaStream_t s) {
         check(launch_upscale_rows(wave_jobs(w), w.count, w.row_blocks, w.max_cols, s), "launching upscale rows");
         check(launch_upscale_columns_l1(wave_jobs(w), w.count, w.column_blocks, s), "launching upscale columns");
+        check(launch_score_finalize(wave_jobs(w), w.count, wave_scores(w), s), "launching score finalize");
     }
 
     void enqueue_all(cudaStream_t s) {
@@ -260,10 +267,6 @@ struct Sweep::Impl {
             w.batch->launch(s);
             enqueue_scoring(w, s);
         }
-        check(launch_score_finalize(reinterpret_cast<const dev::ScoreJob *>(job_mem.data()),
-                                    static_cast<int>(candidates.size()),
-                                    reinterpret_cast<float *>(score_mem.data()), s),
-              "launching score finalize");
     }
 
     template <class F> float time_ms(F &&f, int reps) {
@@ -423,23 +426,16 @@ std::array<double, 4> Sweep::stage_milliseconds(void *stream) {
             check(cudaEventRecord(ev[2], s), "recording event");
             check(launch_upscale_columns_l1(m.wave_jobs(w), w.count, w.column_blocks, s), "launching");
             check(cudaEventRecord(ev[3], s), "recording event");
-            check(cudaEventSynchronize(ev[3]), "waiting for event");
-            for (int k = 0; k < 3; ++k) {
+            check(launch_score_finalize(m.wave_jobs(w), w.count, m.wave_scores(w), s), "launching");
+            check(cudaEventRecord(ev[4], s), "recording event");
+            check(cudaEventSynchronize(ev[4]), "waiting for event");
+            for (int k = 0; k < 4; ++k) {
                 float ms = 0.0F;
                 check(cudaEventElapsedTime(&ms, ev[static_cast<std::size_t>(k)], ev[static_cast<std::size_t>(k + 1)]),
                       "reading event");
                 out[static_cast<std::size_t>(k)] += ms;
             }
         }
-        check(cudaEventRecord(ev[4], s), "recording event");
-        check(launch_score_finalize(reinterpret_cast<const dev::ScoreJob *>(m.job_mem.data()),
-                                    static_cast<int>(m.candidates.size()),
-                                    reinterpret_cast<float *>(m.score_mem.data()), s), "launching");
-        check(cudaEventRecord(ev[5], s), "recording event");
-        check(cudaEventSynchronize(ev[5]), "waiting for event");
-        float ms = 0.0F;
-        check(cudaEventElapsedTime(&ms, ev[4], ev[5]), "reading event");
-        out[3] = ms;
     } catch (...) {
         for (auto &e : ev) cudaEventDestroy(e);
         throw;
@@ -464,8 +460,7 @@ SweepInfo Sweep::info() const {
     i.waves = static_cast<int>(m.waves.size());
     i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.z_mem.bytes + m.partial_mem.bytes
         + m.scratch_mem.bytes + m.job_mem.bytes + m.plain_job_mem.bytes + m.score_mem.bytes;
-    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 2;
-    i.kernel_launches += 1;
+    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 3;
     i.tune_milliseconds = m.tune_ms;
     i.segment_rows = m.segment_rows;
     i.tuning = m.tuning;
