@@ -103,12 +103,20 @@ typedef struct dsmvc_gb_planner_stats {
     uint64_t plan_resident_bytes;
 } dsmvc_gb_planner_stats;
 
+/* Executor counters.  The plan cache holds device copies of plans that were
+ * not prepared (an LRU keyed by plan identity, DSMVC_GB_PLAN_CACHE_MB =
+ * 16..4096 MiB, default 256; the reference's packed-plan cache,
+ * src/cuda/cuda_executor.cpp:1936-2020, DSMVC_CUDA_PLAN_CACHE_MB). */
 typedef struct dsmvc_gb_executor_stats {
     uint64_t launches;
     uint64_t plane_tasks;
     uint64_t plan_uploads;
     uint64_t device_plan_bytes;
     uint64_t workspace_bytes;
+    uint64_t plan_cache_hits;
+    uint64_t plan_cache_misses;
+    uint64_t plan_cache_evictions;
+    uint64_t plan_cache_bytes;
 } dsmvc_gb_executor_stats;
 
 /* One plane of a device-resident batch.  `horizontal`/`vertical` may be

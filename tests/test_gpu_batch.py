@@ -119,3 +119,20 @@ def test_prepared_batch_float64_status(gb, executor):
     batch.launch(sid)
     batch.check(sid)
     assert torch.isfinite(dy).all()
+
+
+def test_unprepared_plans_use_the_device_plan_cache(gb):
+    ex = gb.Executor(0)
+    h = gb.AxisPlan(product_request(gb, SMALL_H), cached=False)
+    v = gb.AxisPlan(product_request(gb, SMALL_V), cached=False)
+    x = make_input(v.source_size, h.source_size, "f32", 41)
+    first = ex.inverse_2d(h, v, x)
+    s1 = ex.stats()
+    second = ex.inverse_2d(h, v, x)
+    s2 = ex.stats()
+    assert np.array_equal(first, second)
+    assert s1["plan_cache_misses"] == 2 and s2["plan_cache_misses"] == 2
+    assert s2["plan_uploads"] == s1["plan_uploads"]
+    assert s2["plan_cache_hits"] == s1["plan_cache_hits"] + 2
+    assert s2["plan_cache_bytes"] > 0
+    ex.close()

@@ -303,6 +303,10 @@ int dsmvc_gb_executor_get_stats(dsmvc_gb_executor *executor, dsmvc_gb_executor_s
         out->plan_uploads = s.plan_uploads;
         out->device_plan_bytes = s.device_plan_bytes;
         out->workspace_bytes = s.workspace_bytes;
+        out->plan_cache_hits = s.plan_cache_hits;
+        out->plan_cache_misses = s.plan_cache_misses;
+        out->plan_cache_evictions = s.plan_cache_evictions;
+        out->plan_cache_bytes = s.plan_cache_bytes;
     });
 }
 
@@ -310,7 +314,8 @@ int dsmvc_gb_inverse_rows(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan
                           const float *input, int64_t input_stride, float *output,
                           int64_t output_stride, int32_t rows) {
     return guarded([&] {
-        exec_of(executor).inverse_rows(plan_of(plan), input, input_stride, output, output_stride, rows);
+        exec_of(executor).inverse_rows(plan_of(plan), input, input_stride, output, output_stride, rows,
+                                       plan->plan);
     });
 }
 
@@ -319,7 +324,7 @@ int dsmvc_gb_inverse_columns(dsmvc_gb_executor *executor, const dsmvc_gb_plan *p
                              int64_t output_stride, int32_t columns) {
     return guarded([&] {
         exec_of(executor).inverse_columns(plan_of(plan), input, input_stride, output, output_stride,
-                                          columns);
+                                          columns, plan->plan);
     });
 }
 
@@ -328,7 +333,8 @@ int dsmvc_gb_inverse_2d(dsmvc_gb_executor *executor, const dsmvc_gb_plan *horizo
                         float *output, int64_t output_stride) {
     return guarded([&] {
         exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::f32,
-                                     input, input_stride, output, output_stride, {});
+                                     input, input_stride, output, output_stride, {}, horizontal->plan,
+                                     vertical->plan);
     });
 }
 
@@ -339,7 +345,7 @@ int dsmvc_gb_inverse_2d_u8(dsmvc_gb_executor *executor, const dsmvc_gb_plan *hor
     return guarded([&] {
         exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::u8,
                                      input, input_stride, output, output_stride,
-                                     to_conversion(conversion));
+                                     to_conversion(conversion), horizontal->plan, vertical->plan);
     });
 }
 
@@ -350,7 +356,7 @@ int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor, const dsmvc_gb_plan *ho
     return guarded([&] {
         exec_of(executor).inverse_2d(plan_of(horizontal), plan_of(vertical), dsmvc_gb::dev::Sample::u16,
                                      input, input_stride, output, output_stride,
-                                     to_conversion(conversion));
+                                     to_conversion(conversion), horizontal->plan, vertical->plan);
     });
 }
 
@@ -366,6 +372,8 @@ std::vector<dsmvc_gb::PlaneTask> task_list(const dsmvc_gb_plane_task *tasks, int
         auto &d = list[static_cast<std::size_t>(i)];
         d.horizontal = t.horizontal ? &plan_of(t.horizontal) : nullptr;
         d.vertical = t.vertical ? &plan_of(t.vertical) : nullptr;
+        if (t.horizontal) d.horizontal_keep = t.horizontal->plan;
+        if (t.vertical) d.vertical_keep = t.vertical->plan;
         d.input = t.input;
         d.input_stride = t.input_stride;
         d.output = t.output;
@@ -469,7 +477,6 @@ int dsmvc_gb_profile_read(dsmvc_gb_executor *executor, dsmvc_gb_kernel_time *out
 }
 
 struct dsmvc_gb_sweep {
-    std::vector<std::shared_ptr<const dsmvc_gb::AxisPlan>> keep;
     std::unique_ptr<dsmvc_gb::Sweep> sweep;
 };
 
@@ -481,12 +488,10 @@ int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor, const dsmvc_gb_plan *cons
         *out = nullptr;
         if (count <= 0 || !horizontal || !vertical) throw std::invalid_argument("invalid candidate list");
         auto s = std::make_unique<dsmvc_gb_sweep>();
-        std::vector<std::pair<const dsmvc_gb::AxisPlan *, const dsmvc_gb::AxisPlan *>> list;
+        std::vector<dsmvc_gb::Sweep::Candidate> list;
         for (int32_t i = 0; i < count; ++i) {
             if (!horizontal[i] || !vertical[i]) throw std::invalid_argument("candidate plan is null");
-            s->keep.push_back(horizontal[i]->plan);
-            s->keep.push_back(vertical[i]->plan);
-            list.emplace_back(horizontal[i]->plan.get(), vertical[i]->plan.get());
+            list.emplace_back(horizontal[i]->plan, vertical[i]->plan);
         }
         dsmvc_gb::SweepOptions o;
         if (options) {

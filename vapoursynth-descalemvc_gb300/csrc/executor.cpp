@@ -20,6 +20,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
+#include <list>
 #include <map>
 #include <mutex>
 #include <stdexcept>
@@ -88,9 +89,8 @@ struct DevicePlan {
     std::size_t bytes = 0;
 };
 
-std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
-    if (!plan || !plan->valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
-    const AxisPlan &p = *plan;
+std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const AxisPlan> keep) {
+    if (!p.valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
     const bool f64 = p.requires_float64();
     std::vector<std::pair<const void *, std::size_t>> parts = {
         {p.transpose_offsets.data(), p.transpose_offsets.size() * 4},
@@ -117,7 +117,7 @@ std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
     std::vector<char> host(total, 0);
     for (std::size_t i = 0; i < parts.size(); ++i)
         if (parts[i].second) std::memcpy(host.data() + offsets[i], parts[i].first, parts[i].second);
-    auto dp = std::make_unique<DevicePlan>();
+    auto dp = std::make_shared<DevicePlan>();
     dp->memory.reserve(total);
     cuda_check(cudaMemcpy(dp->memory.data(), host.data(), total, cudaMemcpyHostToDevice), "uploading plan");
     char *base = dp->memory.data();
@@ -150,7 +150,7 @@ std::unique_ptr<DevicePlan> upload_plan(std::shared_ptr<const AxisPlan> plan) {
         sv.backward = reinterpret_cast<const float *>(base + offsets[9]);
     }
     dp->bytes = total;
-    dp->keep = std::move(plan);
+    dp->keep = std::move(keep);
     return dp;
 }
 
@@ -232,7 +232,18 @@ struct DeviceGuard {
 struct Executor::Impl {
     int device = 0;
     mutable std::mutex mutex;
-    std::unordered_map<const AxisPlan *, std::unique_ptr<DevicePlan>> plans;
+    std::unordered_map<const AxisPlan *, std::shared_ptr<DevicePlan>> plans;
+    // Device plan cache of unprepared plans given with their owners: entries
+    // hold the owner, so a key never outlives its plan; an evicted entry's
+    // memory is released when the last submission holding it is done with it.
+    struct CacheEntry {
+        std::shared_ptr<DevicePlan> plan;
+        std::list<const AxisPlan *>::iterator lru;
+    };
+    std::unordered_map<const AxisPlan *, CacheEntry> cache;
+    std::list<const AxisPlan *> cache_lru;
+    std::size_t cache_bytes = 0;
+    std::size_t cache_capacity = 256ULL << 20;
     bool sealed = false;
     // Synchronous host calls take one of these slots (the reference's
     // execution slots, src/cuda/cuda_executor.cpp:1102-1160).
@@ -271,17 +282,52 @@ struct Executor::Impl {
     bool allow_stream = true;
     std::vector<Record> records;
 
-    const DevicePlan &device_plan(const AxisPlan &plan,
-                                  std::vector<std::unique_ptr<DevicePlan>> &temporaries) {
+    // Prepared plans first, then the cache (plans with owners), else a
+    // private upload for this submission (`held` keeps every non-prepared
+    // device plan alive; `private_uploads` counts the uncached ones).
+    const DevicePlan &device_plan(const AxisPlan &plan, const std::shared_ptr<const AxisPlan> &keep,
+                                  std::vector<std::shared_ptr<DevicePlan>> &held, int &private_uploads) {
         {
             std::scoped_lock lock(mutex);
             if (auto it = plans.find(&plan); it != plans.end()) return *it->second;
+            if (keep && keep.get() == &plan) {
+                if (auto it = cache.find(&plan); it != cache.end()) {
+                    cache_lru.splice(cache_lru.end(), cache_lru, it->second.lru);
+                    ++stats.plan_cache_hits;
+                    held.push_back(it->second.plan);
+                    return *held.back();
+                }
+            }
         }
-        // Not prepared: upload a private copy for this call only.
-        temporaries.push_back(upload_plan(std::make_shared<const AxisPlan>(plan)));
+        if (!keep || keep.get() != &plan) {
+            held.push_back(upload_plan(plan, nullptr));
+            ++private_uploads;
+            std::scoped_lock lock(mutex);
+            ++stats.plan_uploads;
+            return *held.back();
+        }
+        auto dp = upload_plan(plan, keep);
         std::scoped_lock lock(mutex);
         ++stats.plan_uploads;
-        return *temporaries.back();
+        if (auto it = cache.find(&plan); it != cache.end()) {
+            // Another thread uploaded it meanwhile.
+            held.push_back(it->second.plan);
+            return *held.back();
+        }
+        ++stats.plan_cache_misses;
+        cache_lru.push_back(&plan);
+        cache.emplace(&plan, CacheEntry{dp, std::prev(cache_lru.end())});
+        cache_bytes += dp->bytes;
+        while (cache_bytes > cache_capacity && cache.size() > 1) {
+            const AxisPlan *victim = cache_lru.front();
+            auto v = cache.find(victim);
+            cache_bytes -= v->second.plan->bytes;
+            cache_lru.pop_front();
+            cache.erase(v);
+            ++stats.plan_cache_evictions;
+        }
+        held.push_back(std::move(dp));
+        return *held.back();
     }
 
     Workspace &acquire_slot(std::size_t &index) {
@@ -335,7 +381,8 @@ struct Executor::Impl {
     using GroupTuple = std::tuple<int, int, int, int, int, int>;
     using Tuning = std::map<GroupTuple, int>;
     struct Compiled {
-        std::vector<std::unique_ptr<DevicePlan>> temporaries;
+        std::vector<std::shared_ptr<DevicePlan>> temporaries;   // non-prepared plans in use
+        int private_uploads = 0;
         std::vector<char> table;
         std::vector<Launch> launches;
         std::size_t scratch_bytes = 0;
@@ -403,8 +450,8 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         const AxisPlan *h = task.horizontal, *v = task.vertical;
         if (!h && !v) throw std::invalid_argument("plane task without a plan");
         auto &r = routes[t];
-        r.h = h ? &device_plan(*h, temporaries) : nullptr;
-        r.v = v ? &device_plan(*v, temporaries) : nullptr;
+        r.h = h ? &device_plan(*h, task.horizontal_keep, temporaries, out.private_uploads) : nullptr;
+        r.v = v ? &device_plan(*v, task.vertical_keep, temporaries, out.private_uploads) : nullptr;
         r.f64 = (h && h->requires_float64()) || (v && v->requires_float64());
         if (!r.f64 && allow_stream) {
             r.h_stream = r.h && stream_row_ok(*r.h, h && v ? task.sample : dev::Sample::f32);
@@ -669,8 +716,10 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks)
     if (c.launches.empty()) return;
     ws.upload_table(c.table);
     launch(c, ws.jobs.data(), ws.stream, ws.status);
-    if (!c.temporaries.empty()) {
-        // Private plan copies must outlive the kernels that read them.
+    if (c.private_uploads > 0) {
+        // Private plan uploads must outlive the kernels that read them.
+        // (Cached plans evicted meanwhile are released by cudaFree, which
+        // waits for the work in flight.)
         cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
     }
 }
@@ -698,6 +747,12 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     impl_->device = device;
     if (const char *env = std::getenv("DSMVC_GB_STREAM"); env && std::string(env) == "0")
         impl_->allow_stream = false;
+    if (const char *env = std::getenv("DSMVC_GB_PLAN_CACHE_MB")) {
+        char *end = nullptr;
+        const long v = std::strtol(env, &end, 10);
+        if (end && *end == '\0' && v >= 16 && v <= 4096)
+            impl_->cache_capacity = static_cast<std::size_t>(v) << 20;
+    }
     if (const char *env = std::getenv("DSMVC_GB_STREAMS")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);
@@ -726,7 +781,7 @@ void Executor::prepare(std::shared_ptr<const AxisPlan> plan) {
         if (impl_->sealed) throw std::logic_error("executor is sealed; prepare plans before seal()");
     }
     DeviceGuard guard(impl_->device);
-    auto dp = upload_plan(plan);
+    auto dp = upload_plan(*plan, plan);
     std::scoped_lock lock(impl_->mutex);
     impl_->stats.plan_uploads += 1;
     impl_->stats.device_plan_bytes += dp->bytes;
@@ -755,7 +810,8 @@ void check_columns(const AxisPlan &plan, const void *in, std::ptrdiff_t is, cons
 } // namespace
 
 void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdiff_t is,
-                            float *output, std::ptrdiff_t os, std::int32_t rows) {
+                            float *output, std::ptrdiff_t os, std::int32_t rows,
+                            const std::shared_ptr<const AxisPlan> &keep) {
     check_rows(plan, input, is, output, os, rows);
     if (rows == 0) return;
     DeviceGuard guard(impl_->device);
@@ -771,6 +827,7 @@ void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdi
                                      rows, cudaMemcpyHostToDevice, ws.stream), "uploading rows");
         PlaneTask t;
         t.horizontal = &plan;
+        t.horizontal_keep = keep;
         t.input = din;
         t.input_stride = plan.source_size;
         t.output = dout;
@@ -790,7 +847,8 @@ void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdi
 }
 
 void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::ptrdiff_t is,
-                               float *output, std::ptrdiff_t os, std::int32_t columns) {
+                               float *output, std::ptrdiff_t os, std::int32_t columns,
+                               const std::shared_ptr<const AxisPlan> &keep) {
     check_columns(plan, input, is, output, os, columns);
     if (columns == 0) return;
     DeviceGuard guard(impl_->device);
@@ -806,6 +864,7 @@ void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::pt
                                      cudaMemcpyHostToDevice, ws.stream), "uploading columns");
         PlaneTask t;
         t.vertical = &plan;
+        t.vertical_keep = keep;
         t.input = din;
         t.input_stride = columns;
         t.output = dout;
@@ -826,7 +885,8 @@ void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::pt
 
 void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
                           const void *input, std::ptrdiff_t is, void *output, std::ptrdiff_t os,
-                          const IntegerConversion &conv) {
+                          const IntegerConversion &conv, const std::shared_ptr<const AxisPlan> &h_keep,
+                          const std::shared_ptr<const AxisPlan> &v_keep) {
     if (!h.valid() || !v.valid() || !input || !output || is < h.source_size
         || os < h.destination_size || sample == dev::Sample::f64)
         throw std::invalid_argument("invalid 2D executor arguments");
@@ -855,6 +915,8 @@ void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample samp
         PlaneTask t;
         t.horizontal = &h;
         t.vertical = &v;
+        t.horizontal_keep = h_keep;
+        t.vertical_keep = v_keep;
         t.input = din;
         t.input_stride = h.source_size;
         t.output = dout;
@@ -1065,6 +1127,7 @@ std::vector<KernelTime> Executor::kernel_times() {
 ExecutorStats Executor::stats() const {
     std::scoped_lock lock(impl_->mutex);
     ExecutorStats s = impl_->stats;
+    s.plan_cache_bytes = impl_->cache_bytes;
     for (const auto &ws : impl_->slots) s.workspace_bytes += ws->scratch.size() + ws->staging.size();
     for (const auto &[k, ws] : impl_->stream_spaces) s.workspace_bytes += ws->scratch.size();
     return s;

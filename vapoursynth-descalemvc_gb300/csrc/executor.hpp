@@ -46,6 +46,10 @@ struct PlaneTask {
     // Source extent of a one-axis task: rows for rows-only, columns for
     // columns-only (ignored for 2D tasks).
     std::int32_t vectors = 0;
+    // Optional owners of the plans.  A plan that was not prepared is looked
+    // up in (or added to) the executor's device plan cache when its owner is
+    // given; otherwise it is uploaded for this submission only.
+    std::shared_ptr<const AxisPlan> horizontal_keep, vertical_keep;
 };
 
 // Per-kernel CUDA-event timing aggregated by kernel name; `bytes` counts the
@@ -63,6 +67,13 @@ struct ExecutorStats {
     std::uint64_t plan_uploads = 0;
     std::size_t device_plan_bytes = 0;
     std::size_t workspace_bytes = 0;
+    // Device plan cache of plans that were not prepared (an LRU keyed by
+    // plan identity and bounded by DSMVC_GB_PLAN_CACHE_MB, 16..4096 MiB,
+    // default 256; the counterpart of DSMVC_CUDA_PLAN_CACHE_MB).
+    std::uint64_t plan_cache_hits = 0;
+    std::uint64_t plan_cache_misses = 0;
+    std::uint64_t plan_cache_evictions = 0;
+    std::size_t plan_cache_bytes = 0;
 };
 
 class Executor;
@@ -128,13 +139,18 @@ public:
     void seal();
 
     // Synchronous host-frame calls (reference Executor contract).
+    // The optional owners let unprepared plans use the device plan cache.
     void inverse_rows(const AxisPlan &plan, const float *input, std::ptrdiff_t input_stride,
-                      float *output, std::ptrdiff_t output_stride, std::int32_t rows);
+                      float *output, std::ptrdiff_t output_stride, std::int32_t rows,
+                      const std::shared_ptr<const AxisPlan> &keep = nullptr);
     void inverse_columns(const AxisPlan &plan, const float *input, std::ptrdiff_t input_stride,
-                         float *output, std::ptrdiff_t output_stride, std::int32_t columns);
+                         float *output, std::ptrdiff_t output_stride, std::int32_t columns,
+                         const std::shared_ptr<const AxisPlan> &keep = nullptr);
     void inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
                     const void *input, std::ptrdiff_t input_stride, void *output,
-                    std::ptrdiff_t output_stride, const IntegerConversion &conversion);
+                    std::ptrdiff_t output_stride, const IntegerConversion &conversion,
+                    const std::shared_ptr<const AxisPlan> &h_keep = nullptr,
+                    const std::shared_ptr<const AxisPlan> &v_keep = nullptr);
 
     // Device-pointer batch: every task is enqueued on `stream` (null: the
     // executor's own).  With `synchronize` the call waits and raises on a

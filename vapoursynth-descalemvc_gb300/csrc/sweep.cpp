@@ -77,6 +77,7 @@ constexpr int kSegments[] = {16, 32, 64, 128, 256};   // multiples of kScoreRowB
 struct Sweep::Impl {
     Executor *executor = nullptr;
     std::vector<std::pair<const AxisPlan *, const AxisPlan *>> candidates;
+    std::vector<Sweep::Candidate> owners;
     const float *frame = nullptr;
     std::ptrdiff_t frame_stride = 0;
     int width = 0, height = 0;
@@ -192,6 +193,8 @@ struct Sweep::Impl {
                 PlaneTask t;
                 t.horizontal = candidates[i].first;
                 t.vertical = candidates[i].second;
+                t.horizontal_keep = owners[i].first;
+                t.vertical_keep = owners[i].second;
                 t.input = frame;
                 t.input_stride = frame_stride;
                 t.output = y_mem.data() + y_offset[i];
@@ -352,10 +355,12 @@ struct Sweep::Impl {
     }
 };
 
-Sweep::Sweep(Executor &executor, const std::vector<std::pair<const AxisPlan *, const AxisPlan *>> &candidates,
-             const float *frame, std::ptrdiff_t frame_stride, const SweepOptions &options)
+Sweep::Sweep(Executor &executor, const std::vector<Candidate> &owners, const float *frame,
+             std::ptrdiff_t frame_stride, const SweepOptions &options)
     : impl_(std::make_unique<Impl>()) {
-    if (candidates.empty() || !frame) throw std::invalid_argument("a sweep needs candidates and a frame");
+    if (owners.empty() || !frame) throw std::invalid_argument("a sweep needs candidates and a frame");
+    std::vector<std::pair<const AxisPlan *, const AxisPlan *>> candidates;
+    for (const auto &[h, v] : owners) candidates.emplace_back(h.get(), v.get());
     const AxisPlan *h0 = candidates.front().first, *v0 = candidates.front().second;
     if (!h0 || !v0) throw std::invalid_argument("sweep candidate without a plan");
     for (const auto &[h, v] : candidates) {
@@ -367,6 +372,7 @@ Sweep::Sweep(Executor &executor, const std::vector<std::pair<const AxisPlan *, c
     auto &m = *impl_;
     m.executor = &executor;
     m.candidates = candidates;
+    m.owners = owners;
     m.frame = frame;
     m.frame_stride = frame_stride;
     m.width = h0->source_size;

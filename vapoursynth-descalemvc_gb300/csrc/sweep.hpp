@@ -46,10 +46,11 @@ class Sweep {
 public:
     // `frame` is a device plane of horizontal source size x vertical source
     // size Float32 samples, `frame_stride` samples apart; every candidate's
-    // plans must have those source sizes.  Plans and the frame must outlive
-    // the sweep.
-    Sweep(Executor &executor, const std::vector<std::pair<const AxisPlan *, const AxisPlan *>> &candidates,
-          const float *frame, std::ptrdiff_t frame_stride, const SweepOptions &options);
+    // plans (horizontal, vertical) must have those source sizes.  The frame
+    // must outlive the sweep.
+    using Candidate = std::pair<std::shared_ptr<const AxisPlan>, std::shared_ptr<const AxisPlan>>;
+    Sweep(Executor &executor, const std::vector<Candidate> &candidates, const float *frame,
+          std::ptrdiff_t frame_stride, const SweepOptions &options);
     ~Sweep();
     Sweep(const Sweep &) = delete;
     Sweep &operator=(const Sweep &) = delete;

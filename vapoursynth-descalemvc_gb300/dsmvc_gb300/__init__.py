@@ -68,7 +68,9 @@ class PlannerStatsC(C.Structure):
 class ExecutorStatsC(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("plane_tasks", C.c_uint64),
                 ("plan_uploads", C.c_uint64), ("device_plan_bytes", C.c_uint64),
-                ("workspace_bytes", C.c_uint64)]
+                ("workspace_bytes", C.c_uint64), ("plan_cache_hits", C.c_uint64),
+                ("plan_cache_misses", C.c_uint64), ("plan_cache_evictions", C.c_uint64),
+                ("plan_cache_bytes", C.c_uint64)]
 
 
 class PlaneTaskC(C.Structure):
