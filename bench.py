@@ -368,6 +368,141 @@ def run_sweep(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+SERVE_SIZES = [(1280, 720), (1920, 1080), (2560, 1440), (3840, 2160)]
+SERVE_KERNELS = [("bilinear", 3, 0.0, 0.5), ("bicubic", 3, 0.0, 0.5), ("lanczos", 3, 0.0, 0.5),
+                 ("spline36", 3, 0.0, 0.5)]
+SERVE_METRIC = "served Mpix/s with p50/p99 latency (mixed descale requests, Poisson arrivals)"
+
+
+def run_serving(args, rank, world):
+    """Request loop: seeded Poisson arrivals of mixed descale requests --
+    sources 1280x720..3840x2160, target ratios from a seeded set of 12 in
+    [0.5, 0.9], kernels uniform over bilinear / bicubic(0, 0.5) / lanczos3 /
+    spline36, 80 % Float32 (f64mode=0) and 20 % f64mode=2, GRAYS float32 or
+    YUV420P16 -- submitted through the server (host frames in pinned memory,
+    copies included) at each offered rate for a fixed time."""
+    import torch
+    import dsmvc_gb300 as gb
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    ratios = np.sort(rng.uniform(0.5, 0.9, 12))
+    ex = gb.Executor(local)
+    server = gb.Server(ex, memory_budget=args.serve_budget << 20, streams=args.serve_streams,
+                       max_batch=32)
+
+    def even(v):
+        v = int(round(v))
+        return v + (v & 1)
+
+    # Pinned inputs per (size, format) and output slots per request shape.
+    inputs = {}
+    for (w, h) in SERVE_SIZES:
+        g = torch.empty((h, w), dtype=torch.float32, pin_memory=True).numpy()
+        g[...] = np.random.default_rng(w).random((h, w), dtype=np.float32)
+        y = [torch.empty((hh, ww), dtype=torch.int16, pin_memory=True).numpy().view(np.uint16)
+             for hh, ww in ((h, w), (h // 2, w // 2), (h // 2, w // 2))]
+        for k, plane in enumerate(y):
+            plane[...] = np.random.default_rng(w + k).integers(4096, 60000, plane.shape, dtype=np.uint16)
+        inputs[(w, h)] = (g, y)
+    plans = {}
+    outputs = {}
+    conv_l = gb.integer_conversion(16, False, False)
+    conv_c = gb.integer_conversion(16, True, False)
+
+    def plan_pair(sw, sh, ow, oh, kern, f64):
+        key = (sw, sh, ow, oh, kern, f64)
+        if key not in plans:
+            k, taps, b, c = kern
+            plans[key] = (gb.AxisPlan(gb.AxisRequest(sw, ow, float(ow), 0.0, k, taps, b, c, 1.0, "mirror", f64)),
+                          gb.AxisPlan(gb.AxisRequest(sh, oh, float(oh), 0.0, k, taps, b, c, 1.0, "mirror", f64)))
+        return plans[key]
+
+    def make_request(i):
+        w, h = SERVE_SIZES[int(rng.integers(len(SERVE_SIZES)))]
+        ratio = float(ratios[int(rng.integers(len(ratios)))])
+        kern = SERVE_KERNELS[int(rng.integers(len(SERVE_KERNELS)))]
+        f64 = 2 if rng.random() < 0.2 else 0
+        yuv = bool(rng.random() < 0.5)
+        dw, dh = even(w * ratio), even(h * ratio)
+        g, y = inputs[(w, h)]
+        if yuv:
+            shapes = [(w, h, dw, dh, y[0], conv_l), (w // 2, h // 2, dw // 2, dh // 2, y[1], conv_c),
+                      (w // 2, h // 2, dw // 2, dh // 2, y[2], conv_c)]
+        else:
+            shapes = [(w, h, dw, dh, g, None)]
+        planes = []
+        for sw, sh, ow, oh, x, conv in shapes:
+            ph, pv = plan_pair(sw, sh, ow, oh, kern, f64)
+            slot = (ow, oh, x.dtype.str, i % 48)
+            if slot not in outputs:
+                t = torch.empty((oh, ow), dtype=torch.float32 if x.dtype == np.float32 else torch.int16,
+                                pin_memory=True).numpy()
+                outputs[slot] = t if x.dtype == np.float32 else t.view(np.uint16)
+            planes.append((ph, pv, x, outputs[slot], conv))
+        return planes, sum(sw * sh for sw, sh, *_ in shapes)
+
+    results = []
+    for rate in args.rates:
+        # Requests are built (plans planned, output slots pinned) before the
+        # clock starts; arrivals follow exponential gaps at `rate` per second.
+        count = max(8, int(rate * args.serve_seconds))
+        reqs = [make_request(i) for i in range(count)]
+        gaps = rng.exponential(1.0 / rate, count)
+        # Warm the plan cache and the kernels with every distinct plan once.
+        for planes, _ in reqs[:64]:
+            server.wait(server.submit(planes))
+        server.reset_stats()
+        pending = {}
+        t0 = time.perf_counter()
+        due = t0
+        for i, ((planes, pix), gap) in enumerate(zip(reqs, gaps)):
+            due += gap
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
+                time.sleep(min(due - now, 0.0005))
+            slot = i % 48
+            if slot in pending:                       # the output slot is reused
+                server.wait(pending.pop(slot))
+            pending[slot] = server.submit(planes)
+        for t in pending.values():
+            server.wait(t)
+        elapsed = time.perf_counter() - t0
+        st = server.stats()
+        results.append({"offered_rate": rate, "requests": count, "seconds": elapsed,
+                        "achieved_rate": st["completed"] / elapsed,
+                        "mpix_per_s": st["source_pixels"] / elapsed / 1e6,
+                        "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
+                        "latency_mean_ms": st["latency_mean_ms"], "latency_max_ms": st["latency_max_ms"],
+                        "batches": st["batches"], "mean_batch_requests": st["mean_batch_requests"],
+                        "failed": st["failed"], "peak_device_bytes": st["peak_device_bytes"]})
+    cache = ex.stats()
+    server.close()
+    if rank != 0:
+        return
+    head = results[-1]
+    line = {
+        "metric": SERVE_METRIC, "value": head["mpix_per_s"], "unit": "Mpix/s", "n_gpus": world,
+        "steps": len(results), "warmup": 64, "ms_per_step": head["seconds"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": "C4 serving: Poisson arrivals, sources 1280x720..3840x2160, ratios "
+                               "0.5-0.9, bilinear/bicubic/lanczos3/spline36, 80% f32 / 20% f64mode=2, "
+                               "GRAYS f32 or YUV420P16, host frames (pinned)",
+                   "memory_budget_mb": args.serve_budget, "streams": args.serve_streams,
+                   "l2": "inputs larger than L2 per batch; no flush", "parallelism": "replicas"},
+        "latency_p50_ms": head["latency_p50_ms"], "latency_p99_ms": head["latency_p99_ms"],
+        "rates": results,
+        "plan_cache": {k: cache[k] for k in ("plan_cache_hits", "plan_cache_misses",
+                                             "plan_cache_evictions", "plan_cache_bytes")},
+        "e2e": {"value": head["mpix_per_s"], "unit": "Mpix/s",
+                "note": "every request is a host frame: copies are inside the latency"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def workload_config():
     return {"workload": "Delanczos(taps=3) YUV420P16 1920x1080->1440x810, 64 frames, "
                         "f64mode=0, padding=1",
@@ -388,8 +523,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per step (profiling runs use fewer; the benchmark line uses 64)")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
-                    help="c1: Delanczos YUV420P16 frames (default); c3: candidate sweep")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4"],
+                    help="c1: Delanczos YUV420P16 frames (default); c3: candidate sweep; "
+                         "c4: request loop")
+    ap.add_argument("--rates", type=float, nargs="+", default=[200.0, 800.0],
+                    help="c4: offered request rates (per second)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-budget", type=int, default=8192, help="c4: arena MiB")
+    ap.add_argument("--serve-streams", type=int, default=4)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--kernels-only", action="store_true",
                     help="skip the end-to-end and CPU legs (profiling runs)")
@@ -406,8 +547,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.workload == "c3" and args.impl != "reference":
-        run_sweep(args, rank, world)
+    if args.workload in ("c3", "c4") and args.impl != "reference":
+        (run_sweep if args.workload == "c3" else run_serving)(args, rank, world)
         if dist is not None:
             dist.barrier()
             dist.destroy_process_group()

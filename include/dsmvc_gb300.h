@@ -344,6 +344,63 @@ int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *ou
 int dsmvc_gb_sweep_profile(dsmvc_gb_sweep *sweep, void *stream, double *milliseconds);
 void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep);
 
+/* Request loop (continuous batching; no reference counterpart beyond its
+ * synchronous per-frame calls on execution slots,
+ * src/cuda/cuda_executor.cpp:1462-1503).  Requests of one or more 2D planes
+ * (host buffers, any plans, sizes, kernels and precisions) are queued by
+ * dsmvc_gb_server_submit and taken by `streams` worker threads, each forming
+ * one batch of every queued request that fits the device arena of
+ * `memory_budget` bytes (0 = 8 GiB), at most `max_batch` requests: uploads,
+ * one executor batch, downloads.  Requests arriving while batches run join
+ * the next batch as memory frees up, so the batches of the workers overlap
+ * on the device.  Unprepared plans stay in the executor's device plan cache.
+ * A request larger than the arena is refused (DSMVC_GB_LENGTH_ERROR).
+ * dsmvc_gb_server_wait blocks until the request is done, returns its status
+ * (its message through dsmvc_gb_last_error) and releases the ticket; host
+ * buffers must stay valid until then.  A request's output does not depend on
+ * the requests batched with it.  Latencies are measured from submission to
+ * completion. */
+typedef struct dsmvc_gb_server dsmvc_gb_server;
+typedef struct dsmvc_gb_server_options {
+    int64_t memory_budget;
+    int32_t streams;      /* 1..16 */
+    int32_t max_batch;    /* >= 1 */
+} dsmvc_gb_server_options;
+typedef struct dsmvc_gb_serve_plane {
+    const dsmvc_gb_plan *horizontal;
+    const dsmvc_gb_plan *vertical;
+    const void *input;            /* host */
+    int64_t input_stride;         /* samples */
+    void *output;                 /* host */
+    int64_t output_stride;        /* samples */
+    int32_t sample;               /* enum dsmvc_gb_sample */
+    dsmvc_gb_conversion conversion;
+} dsmvc_gb_serve_plane;
+typedef struct dsmvc_gb_server_stats {
+    uint64_t submitted;
+    uint64_t completed;           /* including failed */
+    uint64_t failed;
+    uint64_t batches;
+    double latency_p50_ms;
+    double latency_p99_ms;
+    double latency_mean_ms;
+    double latency_max_ms;
+    int64_t peak_device_bytes;
+    uint64_t source_pixels;       /* of completed requests */
+    double mean_batch_requests;
+} dsmvc_gb_server_stats;
+int dsmvc_gb_server_create(dsmvc_gb_executor *executor, const dsmvc_gb_server_options *options,
+                           dsmvc_gb_server **out);
+int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_serve_plane *planes,
+                           int32_t count, uint64_t *ticket);
+int dsmvc_gb_server_wait(dsmvc_gb_server *server, uint64_t ticket);
+int dsmvc_gb_server_poll(dsmvc_gb_server *server, uint64_t ticket, int32_t *done);
+int dsmvc_gb_server_get_stats(dsmvc_gb_server *server, dsmvc_gb_server_stats *out);
+/* Clears the latency record and counters (not `submitted`). */
+int dsmvc_gb_server_reset_stats(dsmvc_gb_server *server);
+/* Finishes queued and running requests, then releases the server. */
+void dsmvc_gb_server_destroy(dsmvc_gb_server *server);
+
 /* Kernel timing (the reference's NVTX ranges, src/cuda/nvtx.hpp:11-60, are
  * replaced by CUDA events): while enabled, every launch is bracketed by
  * events on its stream; dsmvc_gb_profile_read waits for them and returns one

@@ -27,7 +27,8 @@ CXXFLAGS = ["-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
 NVCCFLAGS = ARCH + ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
                     "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
-HOST_SOURCES = ["planner.cpp", "stream_plan.cpp", "executor.cpp", "sweep.cpp", "capi.cpp"]
+HOST_SOURCES = ["planner.cpp", "stream_plan.cpp", "executor.cpp", "sweep.cpp", "server.cpp",
+                "capi.cpp"]
 CUDA_SOURCES = ["kernels.cu", "stream.cu", "stream_hb1.cu", "stream_hb3.cu", "stream_hb5.cu",
                 "stream_hb7.cu", "tstream_hb1.cu", "tstream_hb3.cu",
                 "tstream_hb5.cu", "tstream_hb7.cu", "noalloc.cu", "score.cu"]

@@ -4,6 +4,7 @@
 
 #include "executor.hpp"
 #include "noalloc.hpp"
+#include "server.hpp"
 #include "sweep.hpp"
 #include "planner.hpp"
 #include "stream.cuh"
@@ -549,5 +550,97 @@ int dsmvc_gb_sweep_profile(dsmvc_gb_sweep *sweep, void *stream, double *millisec
 }
 
 void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep) { delete sweep; }
+
+struct dsmvc_gb_server {
+    std::unique_ptr<dsmvc_gb::Server> server;
+};
+
+int dsmvc_gb_server_create(dsmvc_gb_executor *executor, const dsmvc_gb_server_options *options,
+                           dsmvc_gb_server **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        dsmvc_gb::ServerOptions o;
+        if (options) {
+            if (options->memory_budget < 0) throw std::invalid_argument("negative memory budget");
+            o.memory_budget = static_cast<std::size_t>(options->memory_budget);
+            o.streams = options->streams;
+            o.max_batch = options->max_batch;
+        }
+        auto s = std::make_unique<dsmvc_gb_server>();
+        s->server = std::make_unique<dsmvc_gb::Server>(exec_of(executor), o);
+        *out = s.release();
+    });
+}
+
+int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_serve_plane *planes, int32_t count,
+                           uint64_t *ticket) {
+    return guarded([&] {
+        if (!server || !ticket || count <= 0 || !planes) throw std::invalid_argument("invalid request");
+        std::vector<dsmvc_gb::ServePlane> list(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) {
+            const auto &p = planes[i];
+            if (!p.horizontal || !p.vertical) throw std::invalid_argument("request plane without plans");
+            if (p.sample < DSMVC_GB_FLOAT32 || p.sample > DSMVC_GB_UINT16)
+                throw std::invalid_argument("sample kind is invalid");
+            auto &d = list[static_cast<std::size_t>(i)];
+            d.horizontal = p.horizontal->plan;
+            d.vertical = p.vertical->plan;
+            d.input = p.input;
+            d.input_stride = p.input_stride;
+            d.output = p.output;
+            d.output_stride = p.output_stride;
+            d.sample = static_cast<dsmvc_gb::dev::Sample>(p.sample);
+            d.conversion = p.sample == DSMVC_GB_FLOAT32 ? dsmvc_gb::IntegerConversion{} : to_conversion(&p.conversion);
+        }
+        *ticket = server->server->submit(std::move(list));
+    });
+}
+
+int dsmvc_gb_server_wait(dsmvc_gb_server *server, uint64_t ticket) {
+    int status = DSMVC_GB_OK;
+    std::string message;
+    const int rc = guarded([&] {
+        if (!server) throw std::invalid_argument("server is null");
+        status = server->server->wait(ticket, &message);
+    });
+    if (rc != DSMVC_GB_OK) return rc;
+    g_error = message;
+    return status;
+}
+
+int dsmvc_gb_server_poll(dsmvc_gb_server *server, uint64_t ticket, int32_t *done) {
+    return guarded([&] {
+        if (!server || !done) throw std::invalid_argument("server or output is null");
+        *done = server->server->done(ticket) ? 1 : 0;
+    });
+}
+
+int dsmvc_gb_server_get_stats(dsmvc_gb_server *server, dsmvc_gb_server_stats *out) {
+    return guarded([&] {
+        if (!server || !out) throw std::invalid_argument("server or output is null");
+        const auto s = server->server->stats();
+        out->submitted = s.submitted;
+        out->completed = s.completed;
+        out->failed = s.failed;
+        out->batches = s.batches;
+        out->latency_p50_ms = s.latency_p50_ms;
+        out->latency_p99_ms = s.latency_p99_ms;
+        out->latency_mean_ms = s.latency_mean_ms;
+        out->latency_max_ms = s.latency_max_ms;
+        out->peak_device_bytes = static_cast<int64_t>(s.peak_device_bytes);
+        out->source_pixels = s.source_pixels;
+        out->mean_batch_requests = s.mean_batch_requests;
+    });
+}
+
+int dsmvc_gb_server_reset_stats(dsmvc_gb_server *server) {
+    return guarded([&] {
+        if (!server) throw std::invalid_argument("server is null");
+        server->server->reset_stats();
+    });
+}
+
+void dsmvc_gb_server_destroy(dsmvc_gb_server *server) { delete server; }
 
 } // extern "C"

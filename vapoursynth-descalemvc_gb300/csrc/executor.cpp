@@ -391,7 +391,8 @@ struct Executor::Impl {
     void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                  const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr);
     void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
-    void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks);
+    void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch = nullptr,
+                 std::size_t scratch_capacity = 0);
     void finish(Workspace &ws);
 };
 
@@ -707,9 +708,14 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
     stats.plane_tasks += c.tasks;
 }
 
-void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks) {
+void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch,
+                             std::size_t scratch_capacity) {
     Compiled c;
     compile(tasks, c, [&](std::size_t bytes) {
+        if (scratch) {
+            if (bytes > scratch_capacity) throw std::length_error("batch scratch exceeds the caller's buffer");
+            return scratch;
+        }
         ws.scratch.reserve(bytes);
         return ws.scratch.data();
     });
@@ -959,11 +965,12 @@ void validate_tasks(const std::vector<PlaneTask> &tasks) {
 
 } // namespace
 
-void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize) {
+void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize, void *scratch,
+                         std::size_t scratch_capacity) {
     DeviceGuard guard(impl_->device);
     validate_tasks(tasks);
     Workspace &ws = impl_->stream_space(static_cast<cudaStream_t>(stream));
-    impl_->enqueue(ws, tasks);
+    impl_->enqueue(ws, tasks, static_cast<char *>(scratch), scratch_capacity);
     if (synchronize) impl_->finish(ws);
 }
 

@@ -155,7 +155,10 @@ public:
     // Device-pointer batch: every task is enqueued on `stream` (null: the
     // executor's own).  With `synchronize` the call waits and raises on a
     // Float64 non-finite status; otherwise check_status() does that later.
-    void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize);
+    // With `scratch`, the intermediate planes live in that caller-owned
+    // device buffer of `scratch_capacity` bytes instead of the stream's own.
+    void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize,
+                   void *scratch = nullptr, std::size_t scratch_capacity = 0);
     void check_status(void *stream);
     // Validates, routes and uploads `tasks` once (see PreparedBatch).  With
     // `scratch` the batch's intermediate planes live in that caller-owned

@@ -100,6 +100,25 @@ class SweepInfoC(C.Structure):
                 ("segment_rows", C.c_int32), ("tuned_groups", C.c_int32)]
 
 
+class ServerOptionsC(C.Structure):
+    _fields_ = [("memory_budget", C.c_int64), ("streams", C.c_int32), ("max_batch", C.c_int32)]
+
+
+class ServePlaneC(C.Structure):
+    _fields_ = [("horizontal", C.c_void_p), ("vertical", C.c_void_p),
+                ("input", C.c_void_p), ("input_stride", C.c_int64),
+                ("output", C.c_void_p), ("output_stride", C.c_int64),
+                ("sample", C.c_int32), ("conversion", ConversionC)]
+
+
+class ServerStatsC(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("batches", C.c_uint64), ("latency_p50_ms", C.c_double),
+                ("latency_p99_ms", C.c_double), ("latency_mean_ms", C.c_double),
+                ("latency_max_ms", C.c_double), ("peak_device_bytes", C.c_int64),
+                ("source_pixels", C.c_uint64), ("mean_batch_requests", C.c_double)]
+
+
 class KernelTimeC(C.Structure):
     _fields_ = [("name", C.c_char * 64), ("launches", C.c_uint64),
                 ("milliseconds", C.c_double), ("bytes", C.c_uint64)]
@@ -165,6 +184,15 @@ SIGNATURES = {
     "dsmvc_gb_sweep_get_info": ([C.c_void_p, C.POINTER(SweepInfoC)], C.c_int),
     "dsmvc_gb_sweep_profile": ([C.c_void_p, C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "dsmvc_gb_sweep_destroy": ([C.c_void_p], None),
+    "dsmvc_gb_server_create": ([C.c_void_p, C.POINTER(ServerOptionsC), C.POINTER(C.c_void_p)],
+                               C.c_int),
+    "dsmvc_gb_server_submit": ([C.c_void_p, C.POINTER(ServePlaneC), C.c_int32,
+                               C.POINTER(C.c_uint64)], C.c_int),
+    "dsmvc_gb_server_wait": ([C.c_void_p, C.c_uint64], C.c_int),
+    "dsmvc_gb_server_poll": ([C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)], C.c_int),
+    "dsmvc_gb_server_get_stats": ([C.c_void_p, C.POINTER(ServerStatsC)], C.c_int),
+    "dsmvc_gb_server_reset_stats": ([C.c_void_p], C.c_int),
+    "dsmvc_gb_server_destroy": ([C.c_void_p], None),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -527,6 +555,66 @@ class Sweep:
         if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
             _lib.dsmvc_gb_sweep_destroy(self._h)
             self._h = None
+
+    __del__ = close
+
+
+class Server:
+    """dsmvc_gb_server_*: continuous batching of host-frame requests.
+    A request is a list of planes (h, v, input, output[, conversion]) with
+    2D numpy arrays (rows contiguous); the arrays are kept alive until the
+    request is waited for."""
+
+    def __init__(self, executor: Executor, memory_budget: int = 0, streams: int = 4,
+                 max_batch: int = 32):
+        h = C.c_void_p()
+        opts = ServerOptionsC(int(memory_budget), int(streams), int(max_batch))
+        _check(lib().dsmvc_gb_server_create(executor._h, C.byref(opts), C.byref(h)))
+        self._h = h
+        self._executor = executor
+        self._held = {}
+
+    def submit(self, planes: Sequence[tuple]) -> int:
+        arr = (ServePlaneC * len(planes))()
+        keep = []
+        for i, pl in enumerate(planes):
+            h, v, x, out = pl[:4]
+            conversion = pl[4] if len(pl) > 4 else None
+            assert x.strides[1] == x.itemsize and out.strides[1] == out.itemsize
+            assert x.dtype == out.dtype
+            es = x.itemsize
+            arr[i] = ServePlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
+                                 out.ctypes.data, out.strides[0] // es, SAMPLES[x.dtype],
+                                 _conv(conversion))
+            keep += [h, v, x, out]
+        t = C.c_uint64()
+        _check(lib().dsmvc_gb_server_submit(self._h, arr, len(planes), C.byref(t)))
+        self._held[t.value] = keep
+        return t.value
+
+    def wait(self, ticket: int) -> None:
+        rc = lib().dsmvc_gb_server_wait(self._h, C.c_uint64(ticket))
+        self._held.pop(ticket, None)
+        _check(rc)
+
+    def done(self, ticket: int) -> bool:
+        d = C.c_int32()
+        _check(lib().dsmvc_gb_server_poll(self._h, C.c_uint64(ticket), C.byref(d)))
+        return bool(d.value)
+
+    def stats(self) -> dict:
+        s = ServerStatsC()
+        _check(lib().dsmvc_gb_server_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def reset_stats(self) -> None:
+        _check(lib().dsmvc_gb_server_reset_stats(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
+            _lib.dsmvc_gb_server_destroy(self._h)
+            self._h = None
+            self._held.clear()
 
     __del__ = close
 
