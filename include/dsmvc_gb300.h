@@ -252,6 +252,9 @@ int dsmvc_gb_run_batch(dsmvc_gb_executor *executor,
                        const dsmvc_gb_plane_task *tasks, int32_t count,
                        void *stream, int32_t synchronize);
 int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream);
+/* Waits for `stream` and releases the executor's per-stream resources; call
+ * it before destroying a stream that was passed to dsmvc_gb_run_batch. */
+int dsmvc_gb_stream_release(dsmvc_gb_executor *executor, void *stream);
 
 /* Prepared batch: the task list of dsmvc_gb_run_batch routed, packed and
  * uploaded once (job table, intermediate planes and a status word owned by

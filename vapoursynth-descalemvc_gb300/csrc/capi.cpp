@@ -438,6 +438,10 @@ int dsmvc_gb_stream_check(dsmvc_gb_executor *executor, void *stream) {
     return guarded([&] { exec_of(executor).check_status(stream); });
 }
 
+int dsmvc_gb_stream_release(dsmvc_gb_executor *executor, void *stream) {
+    return guarded([&] { exec_of(executor).release_stream(stream); });
+}
+
 int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal, const dsmvc_gb_plan *vertical,
                                 int32_t sample, const void *input, int64_t input_stride,
                                 void *output, int64_t output_stride,

@@ -203,7 +203,12 @@ struct Workspace {
         cuda_check(cudaMemsetAsync(status, 0, sizeof(std::uint32_t), stream), "clearing status");
     }
     ~Workspace() {
-        if (stream) cudaStreamSynchronize(stream);
+        // A caller's stream may already be destroyed: wait on what this
+        // workspace owns (its own stream, its table copies) and let the
+        // frees below wait for the device.
+        if (owns_stream) cudaStreamSynchronize(stream);
+        for (int k = 0; k < 2; ++k)
+            if (pinned_done[k]) cudaEventSynchronize(pinned_done[k]);
         for (int k = 0; k < 2; ++k) {
             if (pinned[k]) cudaFreeHost(pinned[k]);
             if (pinned_done[k]) cudaEventDestroy(pinned_done[k]);
@@ -1096,6 +1101,19 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
     cuda_check(cudaMallocHost(&b->status_host, sizeof(std::uint32_t)), "allocating status");
     cuda_check(cudaMemset(b->status, 0, sizeof(std::uint32_t)), "clearing status");
     return std::make_unique<PreparedBatch>(std::move(b));
+}
+
+void Executor::release_stream(void *stream) {
+    DeviceGuard guard(impl_->device);
+    std::unique_ptr<Workspace> ws;
+    {
+        std::scoped_lock lock(impl_->mutex);
+        auto it = impl_->stream_spaces.find(static_cast<cudaStream_t>(stream));
+        if (it == impl_->stream_spaces.end()) return;
+        ws = std::move(it->second);
+        impl_->stream_spaces.erase(it);
+    }
+    cuda_check(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "synchronizing");
 }
 
 void Executor::check_status(void *stream) {

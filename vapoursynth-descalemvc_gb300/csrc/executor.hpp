@@ -160,6 +160,9 @@ public:
     void run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool synchronize,
                    void *scratch = nullptr, std::size_t scratch_capacity = 0);
     void check_status(void *stream);
+    // Waits for `stream` and drops the executor's resources for it (call
+    // before destroying a stream used with run_batch).
+    void release_stream(void *stream);
     // Validates, routes and uploads `tasks` once (see PreparedBatch).  With
     // `scratch` the batch's intermediate planes live in that caller-owned
     // device buffer of `scratch_capacity` bytes (batches launched one after

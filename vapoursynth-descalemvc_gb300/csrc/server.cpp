@@ -314,7 +314,13 @@ Server::~Server() {
     }
     impl_->work.notify_all();
     for (auto &t : impl_->workers) t.join();
-    for (auto s : impl_->streams) cudaStreamDestroy(s);
+    for (auto s : impl_->streams) {
+        try {
+            impl_->executor->release_stream(s);
+        } catch (...) {
+        }
+        cudaStreamDestroy(s);
+    }
 }
 
 std::uint64_t Server::submit(std::vector<ServePlane> planes) {

@@ -163,6 +163,7 @@ SIGNATURES = {
     "dsmvc_gb_run_batch": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_void_p,
                             C.c_int32], C.c_int),
     "dsmvc_gb_stream_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_stream_release": ([C.c_void_p, C.c_void_p], C.c_int),
     "dsmvc_gb_batch_create": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32,
                                C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_batch_launch": ([C.c_void_p, C.c_void_p], C.c_int),
@@ -456,6 +457,9 @@ class Executor:
 
     def stream_check(self, stream: int = 0) -> None:
         _check(lib().dsmvc_gb_stream_check(self._h, C.c_void_p(stream or None)))
+
+    def release_stream(self, stream: int) -> None:
+        _check(lib().dsmvc_gb_stream_release(self._h, C.c_void_p(stream or None)))
 
     def profile(self, enable: bool) -> None:
         _check(lib().dsmvc_gb_profile(self._h, 1 if enable else 0))
