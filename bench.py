@@ -414,8 +414,8 @@ def run_serving(args, rank, world):
         key = (sw, sh, ow, oh, kern, f64)
         if key not in plans:
             k, taps, b, c = kern
-            plans[key] = (gb.AxisPlan(gb.AxisRequest(sw, ow, float(ow), 0.0, k, taps, b, c, 1.0, "mirror", f64)),
-                          gb.AxisPlan(gb.AxisRequest(sh, oh, float(oh), 0.0, k, taps, b, c, 1.0, "mirror", f64)))
+            plans[key] = (gb.AxisPlan(gb.AxisRequest(sw, ow, float(ow), 0.0, k, taps, b, c, 1.0, "symmetric", f64)),
+                          gb.AxisPlan(gb.AxisRequest(sh, oh, float(oh), 0.0, k, taps, b, c, 1.0, "symmetric", f64)))
         return plans[key]
 
     def make_request(i):
@@ -503,6 +503,206 @@ def run_serving(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _f64_solution(plan_h, plan_v, x):
+    """Float64 least-squares descale of `x` (rows x cols) with the plans'
+    Float64 weights: (A^T A)^-1 A^T per axis, banded Cholesky solves."""
+    import scipy.sparse as sp
+    from scipy.linalg import solveh_banded
+
+    def axis(p, data):                       # data: vectors x source
+        a = sp.csr_matrix((p.array("transpose_weights_f64"), p.array("transpose_indices"),
+                           p.array("transpose_offsets")), shape=(p.destination_size, p.source_size))
+        g = (a @ a.T).toarray()
+        n, hb = p.destination_size, p.half_bandwidth
+        ab = np.zeros((hb + 1, n))
+        for d in range(hb + 1):
+            ab[hb - d, d:] = np.diagonal(g, d)
+        return solveh_banded(ab, (a @ data.T)).T
+
+    y = axis(plan_h, x.astype(np.float64))
+    return axis(plan_v, y.T).T
+
+
+def run_single_frame(args, rank, world):
+    """C0: one GRAYS float32 frame, Debicubic(b=0, c=0.5) 1920x1080 ->
+    1280x720, padding=3 (symmetric), f64mode=1, on the CPU scalar route (the
+    oracle port, one thread) and on the GPU: host-frame call latency, the
+    device-resident kernels, and the error against the CPU route and a
+    Float64 solve."""
+    import torch
+    import dsmvc_gb300 as gb
+    from dsmvc_gb300 import synthetic
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sw, sh, dw, dh = 1920, 1080, 1280, 720
+    frame = synthetic.gray_frame(sw, sh, dw, dh, seed=args.seed)
+    req = lambda s, d, m: gb.AxisRequest(s, d, float(d), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", m)
+    h, v = gb.AxisPlan(req(sw, dw, 1)), gb.AxisPlan(req(sh, dh, 1))
+    ex = gb.Executor(local)
+    ex.prepare(h)
+    ex.prepare(v)
+    out = np.empty((dh, dw), np.float32)
+    for _ in range(args.warmup):
+        ex.inverse_2d(h, v, frame, out=out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ex.inverse_2d(h, v, frame, out=out)
+    host_ms = (time.perf_counter() - t0) / args.steps * 1e3
+    # Device-resident: the same plane from HBM, kernels only.
+    dx = torch.from_numpy(frame).cuda()
+    dy = torch.empty((dh, dw), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    batch = ex.prepare_batch([gb.PlaneTask(h, v, dx.data_ptr(), sw, dy.data_ptr(), dw, 0, 0, None)])
+    for _ in range(args.warmup):
+        batch.launch(stream.cuda_stream)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(args.steps):
+            batch.launch(stream.cuda_stream)
+        stop.record(stream)
+    stream.synchronize()
+    dev_ms = start.elapsed_time(stop) / args.steps
+    gpu = dy.cpu().numpy()
+    oh = O.Plan(O.make_request(sw, dw, float(dw), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 1))
+    ov = O.Plan(O.make_request(sh, dh, float(dh), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 1))
+    t1 = time.perf_counter()
+    cpu = O.inverse_2d(oh, ov, frame)
+    cpu_ms = (time.perf_counter() - t1) * 1e3
+    f64 = _f64_solution(gb.AxisPlan(req(sw, dw, 2), cached=False), gb.AxisPlan(req(sh, dh, 2), cached=False),
+                        frame)
+    pix = sw * sh
+    hbm, peak_kind = peaks()
+    algo = frame.nbytes + out.nbytes
+    if rank != 0:
+        return
+    line = {
+        "metric": "descale Mpix/s, single frame (Debicubic GRAYS 1920x1080->1280x720)",
+        "value": pix / (dev_ms / 1e3) / 1e6, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "C0: Debicubic(b=0,c=0.5) GRAYS f32 1920x1080->1280x720, padding=3, "
+                               "f64mode=1, single frame", "l2": "single 8.3 MB frame (L2-resident)"},
+        "e2e": {"value": pix / (host_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": host_ms,
+                "h2d_bytes_per_step": frame.nbytes, "d2h_bytes_per_step": out.nbytes},
+        "cpu_baseline": {"value": pix / (cpu_ms / 1e3) / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
+                         "ms_per_frame": cpu_ms, "sample": "one frame, scalar 2D route"},
+        "error": {"max_abs_vs_cpu_scalar": float(np.abs(gpu - cpu).max()),
+                  "mean_abs_vs_cpu_scalar": float(np.abs(gpu - cpu).mean()),
+                  "max_abs_vs_f64": float(np.abs(gpu - f64).max()),
+                  "cpu_scalar_max_abs_vs_f64": float(np.abs(cpu - f64).max())},
+        "roofline": {"bound": "hbm", "achieved": algo / (dev_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": algo / (dev_ms / 1e3) / 1e9 / hbm, "traffic": None, "peak_source": peak_kind},
+    }
+    print(json.dumps(line), flush=True)
+
+
+F64_CASES = {
+    "spline64-blur1.1": ("spline64", 3, 0.0, 0.5),
+    "bicubic(1/3,1/3)-blur1.1": ("bicubic", 3, 1.0 / 3.0, 1.0 / 3.0),
+}
+
+
+def run_float64(args, rank, world):
+    """C2: Despline64 and Debicubic(b=1/3, c=1/3) with blur=1.1, GRAYS
+    float32 3840x2160 -> 2560x1440, 32 frames per step, f64mode=2 (forced
+    Float64) and f64mode=0 (auto), from HBM.  Float64 FLOP/s against the
+    measured FP64 peak; error against the CPU scalar route (float32 ULPs,
+    Float64 route) and a Float64 solve."""
+    import torch
+    import dsmvc_gb300 as gb
+    from dsmvc_gb300 import synthetic
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sw, sh, dw, dh = 3840, 2160, 2560, 1440
+    nframes = args.frames if args.frames != FRAMES else 32
+    base = synthetic.gray_frame(sw, sh, dw, dh, seed=args.seed)
+    rng = np.random.default_rng(args.seed)
+    frames = [torch.from_numpy(base + rng.normal(0, 1e-3, base.shape).astype(np.float32)).cuda()
+              for _ in range(4)]
+    outs = [torch.empty((dh, dw), dtype=torch.float32, device="cuda") for _ in range(nframes)]
+    fp64_peak = gb.measure_fp64_peak(local)
+    hbm, peak_kind = peaks()
+    ex = gb.Executor(local)
+    stream = torch.cuda.Stream()
+    sid = stream.cuda_stream
+    results = {}
+    for name, (k, taps, b, c) in F64_CASES.items():
+        for mode in (2, 0):
+            req = lambda s, d: gb.AxisRequest(s, d, float(d), 0.0, k, taps, b, c, 1.1, "symmetric", mode)
+            h, v = gb.AxisPlan(req(sw, dw), cached=False), gb.AxisPlan(req(sh, dh), cached=False)
+            ex.prepare(h)
+            ex.prepare(v)
+            tasks = [gb.PlaneTask(h, v, frames[i % 4].data_ptr(), sw, outs[i].data_ptr(), dw, 0, 0, None)
+                     for i in range(nframes)]
+            batch = ex.prepare_batch(tasks)
+            for _ in range(args.warmup):
+                batch.launch(sid)
+            torch.cuda.synchronize()
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                start.record(stream)
+                for _ in range(args.steps):
+                    batch.launch(sid)
+                stop.record(stream)
+            stream.synchronize()
+            batch.check(sid)
+            ms = start.elapsed_time(stop) / args.steps
+            f64 = h.requires_float64 or v.requires_float64
+            # Flops per output per axis: 2 per gather entry, 4 per band
+            # element (forward and backward multiply-add), 2 for the scale.
+            flops = 0
+            for p, vectors in ((h, sh), (v, dw)):
+                flops += vectors * (2 * int(p.nonzeros) + p.destination_size * (4 * p.half_bandwidth + 2))
+            flops *= nframes
+            gpu = outs[0].cpu().numpy()
+            x0 = frames[0].cpu().numpy()
+            oh = O.Plan(O.make_request(sw, dw, float(dw), 0.0, k, taps, b, c, 1.1, "symmetric", mode))
+            ov = O.Plan(O.make_request(sh, dh, float(dh), 0.0, k, taps, b, c, 1.1, "symmetric", mode))
+            cpu = O.inverse_2d(oh, ov, x0)
+            ref = _f64_solution(gb.AxisPlan(req(sw, dw), cached=False) if mode == 2 else
+                                gb.AxisPlan(gb.AxisRequest(sw, dw, float(dw), 0.0, k, taps, b, c, 1.1,
+                                                           "symmetric", 2), cached=False),
+                                gb.AxisPlan(req(sh, dh), cached=False) if mode == 2 else
+                                gb.AxisPlan(gb.AxisRequest(sh, dh, float(dh), 0.0, k, taps, b, c, 1.1,
+                                                           "symmetric", 2), cached=False), x0)
+            sys.path.insert(0, os.path.join(REPO, "tests"))
+            from common import max_ulp
+            algo = nframes * (sw * sh + dw * dh) * 4
+            results[f"{name}/f64mode={mode}"] = {
+                "route": "float64" if f64 else "float32", "ms_per_step": ms,
+                "mpix_per_s": nframes * sw * sh / (ms / 1e3) / 1e6,
+                "gflops": flops / (ms / 1e3) / 1e9,
+                "fp64_frac": (flops / (ms / 1e3) / 1e12 / fp64_peak) if f64 else None,
+                "hbm_frac": algo / (ms / 1e3) / 1e9 / hbm,
+                "rcond": [h.normal_rcond, v.normal_rcond], "half_bandwidth": [h.half_bandwidth, v.half_bandwidth],
+                "max_ulp_vs_cpu_scalar": max_ulp(gpu, cpu),
+                "max_abs_vs_cpu_scalar": float(np.abs(gpu - cpu).max()),
+                "max_abs_vs_f64": float(np.abs(gpu - ref).max()),
+            }
+    if rank != 0:
+        return
+    head = results["spline64-blur1.1/f64mode=2"]
+    line = {
+        "metric": "descale Mpix/s, Float64 route (Despline64 blur 1.1, GRAYS 3840x2160->2560x1440)",
+        "value": head["mpix_per_s"], "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"C2: GRAYS f32 3840x2160->2560x1440, {nframes} frames, blur 1.1, "
+                               "f64mode 2 and 0", "frames_per_step": nframes,
+                   "l2": "inputs (1.06 GB) larger than L2; no flush"},
+        "fp64_peak_tflops": fp64_peak, "cases": results,
+        "roofline": {"bound": "fp64", "achieved": head["gflops"] / 1e3, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": head["fp64_frac"], "traffic": None,
+                     "peak_source": "measured (dsmvc_gb_measure_fp64_peak)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def workload_config():
     return {"workload": "Delanczos(taps=3) YUV420P16 1920x1080->1440x810, 64 frames, "
                         "f64mode=0, padding=1",
@@ -523,9 +723,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--frames", type=int, default=FRAMES,
                     help="frames per step (profiling runs use fewer; the benchmark line uses 64)")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4"],
-                    help="c1: Delanczos YUV420P16 frames (default); c3: candidate sweep; "
-                         "c4: request loop")
+    ap.add_argument("--workload", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
+                    help="c1: Delanczos YUV420P16 frames (default); c0: one Debicubic GRAYS frame; "
+                         "c2: Float64 route at 4K; c3: candidate sweep; c4: request loop")
     ap.add_argument("--rates", type=float, nargs="+", default=[200.0, 800.0],
                     help="c4: offered request rates (per second)")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
@@ -547,8 +747,9 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    if args.workload in ("c3", "c4") and args.impl != "reference":
-        (run_sweep if args.workload == "c3" else run_serving)(args, rank, world)
+    if args.workload != "c1" and args.impl != "reference":
+        {"c0": run_single_frame, "c2": run_float64, "c3": run_sweep,
+         "c4": run_serving}[args.workload](args, rank, world)
         if dist is not None:
             dist.barrier()
             dist.destroy_process_group()

@@ -404,6 +404,10 @@ int dsmvc_gb_server_reset_stats(dsmvc_gb_server *server);
 /* Finishes queued and running requests, then releases the server. */
 void dsmvc_gb_server_destroy(dsmvc_gb_server *server);
 
+/* Measured FP64 throughput of `device` in TFLOP/s (two per FMA), the
+ * denominator of the Float64 route's FLOP roofline. */
+int dsmvc_gb_measure_fp64_peak(int32_t device, double *tflops);
+
 /* Kernel timing (the reference's NVTX ranges, src/cuda/nvtx.hpp:11-60, are
  * replaced by CUDA events): while enabled, every launch is bracketed by
  * events on its stream; dsmvc_gb_profile_read waits for them and returns one

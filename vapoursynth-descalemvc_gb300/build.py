@@ -31,7 +31,8 @@ HOST_SOURCES = ["planner.cpp", "stream_plan.cpp", "executor.cpp", "sweep.cpp", "
                 "capi.cpp"]
 CUDA_SOURCES = ["kernels.cu", "stream.cu", "stream_hb1.cu", "stream_hb3.cu", "stream_hb5.cu",
                 "stream_hb7.cu", "tstream_hb1.cu", "tstream_hb3.cu",
-                "tstream_hb5.cu", "tstream_hb7.cu", "noalloc.cu", "score.cu"]
+                "tstream_hb5.cu", "tstream_hb7.cu", "noalloc.cu", "score.cu",
+                "peak.cu"]
 
 
 def cuda_home() -> str:

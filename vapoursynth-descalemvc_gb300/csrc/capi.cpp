@@ -4,6 +4,7 @@
 
 #include "executor.hpp"
 #include "noalloc.hpp"
+#include "peak.hpp"
 #include "server.hpp"
 #include "sweep.hpp"
 #include "planner.hpp"
@@ -457,6 +458,16 @@ int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal, const dsmvc_gb_
         dsmvc_gb::inverse_2d_noalloc(plan_of(horizontal), plan_of(vertical),
                                      static_cast<dsmvc_gb::dev::Sample>(sample), input, input_stride,
                                      output, output_stride, conv, stream);
+    });
+}
+
+int dsmvc_gb_measure_fp64_peak(int32_t device, double *tflops) {
+    return guarded([&] {
+        if (!tflops) throw std::invalid_argument("output is null");
+        const int rc = dsmvc_gb::measure_fp64_peak(device, tflops);
+        if (rc != 0)
+            throw std::runtime_error(std::string("CUDA measuring the FP64 peak: ")
+                                     + cudaGetErrorString(static_cast<cudaError_t>(rc)));
     });
 }
 

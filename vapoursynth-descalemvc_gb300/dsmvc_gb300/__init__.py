@@ -194,6 +194,7 @@ SIGNATURES = {
     "dsmvc_gb_server_get_stats": ([C.c_void_p, C.POINTER(ServerStatsC)], C.c_int),
     "dsmvc_gb_server_reset_stats": ([C.c_void_p], C.c_int),
     "dsmvc_gb_server_destroy": ([C.c_void_p], None),
+    "dsmvc_gb_measure_fp64_peak": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -333,6 +334,13 @@ class AxisPlan:
         if h is not None and h.value and _lib is not None:
             _lib.dsmvc_gb_plan_release(h)
             self._h = None
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 TFLOP/s of the device (dsmvc_gb_measure_fp64_peak)."""
+    t = C.c_double()
+    _check(lib().dsmvc_gb_measure_fp64_peak(int(device), C.byref(t)))
+    return t.value
 
 
 def build_plans(requests: Sequence[AxisRequest], threads: int = 0) -> list:

@@ -54,7 +54,7 @@ def sweep_width(height: int, width_per_height: float = 16.0 / 9.0) -> int:
 
 def native_resolution_candidates(width: int, height: int, heights: Sequence[int],
                                  kernels: Sequence[str] = ("bicubic", "bilinear", "lanczos3"),
-                                 border: str = "mirror", f64_mode: int = 0
+                                 border: str = "symmetric", f64_mode: int = 0
                                  ) -> List[Tuple[str, int, int, AxisRequest, AxisRequest]]:
     """(kernel, w, h, horizontal request, vertical request) per candidate,
     heights outer, kernels inner; default arguments of the plugin's filters
