@@ -38,19 +38,32 @@ def executor(gb):
     ex.close()
 
 
+def _executor_with(gb, name):
+    if not gb.cuda_available():
+        pytest.skip("no CUDA device")
+    old = os.environ.get(name)
+    os.environ[name] = "0"
+    try:
+        return gb.Executor(0)
+    finally:
+        if old is None:
+            del os.environ[name]
+        else:
+            os.environ[name] = old
+
+
 @pytest.fixture(scope="session")
 def seq_executor(gb):
     """An executor pinned to the sequential kernels (DSMVC_GB_STREAM=0)."""
-    if not gb.cuda_available():
-        pytest.skip("no CUDA device")
-    old = os.environ.get("DSMVC_GB_STREAM")
-    os.environ["DSMVC_GB_STREAM"] = "0"
-    try:
-        ex = gb.Executor(0)
-    finally:
-        if old is None:
-            del os.environ["DSMVC_GB_STREAM"]
-        else:
-            os.environ["DSMVC_GB_STREAM"] = old
+    ex = _executor_with(gb, "DSMVC_GB_STREAM")
+    yield ex
+    ex.close()
+
+
+@pytest.fixture(scope="session")
+def unpaired_executor(gb):
+    """An executor whose 2D planes use the unpaired transposing kernels
+    (DSMVC_GB_PAIRED=0)."""
+    ex = _executor_with(gb, "DSMVC_GB_PAIRED")
     yield ex
     ex.close()

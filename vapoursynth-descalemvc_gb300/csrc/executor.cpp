@@ -86,6 +86,8 @@ struct DevicePlan {
     bool stream_u16 = false, stream_u8 = false;
     bool stream_t = false;          // transposing 2D kernels admitted
     dev::StreamPlanView stream_view{};
+    bool stream_p = false;          // paired transposing 2D kernels admitted
+    dev::StreamPlanView stream_view2{};
     std::size_t bytes = 0;
 };
 
@@ -107,6 +109,10 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     if (pack.eligible) {
         parts.push_back({pack.forward.data(), pack.forward.size() * 4});
         parts.push_back({pack.backward.data(), pack.backward.size() * 4});
+        if (pack.paired) {
+            parts.push_back({pack.paired_forward.data(), pack.paired_forward.size() * 4});
+            parts.push_back({pack.paired_backward.data(), pack.paired_backward.size() * 4});
+        }
     }
     std::size_t total = 0;
     std::vector<std::size_t> offsets;
@@ -148,6 +154,15 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         sv.backward_stride = pack.backward_stride;
         sv.forward = reinterpret_cast<const float *>(base + offsets[8]);
         sv.backward = reinterpret_cast<const float *>(base + offsets[9]);
+        if (pack.paired) {
+            dp->stream_p = true;
+            auto &pv = dp->stream_view2;
+            pv = sv;
+            pv.forward_stride = pack.paired_forward_stride;
+            pv.backward_stride = pack.paired_backward_stride;
+            pv.forward = reinterpret_cast<const float *>(base + offsets[10]);
+            pv.backward = reinterpret_cast<const float *>(base + offsets[11]);
+        }
     }
     dp->bytes = total;
     dp->keep = std::move(keep);
@@ -285,6 +300,8 @@ struct Executor::Impl {
     // DSMVC_GB_STREAM=0 keeps every plan on the sequential kernels (the
     // counterpart of the reference's DSMVC_GPU_SOLVE_PARTITION switch).
     bool allow_stream = true;
+    // DSMVC_GB_PAIRED=0 keeps 2D planes on the unpaired transposing kernels.
+    bool allow_paired = true;
     std::vector<Record> records;
 
     // Prepared plans first, then the cache (plans with owners), else a
@@ -430,7 +447,7 @@ bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
 }
 
 std::string kernel_name(const GroupKey &k) {
-    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32"};
+    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -519,13 +536,15 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             vi.bytes = static_cast<std::uint64_t>(h->destination_size) * v->destination_size
                 * sample_bytes(task.sample);
             if (r.h_t) {
+                // Paired kernels (two vectors per lane) where admitted.
+                const bool pair = allow_paired && r.h->stream_p;
                 auto &j = hi.stream;
-                j.plan = r.h->stream_view;
+                j.plan = pair ? r.h->stream_view2 : r.h->stream_view;
                 j.in = task.input; j.in_elem = 1; j.in_vec = task.input_stride;
                 j.out = mid; j.out_elem = pitch; j.out_vec = 1;
                 j.vectors = v->source_size;
                 j.conv = conv;
-                groups[{0, 3, h->half_bandwidth, task.sample, dev::Sample::f32,
+                groups[{0, pair ? 4 : 3, h->half_bandwidth, task.sample, dev::Sample::f32,
                         j.plan.window == 8 ? 1 : 0}].push_back(hi);
             } else {
                 auto &j = hi.axis;
@@ -538,13 +557,14 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 groups[{0, 0, h->half_bandwidth, task.sample, dev::Sample::f32}].push_back(hi);
             }
             if (r.v_t) {
+                const bool pair = allow_paired && r.v->stream_p;
                 auto &j = vi.stream;
-                j.plan = r.v->stream_view;
+                j.plan = pair ? r.v->stream_view2 : r.v->stream_view;
                 j.in = mid; j.in_elem = 1; j.in_vec = pitch;
                 j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
                 j.vectors = h->destination_size;
                 j.conv = conv;
-                groups[{1, 3, v->half_bandwidth, dev::Sample::f32, task.sample,
+                groups[{1, pair ? 4 : 3, v->half_bandwidth, dev::Sample::f32, task.sample,
                         j.plan.window == 8 ? 1 : 0}].push_back(vi);
             } else {
                 auto &j = vi.axis;
@@ -641,7 +661,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     launches.clear();
     for (auto &[key, items] : groups) {
         const bool is_stream = key.kind >= 2;
-        int per_block = key.kind == 2 ? stream_block : key.kind == 3 ? kTStreamThreads : kSeqThreads;
+        int per_block = key.kind == 2 ? stream_block : key.kind >= 3 ? kTStreamThreads : kSeqThreads;
         if (tuning && key.kind != 2) {
             const GroupTuple g{key.pass, key.kind, key.hb, static_cast<int>(key.in), static_cast<int>(key.out),
                                key.variant};
@@ -656,7 +676,9 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             const int vectors = is_stream ? it.stream.vectors : it.axis.vectors;
             if (vectors <= 0) continue;
             if (is_stream) it.stream.first_block = blocks; else it.axis.first_block = blocks;
-            blocks += (vectors + per_block - 1) / per_block;
+            // Paired kernels give every thread two vectors.
+            const int vectors_per_block = key.kind == 4 ? 2 * per_block : per_block;
+            blocks += (vectors + vectors_per_block - 1) / vectors_per_block;
             bytes_moved += it.bytes;
             if (is_stream)
                 record_floats = std::max(record_floats, it.stream.plan.forward_stride + it.stream.plan.backward_stride);
@@ -690,7 +712,10 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         }
         const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.kind == 3) {
+        if (l.kind == 4) {
+            rc = launch_tstream2(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
+                                 l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
+        } else if (l.kind == 3) {
             rc = launch_tstream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
                                 l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats,
                                 stream);
@@ -758,6 +783,8 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     impl_->device = device;
     if (const char *env = std::getenv("DSMVC_GB_STREAM"); env && std::string(env) == "0")
         impl_->allow_stream = false;
+    if (const char *env = std::getenv("DSMVC_GB_PAIRED"); env && std::string(env) == "0")
+        impl_->allow_paired = false;
     if (const char *env = std::getenv("DSMVC_GB_PLAN_CACHE_MB")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);
@@ -1075,7 +1102,7 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
     validate_tasks(tasks);
     for (const auto &[key, threads] : tuning ? *tuning : BatchTuning{}) {
         const int kind = key[1];
-        const int most = kind == 3 ? 256 : 128;
+        const int most = kind >= 3 ? 256 : 128;
         if (kind == 2 || threads < 32 || threads > most || threads % 32)
             throw std::invalid_argument("invalid CTA size in batch tuning");
     }

@@ -38,6 +38,34 @@ int launch_tstream_hb3(const dev::StreamJob *, int, int, int, int, dev::Sample, 
 int launch_tstream_hb5(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
 int launch_tstream_hb7(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
 
+int launch_tstream2_hb1_k0(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb1_k8(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb3_k0(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb3_k8(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb5_k0(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb5_k8(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb7_k0(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream2_hb7_k8(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, void *);
+
+int launch_tstream2(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
+                    int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
+    const bool k8 = window == 8;
+#define DSMVC_PAIRED(H)                                                                                        \
+    case H:                                                                                                    \
+        return k8 ? launch_tstream2_hb##H##_k8(jobs, job_count, total_blocks, threads, in, out, record_floats, \
+                                               stream)                                                         \
+                  : launch_tstream2_hb##H##_k0(jobs, job_count, total_blocks, threads, in, out, record_floats, \
+                                               stream);
+    switch (half_bandwidth) {
+        DSMVC_PAIRED(1)
+        DSMVC_PAIRED(3)
+        DSMVC_PAIRED(5)
+        DSMVC_PAIRED(7)
+    default: return static_cast<int>(cudaErrorInvalidValue);
+    }
+#undef DSMVC_PAIRED
+}
+
 int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
                    int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
     switch (half_bandwidth) {

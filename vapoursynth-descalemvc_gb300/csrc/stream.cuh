@@ -58,6 +58,13 @@ int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, 
                    int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
                    void *stream);
 
+// Paired transposing 2D passes (tstream2_impl.cuh): as launch_tstream with
+// two vectors per thread (a CTA of `threads` covers 2 x threads vectors) and
+// the plans' paired records; windows <= 16.
+int launch_tstream2(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
+                    int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
+                    void *stream);
+
 // `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,
                   int chunk, bool contiguous, dev::Sample in, dev::Sample out, int record_floats,

@@ -149,6 +149,32 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
         }
     }
     out.eligible = true;
+
+    if (out.ring_ok_transposed && window <= 16) {
+        const int pl = round4(2 * hb);
+        out.paired = true;
+        out.paired_forward_stride = 4 + 2 * window + pl;
+        out.paired_backward_stride = std::max(4, pl);
+        out.paired_forward.assign(padded * static_cast<std::size_t>(out.paired_forward_stride), 0.0F);
+        out.paired_backward.assign(padded * static_cast<std::size_t>(out.paired_backward_stride), 0.0F);
+        for (std::size_t j = 0; j < padded; ++j) {
+            const float *f = out.forward.data() + j * static_cast<std::size_t>(out.forward_stride);
+            float *g = out.paired_forward.data() + j * static_cast<std::size_t>(out.paired_forward_stride);
+            g[0] = f[0];                                   // window start bits
+            g[1] = f[1];                                   // inverse diagonal, twice
+            g[2] = f[1];
+            for (int k = 0; k < window + hb; ++k) {        // weights, then -lower
+                g[4 + 2 * k] = f[4 + k];
+                g[4 + 2 * k + 1] = f[4 + k];
+            }
+            const float *b = out.backward.data() + j * static_cast<std::size_t>(out.backward_stride);
+            float *h = out.paired_backward.data() + j * static_cast<std::size_t>(out.paired_backward_stride);
+            for (int q = 0; q < hb; ++q) {
+                h[2 * q] = -b[q];
+                h[2 * q + 1] = -b[q];
+            }
+        }
+    }
     return out;
 }
 

@@ -28,6 +28,14 @@ struct StreamPack {
     // records past the end).
     std::vector<float> forward;     // * forward_stride
     std::vector<float> backward;    // * backward_stride
+    // Records of the paired 2D kernels (tstream2_impl.cuh), when the window
+    // is at most 16 and the transposing feed fits: every coefficient twice,
+    // backward factors negated.
+    bool paired = false;
+    int paired_forward_stride = 0;  // 4 + 2 window + round4(2 hb)
+    int paired_backward_stride = 0; // round4(2 hb)
+    std::vector<float> paired_forward;
+    std::vector<float> paired_backward;
 };
 
 // `chunk` destinations per register chunk, `ring` source samples held per

@@ -298,7 +298,7 @@ struct Sweep::Impl {
         for (const int threads : {32, 64, 128, 256}) {
             BatchTuning all;
             for (const auto &g : keys) {
-                const int most = g.kind == 3 ? 256 : 128;
+                const int most = g.kind >= 3 ? 256 : 128;
                 if (g.kind != 2 && threads <= most) all[g.key] = threads;
             }
             if (all.empty()) continue;
