@@ -672,13 +672,32 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         std::uint64_t bytes_moved = 0;
         const std::size_t offset = align_up(table.size());
         table.resize(offset);
+        // Transposing kernels are assigned warps, not CTAs: a CTA's warps
+        // may serve consecutive jobs of one plan (they share the CTA's record
+        // copies), so only plan changes round up to a whole CTA.
+        const bool by_warp = key.kind >= 3;
+        const int warps_per_cta = per_block / 32;
+        const int vectors_per_warp = key.kind == 4 ? 64 : 32;
+        if (by_warp)
+            std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) {
+                return a.stream.plan.forward < b.stream.plan.forward;
+            });
+        int warps = 0;
+        const float *run_plan = nullptr;
         for (auto &it : items) {
             const int vectors = is_stream ? it.stream.vectors : it.axis.vectors;
             if (vectors <= 0) continue;
-            if (is_stream) it.stream.first_block = blocks; else it.axis.first_block = blocks;
-            // Paired kernels give every thread two vectors.
-            const int vectors_per_block = key.kind == 4 ? 2 * per_block : per_block;
-            blocks += (vectors + vectors_per_block - 1) / vectors_per_block;
+            if (by_warp) {
+                if (warps && it.stream.plan.forward != run_plan)
+                    warps = (warps + warps_per_cta - 1) / warps_per_cta * warps_per_cta;
+                run_plan = it.stream.plan.forward;
+                it.stream.first_block = warps;     // first warp of the job
+                warps += (vectors + vectors_per_warp - 1) / vectors_per_warp;
+                blocks = (warps + warps_per_cta - 1) / warps_per_cta;
+            } else {
+                if (is_stream) it.stream.first_block = blocks; else it.axis.first_block = blocks;
+                blocks += (vectors + per_block - 1) / per_block;
+            }
             bytes_moved += it.bytes;
             if (is_stream)
                 record_floats = std::max(record_floats, it.stream.plan.forward_stride + it.stream.plan.backward_stride);

@@ -35,7 +35,7 @@ struct StreamJob {
     void *out;
     std::int64_t out_elem, out_vec;
     std::int32_t vectors;
-    std::int32_t first_block;
+    std::int32_t first_block;       // transposing kernels: the job's first warp
     Conversion conv;
 };
 

@@ -315,29 +315,31 @@ template <int HB, int K, class In, class Out>
 __global__ void __launch_bounds__(kPMaxThreads)
 tstream2_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats) {
     extern __shared__ __align__(16) float smem[];
-    const int jidx = find_pjob(jobs, job_count, static_cast<int>(blockIdx.x));
-    const StreamJob &job = jobs[jidx];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthreads = static_cast<int>(blockDim.x), nwarps = nthreads >> 5;
-    const dev::StreamPlanView p = job.plan;
+    // Jobs are assigned warps; a CTA's warps share one plan (the host rounds
+    // plan changes up to whole CTAs), whose records the CTA copies once.
+    const int cta_warp = static_cast<int>(blockIdx.x) * nwarps;
+    const StreamJob &job = jobs[find_pjob(jobs, job_count, cta_warp + warp)];
+    const dev::StreamPlanView p = jobs[find_pjob(jobs, job_count, cta_warp)].plan;
     const int n = p.destination_size;
     const int per_buffer = kPChunk * record_floats;
     float *bufs = smem;
     float *ring = smem + 3 * per_buffer + warp * kPRingFloats;
     float2 *ysm = reinterpret_cast<float2 *>(smem + 3 * per_buffer + nwarps * kPRingFloats + warp * kPYFloats);
 
-    // The warp's 64 vectors; a warp past the last vector takes part in the
-    // CTA's record copies and barriers on a clamped vector, storing nothing.
-    const int block_first = (static_cast<int>(blockIdx.x) - job.first_block) * nthreads * 2;
-    int warp_first = block_first + warp * 64;
+    // The warp's 64 vectors; a warp past its job's last vector only takes
+    // part in the CTA's record copies and barriers.
+    int warp_first = (cta_warp + warp - job.first_block) * 64;
     int warp_vectors = job.vectors - warp_first;
+    const bool idle = warp_vectors <= 0;
     if (warp_vectors <= 0) {
         warp_first = job.vectors - 1;
         warp_vectors = 1;
     } else if (warp_vectors > 64) {
         warp_vectors = 64;
     }
-    const int v0 = block_first + warp * 64 + 2 * lane;
+    const int v0 = (cta_warp + warp - job.first_block) * 64 + 2 * lane;
     const bool a0 = v0 < job.vectors, a1 = v0 + 1 < job.vectors;
 
     PairFeeder<In> feed;
@@ -350,7 +352,7 @@ tstream2_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
-    feed.start();
+    if (!idle) feed.start();
 
     Out *out = static_cast<Out *>(job.out) + (a0 ? v0 : 0);
     const bool pair_store = sizeof(Out) == 4 && a0 && a1 && (job.out_elem % 2 == 0)
@@ -372,28 +374,31 @@ tstream2_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
         __syncthreads();
         const float *cur = bufs + (c % 3) * per_buffer;
         const float *prev = bufs + ((c + 2) % 3) * per_buffer;
-        pforward<HB, K>(y, hist, c * kPChunk, p, cur, feed, lane);
         const float *cur_b = cur + kPChunk * pfwd_stride<HB, K>(p);
         const float *prev_b = prev + kPChunk * pfwd_stride<HB, K>(p);
         const bool last = c + 1 == chunks;
-        if (last) {
+        if (!idle) {
+            pforward<HB, K>(y, hist, c * kPChunk, p, cur, feed, lane);
+            if (last) {
 #pragma unroll
-            for (int d = 0; d < HB; ++d) carry[d] = make_float2(0.0f, 0.0f);
-            pbackward<HB, K>(y, nullptr, carry, c * kPChunk, p, cur_b, out, job.out_elem, a0, a1, pair_store,
-                             job.conv, lane);
-            if (c > 0)
-                pbackward<HB, K>(y, ysm, carry, (c - 1) * kPChunk, p, prev_b, out, job.out_elem, a0, a1,
-                                 pair_store, job.conv, lane);
-            break;
+                for (int d = 0; d < HB; ++d) carry[d] = make_float2(0.0f, 0.0f);
+                pbackward<HB, K>(y, nullptr, carry, c * kPChunk, p, cur_b, out, job.out_elem, a0, a1, pair_store,
+                                 job.conv, lane);
+                if (c > 0)
+                    pbackward<HB, K>(y, ysm, carry, (c - 1) * kPChunk, p, prev_b, out, job.out_elem, a0, a1,
+                                     pair_store, job.conv, lane);
+            } else {
+                pwarmup<HB, K>(y, carry, p, cur_b);
+                if (c > 0)
+                    pbackward<HB, K>(y, ysm, carry, (c - 1) * kPChunk, p, prev_b, out, job.out_elem, a0, a1,
+                                     pair_store, job.conv, lane);
+#pragma unroll
+                for (int t = 0; t < kPChunk; ++t) ysm[t * 32 + lane] = y[t];
+#pragma unroll
+                for (int d = 0; d < HB; ++d) hist[d] = y[kPChunk - HB + d];
+            }
         }
-        pwarmup<HB, K>(y, carry, p, cur_b);
-        if (c > 0)
-            pbackward<HB, K>(y, ysm, carry, (c - 1) * kPChunk, p, prev_b, out, job.out_elem, a0, a1, pair_store,
-                             job.conv, lane);
-#pragma unroll
-        for (int t = 0; t < kPChunk; ++t) ysm[t * 32 + lane] = y[t];
-#pragma unroll
-        for (int d = 0; d < HB; ++d) hist[d] = y[kPChunk - HB + d];
+        if (last) break;
         // Every warp is done with chunk c-1's records: fetch chunk c+2.
         __syncthreads();
         if (c + 2 < chunks) pstage(const_cast<float *>(prev), p, c + 2, tid, nthreads);

@@ -294,28 +294,30 @@ __global__ void __launch_bounds__(kTMaxThreads)
 tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats) {
     static_assert(LC == kTChunk, "record chunks and register chunks coincide");
     extern __shared__ __align__(16) float smem[];
-    const int jidx = find_tjob(jobs, job_count, static_cast<int>(blockIdx.x));
-    const StreamJob &job = jobs[jidx];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthreads = static_cast<int>(blockDim.x);
-    const dev::StreamPlanView p = job.plan;
+    // Jobs are assigned warps; a CTA's warps share one plan (the host rounds
+    // plan changes up to whole CTAs), whose records the CTA copies once.
+    const int cta_warp = static_cast<int>(blockIdx.x) * (nthreads >> 5);
+    const StreamJob &job = jobs[find_tjob(jobs, job_count, cta_warp + warp)];
+    const dev::StreamPlanView p = jobs[find_tjob(jobs, job_count, cta_warp)].plan;
     const int n = p.destination_size;
     const int per_buffer = kTChunk * record_floats;
     float *bufs = smem;
     float *ring = smem + 3 * per_buffer + warp * kTRingFloats;
 
-    // The warp's vectors; a warp past the last vector still takes part in
-    // the CTA's record copies and barriers, on a clamped vector.
-    const int block_first = (static_cast<int>(blockIdx.x) - job.first_block) * nthreads;
-    int warp_first = block_first + warp * 32;
+    // The warp's vectors; a warp past its job's last vector only takes part
+    // in the CTA's record copies and barriers.
+    int warp_first = (cta_warp + warp - job.first_block) * 32;
     int warp_vectors = job.vectors - warp_first;
+    const bool idle = warp_vectors <= 0;
     if (warp_vectors <= 0) {
         warp_first = job.vectors - 1;
         warp_vectors = 1;
     } else if (warp_vectors > 32) {
         warp_vectors = 32;
     }
-    const bool active = block_first + warp * 32 + lane < job.vectors;
+    const bool active = (cta_warp + warp - job.first_block) * 32 + lane < job.vectors;
 
     WarpFeeder<In> feed;
     feed.base = static_cast<const In *>(job.in) + warp_first * job.in_vec;
@@ -327,7 +329,7 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
-    feed.start();
+    if (!idle) feed.start();
 
     Out *out = static_cast<Out *>(job.out) + (warp_first + (lane < warp_vectors ? lane : 0));
 
@@ -346,19 +348,21 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
         __syncthreads();
         const float *cur = bufs + (c % 3) * per_buffer;
         const float *prev = bufs + ((c + 2) % 3) * per_buffer;
-        tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
-        const float *cur_b = cur + kTChunk * fwd_stride<HB, K>(p);
         const bool last = c + 1 == chunks;
-        if (last) {
+        if (!idle) {
+            tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
+            const float *cur_b = cur + kTChunk * fwd_stride<HB, K>(p);
+            if (last) {
 #pragma unroll
-            for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
-            tbackward<HB, LC, K, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
-        } else {
-            twarmup<HB, LC, K>(y, carry, p, cur_b);
-        }
-        if (c > 0) {
-            tbackward<HB, LC, K, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * fwd_stride<HB, K>(p), out,
-                                    job.out_elem, active, job.conv);
+                for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
+                tbackward<HB, LC, K, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
+            } else {
+                twarmup<HB, LC, K>(y, carry, p, cur_b);
+            }
+            if (c > 0) {
+                tbackward<HB, LC, K, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * fwd_stride<HB, K>(p), out,
+                                        job.out_elem, active, job.conv);
+            }
         }
         if (last) break;
         // Every warp is done with chunk c-1's records: fetch chunk c+2.
