@@ -38,11 +38,11 @@ def executor(gb):
     ex.close()
 
 
-def _executor_with(gb, name):
+def _executor_with(gb, name, value="0"):
     if not gb.cuda_available():
         pytest.skip("no CUDA device")
     old = os.environ.get(name)
-    os.environ[name] = "0"
+    os.environ[name] = value
     try:
         return gb.Executor(0)
     finally:
@@ -61,9 +61,9 @@ def seq_executor(gb):
 
 
 @pytest.fixture(scope="session")
-def unpaired_executor(gb):
-    """An executor whose 2D planes use the unpaired transposing kernels
-    (DSMVC_GB_PAIRED=0)."""
-    ex = _executor_with(gb, "DSMVC_GB_PAIRED")
+def paired_executor(gb):
+    """An executor whose admitted 2D planes use the paired transposing
+    kernels (DSMVC_GB_PAIRED=1)."""
+    ex = _executor_with(gb, "DSMVC_GB_PAIRED", "1")
     yield ex
     ex.close()

@@ -119,13 +119,13 @@ RANDOM_2D = _random_geometries(28, 99)
 
 
 @pytest.mark.parametrize("hq,vq", RANDOM_2D, ids=[f"g{i}" for i in range(len(RANDOM_2D))])
-def test_2d_random_geometries(gb, executor, unpaired_executor, hq, vq):
+def test_2d_random_geometries(gb, executor, paired_executor, hq, vq):
     h, oh = plans(gb, executor, hq)
     v, ov = plans(gb, executor, vq)
     x = image(v.source_size, h.source_size, 11)
     scalar = O.inverse_2d(oh, ov, x)
     got = executor.inverse_2d(h, v, x)
-    assert np.array_equal(got, unpaired_executor.inverse_2d(h, v, x))
+    assert np.array_equal(got, paired_executor.inverse_2d(h, v, x))
     err = np.abs(got.astype(np.float64) - scalar)
     assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS, (hq, vq, err.max())
     xi = make_input(v.source_size, h.source_size, "u16", 12)
@@ -249,7 +249,7 @@ FULL = [
 
 
 @pytest.mark.parametrize("name,hq,vq,sample", FULL, ids=[c[0] for c in FULL])
-def test_full_size_frames_use_streaming_kernels(gb, executor, unpaired_executor, name, hq, vq, sample):
+def test_full_size_frames_use_streaming_kernels(gb, executor, paired_executor, name, hq, vq, sample):
     """Full-size frames of the benchmark configurations: the paired
     streaming kernels run (profiled kernel names), give the same samples as
     the unpaired ones, and agree with the CPU scalar route within the
@@ -264,14 +264,15 @@ def test_full_size_frames_use_streaming_kernels(gb, executor, unpaired_executor,
     got = executor.inverse_2d(h, v, x, conv)
     names = {k["name"] for k in executor.kernel_times()}
     executor.profile(False)
+    assert any(n.startswith("tstream_f32/rows") for n in names), names
+    assert any(n.startswith("tstream_f32/columns") for n in names), names
+    paired_executor.profile(True)
+    paired = paired_executor.inverse_2d(h, v, x, conv)
+    names = {k["name"] for k in paired_executor.kernel_times()}
+    paired_executor.profile(False)
     assert any(n.startswith("tstream2_f32/rows") for n in names), names
     assert any(n.startswith("tstream2_f32/columns") for n in names), names
-    unpaired_executor.profile(True)
-    single = unpaired_executor.inverse_2d(h, v, x, conv)
-    names = {k["name"] for k in unpaired_executor.kernel_times()}
-    unpaired_executor.profile(False)
-    assert any(n.startswith("tstream_f32/rows") for n in names), names
-    assert np.array_equal(got, single)
+    assert np.array_equal(got, paired)
     scalar = O.inverse_2d(oh, ov, x, conv)
     if sample == "f32":
         err = np.abs(got.astype(np.float64) - scalar)

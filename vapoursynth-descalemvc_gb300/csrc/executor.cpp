@@ -300,8 +300,13 @@ struct Executor::Impl {
     // DSMVC_GB_STREAM=0 keeps every plan on the sequential kernels (the
     // counterpart of the reference's DSMVC_GPU_SOLVE_PARTITION switch).
     bool allow_stream = true;
-    // DSMVC_GB_PAIRED=0 keeps 2D planes on the unpaired transposing kernels.
-    bool allow_paired = true;
+    // DSMVC_GB_PAIRED=1 runs admitted 2D planes on the paired transposing
+    // kernels (64 vectors per warp); the unpaired ones (32 per warp) are the
+    // default, faster on GB300 at the occupancy the paired ones reach.
+    bool allow_paired = false;
+    // Default CTA size of the transposing kernels (DSMVC_GB_TSTREAM_THREADS,
+    // 32..256 in multiples of 32); batches may tune it per launch group.
+    int tstream_threads = kTStreamThreads;
     std::vector<Record> records;
 
     // Prepared plans first, then the cache (plans with owners), else a
@@ -661,7 +666,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     launches.clear();
     for (auto &[key, items] : groups) {
         const bool is_stream = key.kind >= 2;
-        int per_block = key.kind == 2 ? stream_block : key.kind >= 3 ? kTStreamThreads : kSeqThreads;
+        int per_block = key.kind == 2 ? stream_block : key.kind >= 3 ? tstream_threads : kSeqThreads;
         if (tuning && key.kind != 2) {
             const GroupTuple g{key.pass, key.kind, key.hb, static_cast<int>(key.in), static_cast<int>(key.out),
                                key.variant};
@@ -802,8 +807,13 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     impl_->device = device;
     if (const char *env = std::getenv("DSMVC_GB_STREAM"); env && std::string(env) == "0")
         impl_->allow_stream = false;
-    if (const char *env = std::getenv("DSMVC_GB_PAIRED"); env && std::string(env) == "0")
-        impl_->allow_paired = false;
+    if (const char *env = std::getenv("DSMVC_GB_PAIRED"))
+        impl_->allow_paired = std::string(env) == "1";
+    if (const char *env = std::getenv("DSMVC_GB_TSTREAM_THREADS")) {
+        char *end = nullptr;
+        const long v = std::strtol(env, &end, 10);
+        if (end && *end == '\0' && v >= 32 && v <= 256 && v % 32 == 0) impl_->tstream_threads = static_cast<int>(v);
+    }
     if (const char *env = std::getenv("DSMVC_GB_PLAN_CACHE_MB")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);

@@ -9,7 +9,8 @@ namespace dsmvc_gb::dev {
 
 // Per-destination records, all float-aligned to 16 bytes:
 //   forward[j * forward_stride + ...]:
-//     [0] window start s0 (int bits), [1] inverse diagonal, [2..3] 0,
+//     [0] window start s0 (int bits), [1] inverse diagonal,
+//     [2] (s0 mod 32) * kTRingPitch (int bits), [3] 0,
 //     [4 .. 4+window)  A^T weights of sources s0 .. s0+window-1 (0 where
 //                      the source does not contribute),
 //     [4+window ..)    forward factors -lower_ld for d = HB..1 (0 for d > j),
@@ -47,6 +48,12 @@ int stream_threads();
 bool stream_supports(int half_bandwidth);
 constexpr int kStreamChunk = 32;     // destinations per register chunk
 constexpr int kStreamRing = 32;      // source samples held per thread
+// Ring row pitches (floats) of the transposing kernels, unpaired and paired;
+// the host stores each destination's window offset in the ring, (s0 mod 32)
+// times the pitch (in floats, resp. float2 for the paired kernels), in its
+// forward record.
+constexpr int kTRingPitch = 34;
+constexpr int kPairedRingPitch = 66;
 // `chunk` is 32 or 64; contiguous = the vector's samples are adjacent
 // (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
 // Transposing 2D passes (tstream_impl.cuh): vectors with adjacent samples

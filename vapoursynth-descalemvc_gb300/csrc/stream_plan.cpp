@@ -1,6 +1,8 @@
 // Streaming-kernel packing (see stream_plan.hpp).
 #include "stream_plan.hpp"
 
+#include "stream.cuh"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -127,11 +129,18 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     const auto padded = static_cast<std::size_t>((n + chunk - 1) / chunk) * static_cast<std::size_t>(chunk);
     out.forward.assign(padded * static_cast<std::size_t>(out.forward_stride), 0.0F);
     out.backward.assign(padded * static_cast<std::size_t>(out.backward_stride), 0.0F);
+    // Word 2 of a forward record: the window's offset in the transposing
+    // kernels' ring, (s0 mod 32) * kTRingPitch.
+    auto header = [&](float *f, int start) {
+        const int ring_offset = (start & (kStreamRing - 1)) * kTRingPitch;
+        std::memcpy(&f[0], &start, sizeof(int));
+        std::memcpy(&f[2], &ring_offset, sizeof(int));
+    };
     for (std::size_t j = static_cast<std::size_t>(n); j < padded; ++j)
-        std::memcpy(&out.forward[j * static_cast<std::size_t>(out.forward_stride)], &s0.back(), sizeof(int));
+        header(&out.forward[j * static_cast<std::size_t>(out.forward_stride)], s0.back());
     for (int j = 0; j < n; ++j) {
         float *f = out.forward.data() + static_cast<std::size_t>(j) * out.forward_stride;
-        std::memcpy(&f[0], &s0[j], sizeof(int));
+        header(f, s0[j]);
         f[1] = p.inverse_diagonal[j];
         for (auto k = p.transpose_offsets[j]; k < p.transpose_offsets[j + 1]; ++k)
             f[4 + (p.transpose_indices[k] - s0[j])] = p.transpose_weights[k];
@@ -163,6 +172,10 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
             g[0] = f[0];                                   // window start bits
             g[1] = f[1];                                   // inverse diagonal, twice
             g[2] = f[1];
+            int start = 0;                                 // ring offset in float2 units
+            std::memcpy(&start, &f[0], sizeof(int));
+            const int ring_offset = (start & (kStreamRing - 1)) * (kPairedRingPitch / 2);
+            std::memcpy(&g[3], &ring_offset, sizeof(int));
             for (int k = 0; k < window + hb; ++k) {        // weights, then -lower
                 g[4 + 2 * k] = f[4 + k];
                 g[4 + 2 * k + 1] = f[4 + k];

@@ -1,5 +1,5 @@
-// Host packing of an axis plan for the streaming kernels (stream_impl.cuh)
-// and the checks that admit a plan to them.
+// Host packing of an axis plan for the streaming kernels (stream_impl.cuh,
+// tstream_impl.cuh, tstream2_impl.cuh) and the checks that admit a plan.
 #pragma once
 
 #include "planner.hpp"

@@ -41,7 +41,7 @@ using dev::StreamJob;
 
 constexpr int kPResident = 32;                 // samples resident in a ring
 constexpr int kPRows = 48;                     // 32 rows + the first 16 again
-constexpr int kPPitch = 66;                    // floats between ring rows
+constexpr int kPPitch = kPairedRingPitch;      // floats between ring rows
 constexpr int kPRingFloats = kPRows * kPPitch;
 constexpr int kPChunk = kStreamChunk;
 constexpr int kPYFloats = kPChunk * 64;        // previous chunk, per warp
@@ -198,23 +198,25 @@ __device__ __forceinline__ void pforward(float2 (&y)[kPChunk], const float2 (&hi
         }
         const float *rec = fwd + t * fs;
         const float4 hdr = plds4(rec);
-        const int s0 = __float_as_int(hdr.x);
-        const float2 *win = ring2 + (s0 & (kPResident - 1)) * (kPPitch / 2) + lane;
-        float2 sum = make_float2(0.0f, 0.0f);
+        // Record word 3: the window's ring offset in float2 units.
+        const float2 *win = ring2 + lane + __float_as_int(hdr.w);
+        // Even and odd taps in two partial sums, as the unpaired kernels.
+        float2 se = make_float2(0.0f, 0.0f), so = make_float2(0.0f, 0.0f);
         if constexpr (K > 0) {
 #pragma unroll
             for (int k = 0; k < K; k += 2) {
                 const float4 w = plds4(rec + 4 + 2 * k);
-                sum = __ffma2_rn(lo2(w), win[(k + 0) * (kPPitch / 2)], sum);
-                sum = __ffma2_rn(hi2(w), win[(k + 1) * (kPPitch / 2)], sum);
+                se = __ffma2_rn(lo2(w), win[(k + 0) * (kPPitch / 2)], se);
+                so = __ffma2_rn(hi2(w), win[(k + 1) * (kPPitch / 2)], so);
             }
         } else {
             for (int k = 0; k < kw; k += 2) {
                 const float4 w = plds4(rec + 4 + 2 * k);
-                sum = __ffma2_rn(lo2(w), win[(k + 0) * (kPPitch / 2)], sum);
-                sum = __ffma2_rn(hi2(w), win[(k + 1) * (kPPitch / 2)], sum);
+                se = __ffma2_rn(lo2(w), win[(k + 0) * (kPPitch / 2)], se);
+                so = __ffma2_rn(hi2(w), win[(k + 1) * (kPPitch / 2)], so);
             }
         }
+        float2 sum = __fadd2_rn(se, so);
         const float *low = rec + 4 + 2 * kw;
 #pragma unroll
         for (int q = 0; q < HB; q += 2) {

@@ -40,7 +40,7 @@ using dev::Conversion;
 using dev::StreamJob;
 
 constexpr int kTRing = kStreamRing;        // sample rows per ring
-constexpr int kTPitch = 34;                // floats between ring rows
+constexpr int kTPitch = kTRingPitch;       // floats between ring rows
 constexpr int kTRingFloats = 2 * kTRing * kTPitch;
 constexpr int kTChunk = kStreamChunk;
 constexpr int kTMaxThreads = 256;         // CTA sizes 32..256 (a multiple of 32)
@@ -133,12 +133,19 @@ struct WarpFeeder {
         if (have >= need) return;
         while (have < need) {
             if (pend_ok) {
+                // A block starts on a multiple of 16, so a lane's SPL samples
+                // occupy consecutive ring rows without wrapping.
 #pragma unroll
                 for (int i = 0; i < NI; ++i) {
                     const int v = i * VPI + lane / LPV;
                     const In *vals = reinterpret_cast<const In *>(&pend[i]);
+                    float *r = ring + ((have + (lane % LPV) * SPL) & (kTRing - 1)) * kTPitch + v;
 #pragma unroll
-                    for (int k = 0; k < SPL; ++k) put(have + (lane % LPV) * SPL + k, v, tin(vals[k], conv));
+                    for (int k = 0; k < SPL; ++k) {
+                        const float x = tin(vals[k], conv);
+                        r[k * kTPitch] = x;
+                        r[(kTRing + k) * kTPitch] = x;
+                    }
                 }
                 have += kTBlock;
                 issue();
@@ -183,27 +190,30 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
         }
         const float *rec = fwd + t * fs;
         const float4 hdr = tlds4(rec);
-        const int s0 = __float_as_int(hdr.x);
-        const float *win = feed.ring + (s0 & (kTRing - 1)) * kTPitch + lane;
-        float sum = 0.0f;
+        // Record word 2: the window's ring offset, (s0 mod 32) * kTPitch.
+        const float *win = feed.ring + lane + __float_as_int(hdr.z);
+        // Two interleaved partial sums (even and odd taps) halve the gather's
+        // dependency chain.
+        float se = 0.0f, so = 0.0f;
         if constexpr (K > 0) {
 #pragma unroll
             for (int k = 0; k < K; k += 4) {
                 const float4 w = tlds4(rec + 4 + k);
-                sum = fmaf(w.x, win[(k + 0) * kTPitch], sum);
-                sum = fmaf(w.y, win[(k + 1) * kTPitch], sum);
-                sum = fmaf(w.z, win[(k + 2) * kTPitch], sum);
-                sum = fmaf(w.w, win[(k + 3) * kTPitch], sum);
+                se = fmaf(w.x, win[(k + 0) * kTPitch], se);
+                so = fmaf(w.y, win[(k + 1) * kTPitch], so);
+                se = fmaf(w.z, win[(k + 2) * kTPitch], se);
+                so = fmaf(w.w, win[(k + 3) * kTPitch], so);
             }
         } else {
             for (int k = 0; k < kw; k += 4) {
                 const float4 w = tlds4(rec + 4 + k);
-                sum = fmaf(w.x, win[(k + 0) * kTPitch], sum);
-                sum = fmaf(w.y, win[(k + 1) * kTPitch], sum);
-                sum = fmaf(w.z, win[(k + 2) * kTPitch], sum);
-                sum = fmaf(w.w, win[(k + 3) * kTPitch], sum);
+                se = fmaf(w.x, win[(k + 0) * kTPitch], se);
+                so = fmaf(w.y, win[(k + 1) * kTPitch], so);
+                se = fmaf(w.z, win[(k + 2) * kTPitch], se);
+                so = fmaf(w.w, win[(k + 3) * kTPitch], so);
             }
         }
+        float sum = se + so;
         const float *low = rec + 4 + kw;
 #pragma unroll
         for (int q = 0; q < HB; q += 4) {
