@@ -242,6 +242,28 @@ int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor,
                             uint16_t *output, int64_t output_stride,
                             const dsmvc_gb_conversion *conversion);
 
+/* One host-frame plane (a 2D descale of `input` into `output`, host
+ * buffers, strides in samples); `conversion` is read for integer samples. */
+typedef struct dsmvc_gb_host_plane {
+    const dsmvc_gb_plan *horizontal;
+    const dsmvc_gb_plan *vertical;
+    const void *input;            /* host */
+    int64_t input_stride;         /* samples */
+    void *output;                 /* host */
+    int64_t output_stride;        /* samples */
+    int32_t sample;               /* enum dsmvc_gb_sample */
+    dsmvc_gb_conversion conversion;
+} dsmvc_gb_host_plane;
+/* Synchronous host-frame call over many planes (frames x planes; no
+ * reference counterpart beyond one inverse_2d call per plane): the planes
+ * travel in groups of about DSMVC_GB_PIPELINE_MB (default 96) MiB of input
+ * and output through three streams, so the upload of one group, the kernels
+ * of the previous group and the download of the one before overlap.  Each
+ * output equals the per-plane call's.  Host buffers should be pinned for the
+ * copies to overlap.  Float64 non-finite data in any plane fails the call. */
+int dsmvc_gb_inverse_2d_planes(dsmvc_gb_executor *executor,
+                               const dsmvc_gb_host_plane *planes, int32_t count);
+
 /* Device-resident batch (replaces the reference's per-plane exported-frame
  * calls, src/cuda/cuda_executor.hpp:60-76, and its launch layer,
  * src/cuda/cuda_launch.hpp:11-149): every task is enqueued on `stream`
@@ -369,16 +391,6 @@ typedef struct dsmvc_gb_server_options {
     int32_t streams;      /* 1..16 */
     int32_t max_batch;    /* >= 1 */
 } dsmvc_gb_server_options;
-typedef struct dsmvc_gb_serve_plane {
-    const dsmvc_gb_plan *horizontal;
-    const dsmvc_gb_plan *vertical;
-    const void *input;            /* host */
-    int64_t input_stride;         /* samples */
-    void *output;                 /* host */
-    int64_t output_stride;        /* samples */
-    int32_t sample;               /* enum dsmvc_gb_sample */
-    dsmvc_gb_conversion conversion;
-} dsmvc_gb_serve_plane;
 typedef struct dsmvc_gb_server_stats {
     uint64_t submitted;
     uint64_t completed;           /* including failed */
@@ -394,7 +406,7 @@ typedef struct dsmvc_gb_server_stats {
 } dsmvc_gb_server_stats;
 int dsmvc_gb_server_create(dsmvc_gb_executor *executor, const dsmvc_gb_server_options *options,
                            dsmvc_gb_server **out);
-int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_serve_plane *planes,
+int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_host_plane *planes,
                            int32_t count, uint64_t *ticket);
 int dsmvc_gb_server_wait(dsmvc_gb_server *server, uint64_t ticket);
 int dsmvc_gb_server_poll(dsmvc_gb_server *server, uint64_t ticket, int32_t *done);

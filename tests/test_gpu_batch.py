@@ -136,3 +136,41 @@ def test_unprepared_plans_use_the_device_plan_cache(gb):
     assert s2["plan_cache_hits"] == s1["plan_cache_hits"] + 2
     assert s2["plan_cache_bytes"] > 0
     ex.close()
+
+
+def test_pipelined_host_planes_equal_single_calls(gb):
+    """dsmvc_gb_inverse_2d_planes: many host planes pipelined through three
+    streams in groups (1 MiB groups here, so most planes are in different
+    groups) give exactly the per-plane calls' samples."""
+    import os
+    old = os.environ.get("DSMVC_GB_PIPELINE_MB")
+    os.environ["DSMVC_GB_PIPELINE_MB"] = "1"
+    try:
+        ex = gb.Executor(0)
+    finally:
+        if old is None:
+            del os.environ["DSMVC_GB_PIPELINE_MB"]
+        else:
+            os.environ["DSMVC_GB_PIPELINE_MB"] = old
+    geoms = [(CHROMA_H, CHROMA_V, "u16"), (SMALL_H, SMALL_V, "f32"),
+             ((97, 67, 67.0, 0.1, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2),
+              (73, 51, 51.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "reflect101", 2), "f32")]
+    planes, want = [], []
+    for i, (hq, vq, sample) in enumerate(geoms * 4):
+        h = gb.AxisPlan(product_request(gb, hq), cached=False)
+        v = gb.AxisPlan(product_request(gb, vq), cached=False)
+        x = make_input(v.source_size, h.source_size, sample, 500 + i)
+        conv = gb.integer_conversion(16, True, False) if sample == "u16" else None
+        out = np.zeros((v.destination_size, h.destination_size), x.dtype)
+        planes.append((h, v, x, out, conv))
+        want.append(ex.inverse_2d(h, v, x, conv))
+    ex.inverse_2d_planes(planes)
+    for (_h, _v, _x, out, _c), w in zip(planes, want):
+        assert np.array_equal(out, w)
+    # Non-finite data in a Float64 plane fails the call.
+    h, v, x, out, _ = planes[2]
+    bad = x.copy()
+    bad[1, 1] = np.inf
+    with pytest.raises(gb.DescaleError):
+        ex.inverse_2d_planes(planes[:2] + [(h, v, bad, out)])
+    ex.close()

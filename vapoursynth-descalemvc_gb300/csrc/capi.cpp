@@ -362,6 +362,31 @@ int dsmvc_gb_inverse_2d_u16(dsmvc_gb_executor *executor, const dsmvc_gb_plan *ho
     });
 }
 
+int dsmvc_gb_inverse_2d_planes(dsmvc_gb_executor *executor, const dsmvc_gb_host_plane *planes, int32_t count) {
+    return guarded([&] {
+        if (count < 0 || (count > 0 && !planes)) throw std::invalid_argument("invalid plane list");
+        std::vector<dsmvc_gb::HostPlane> list(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) {
+            const auto &p = planes[i];
+            if (!p.horizontal || !p.vertical) throw std::invalid_argument("plane without plans");
+            if (p.sample < DSMVC_GB_FLOAT32 || p.sample > DSMVC_GB_UINT16)
+                throw std::invalid_argument("sample kind is invalid");
+            auto &d = list[static_cast<std::size_t>(i)];
+            d.horizontal = p.horizontal->plan.get();
+            d.vertical = p.vertical->plan.get();
+            d.horizontal_keep = p.horizontal->plan;
+            d.vertical_keep = p.vertical->plan;
+            d.sample = static_cast<dsmvc_gb::dev::Sample>(p.sample);
+            d.input = p.input;
+            d.input_stride = p.input_stride;
+            d.output = p.output;
+            d.output_stride = p.output_stride;
+            d.conversion = p.sample == DSMVC_GB_FLOAT32 ? dsmvc_gb::IntegerConversion{} : to_conversion(&p.conversion);
+        }
+        exec_of(executor).inverse_2d_planes(list);
+    });
+}
+
 namespace {
 
 std::vector<dsmvc_gb::PlaneTask> task_list(const dsmvc_gb_plane_task *tasks, int32_t count) {
@@ -588,7 +613,7 @@ int dsmvc_gb_server_create(dsmvc_gb_executor *executor, const dsmvc_gb_server_op
     });
 }
 
-int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_serve_plane *planes, int32_t count,
+int dsmvc_gb_server_submit(dsmvc_gb_server *server, const dsmvc_gb_host_plane *planes, int32_t count,
                            uint64_t *ticket) {
     return guarded([&] {
         if (!server || !ticket || count <= 0 || !planes) throw std::invalid_argument("invalid request");

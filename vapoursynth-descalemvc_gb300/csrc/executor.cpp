@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
@@ -277,6 +278,11 @@ struct Executor::Impl {
     std::condition_variable slot_free;
     std::map<cudaStream_t, std::unique_ptr<Workspace>> stream_spaces;
     ExecutorStats stats;
+    // Multi-plane host calls: three workspaces with their own streams, one
+    // such call at a time.
+    std::mutex pipe_mutex;
+    std::array<std::unique_ptr<Workspace>, 3> pipe;
+    std::size_t pipe_group_bytes = 96ULL << 20;
 
     // Optional per-launch CUDA-event timing (dsmvc_gb_profile).
     struct Record {
@@ -809,6 +815,11 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         impl_->allow_stream = false;
     if (const char *env = std::getenv("DSMVC_GB_PAIRED"))
         impl_->allow_paired = std::string(env) == "1";
+    if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
+        char *end = nullptr;
+        const long v = std::strtol(env, &end, 10);
+        if (end && *end == '\0' && v >= 1 && v <= 65536) impl_->pipe_group_bytes = static_cast<std::size_t>(v) << 20;
+    }
     if (const char *env = std::getenv("DSMVC_GB_TSTREAM_THREADS")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);
@@ -950,10 +961,10 @@ void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::pt
     impl_->release_slot(slot);
 }
 
-void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
-                          const void *input, std::ptrdiff_t is, void *output, std::ptrdiff_t os,
-                          const IntegerConversion &conv, const std::shared_ptr<const AxisPlan> &h_keep,
-                          const std::shared_ptr<const AxisPlan> &v_keep) {
+namespace {
+
+void check_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample, const void *input, std::ptrdiff_t is,
+              const void *output, std::ptrdiff_t os, const IntegerConversion &conv) {
     if (!h.valid() || !v.valid() || !input || !output || is < h.source_size
         || os < h.destination_size || sample == dev::Sample::f64)
         throw std::invalid_argument("invalid 2D executor arguments");
@@ -965,6 +976,93 @@ void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample samp
             || conv.output_maximum == 0U || conv.output_maximum > limit)
             throw std::invalid_argument("invalid integer 2D executor arguments");
     }
+}
+
+} // namespace
+
+void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size_t group_bytes) {
+    for (const auto &p : planes) {
+        if (!p.horizontal || !p.vertical) throw std::invalid_argument("host plane without plans");
+        check_2d(*p.horizontal, *p.vertical, p.sample, p.input, p.input_stride, p.output, p.output_stride,
+                 p.conversion);
+    }
+    if (planes.empty()) return;
+    if (group_bytes == 0) group_bytes = impl_->pipe_group_bytes;
+    auto in_row = [](const HostPlane &p) { return static_cast<std::size_t>(p.horizontal->source_size) * sample_bytes(p.sample); };
+    auto out_row = [](const HostPlane &p) { return static_cast<std::size_t>(p.horizontal->destination_size) * sample_bytes(p.sample); };
+    auto plane_bytes = [&](const HostPlane &p) {
+        return align_up(in_row(p) * static_cast<std::size_t>(p.vertical->source_size))
+            + align_up(out_row(p) * static_cast<std::size_t>(p.vertical->destination_size));
+    };
+    // Groups of consecutive planes within the byte target (at least one).
+    std::vector<std::pair<std::size_t, std::size_t>> groups;   // [first, last)
+    std::size_t most = 0;
+    for (std::size_t i = 0; i < planes.size();) {
+        std::size_t j = i, bytes = 0;
+        while (j < planes.size() && (j == i || bytes + plane_bytes(planes[j]) <= group_bytes)) bytes += plane_bytes(planes[j++]);
+        groups.emplace_back(i, j);
+        most = std::max(most, bytes);
+        i = j;
+    }
+    DeviceGuard guard(impl_->device);
+    std::scoped_lock pipe_lock(impl_->pipe_mutex);
+    for (auto &ws : impl_->pipe) {
+        if (!ws) ws = std::make_unique<Workspace>(nullptr);
+        ws->staging.reserve(most);
+    }
+    std::size_t used = 0;
+    try {
+        for (std::size_t g = 0; g < groups.size(); ++g) {
+            Workspace &ws = *impl_->pipe[g % impl_->pipe.size()];
+            used = std::max(used, g % impl_->pipe.size() + 1);
+            char *at = ws.staging.data();
+            std::vector<PlaneTask> tasks;
+            std::vector<char *> outs;
+            for (std::size_t i = groups[g].first; i < groups[g].second; ++i) {
+                const HostPlane &p = planes[i];
+                const std::size_t es = sample_bytes(p.sample);
+                char *din = at;
+                at += align_up(in_row(p) * static_cast<std::size_t>(p.vertical->source_size));
+                char *dout = at;
+                at += align_up(out_row(p) * static_cast<std::size_t>(p.vertical->destination_size));
+                cuda_check(cudaMemcpy2DAsync(din, in_row(p), p.input, p.input_stride * es, in_row(p),
+                                             p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
+                           "uploading plane");
+                PlaneTask t;
+                t.horizontal = p.horizontal;
+                t.vertical = p.vertical;
+                t.horizontal_keep = p.horizontal_keep;
+                t.vertical_keep = p.vertical_keep;
+                t.input = din;
+                t.input_stride = p.horizontal->source_size;
+                t.output = dout;
+                t.output_stride = p.horizontal->destination_size;
+                t.sample = p.sample;
+                t.conversion = p.conversion;
+                tasks.push_back(t);
+                outs.push_back(dout);
+            }
+            impl_->enqueue(ws, tasks);
+            for (std::size_t i = groups[g].first, k = 0; i < groups[g].second; ++i, ++k) {
+                const HostPlane &p = planes[i];
+                const std::size_t es = sample_bytes(p.sample);
+                cuda_check(cudaMemcpy2DAsync(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
+                                             p.vertical->destination_size, cudaMemcpyDeviceToHost, ws.stream),
+                           "downloading plane");
+            }
+        }
+        for (std::size_t k = 0; k < used; ++k) impl_->finish(*impl_->pipe[k]);
+    } catch (...) {
+        for (std::size_t k = 0; k < used; ++k) cudaStreamSynchronize(impl_->pipe[k]->stream);
+        throw;
+    }
+}
+
+void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample sample,
+                          const void *input, std::ptrdiff_t is, void *output, std::ptrdiff_t os,
+                          const IntegerConversion &conv, const std::shared_ptr<const AxisPlan> &h_keep,
+                          const std::shared_ptr<const AxisPlan> &v_keep) {
+    check_2d(h, v, sample, input, is, output, os, conv);
     const std::size_t es = sample_bytes(sample);
     DeviceGuard guard(impl_->device);
     std::size_t slot = 0;

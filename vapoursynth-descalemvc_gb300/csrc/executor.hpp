@@ -52,6 +52,19 @@ struct PlaneTask {
     std::shared_ptr<const AxisPlan> horizontal_keep, vertical_keep;
 };
 
+// One host-frame plane of a multi-plane call (Executor::inverse_2d_planes).
+struct HostPlane {
+    const AxisPlan *horizontal = nullptr;
+    const AxisPlan *vertical = nullptr;
+    std::shared_ptr<const AxisPlan> horizontal_keep, vertical_keep;   // optional owners
+    dev::Sample sample = dev::Sample::f32;
+    const void *input = nullptr;        // host
+    std::ptrdiff_t input_stride = 0;    // samples
+    void *output = nullptr;             // host
+    std::ptrdiff_t output_stride = 0;   // samples
+    IntegerConversion conversion{};
+};
+
 // Per-kernel CUDA-event timing aggregated by kernel name; `bytes` counts the
 // compulsory traffic of the launches (first-pass input, last-pass output).
 struct KernelTime {
@@ -151,6 +164,14 @@ public:
                     std::ptrdiff_t output_stride, const IntegerConversion &conversion,
                     const std::shared_ptr<const AxisPlan> &h_keep = nullptr,
                     const std::shared_ptr<const AxisPlan> &v_keep = nullptr);
+
+    // Synchronous host-frame call over many planes (frames x planes): the
+    // planes go in groups of about `group_bytes` of input and output
+    // (0: DSMVC_GB_PIPELINE_MB, default 96 MiB) through three streams, so the
+    // upload of one group, the kernels of the previous one and the download
+    // of the one before overlap.  Results equal per-plane inverse_2d calls.
+    // Host buffers should be pinned for the copies to overlap.
+    void inverse_2d_planes(const std::vector<HostPlane> &planes, std::size_t group_bytes = 0);
 
     // Device-pointer batch: every task is enqueued on `stream` (null: the
     // executor's own).  With `synchronize` the call waits and raises on a

@@ -104,7 +104,7 @@ class ServerOptionsC(C.Structure):
     _fields_ = [("memory_budget", C.c_int64), ("streams", C.c_int32), ("max_batch", C.c_int32)]
 
 
-class ServePlaneC(C.Structure):
+class HostPlaneC(C.Structure):
     _fields_ = [("horizontal", C.c_void_p), ("vertical", C.c_void_p),
                 ("input", C.c_void_p), ("input_stride", C.c_int64),
                 ("output", C.c_void_p), ("output_stride", C.c_int64),
@@ -160,6 +160,7 @@ SIGNATURES = {
                                 C.c_void_p, C.c_int64, C.POINTER(ConversionC)], C.c_int),
     "dsmvc_gb_inverse_2d_u16": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                  C.c_void_p, C.c_int64, C.POINTER(ConversionC)], C.c_int),
+    "dsmvc_gb_inverse_2d_planes": ([C.c_void_p, C.POINTER(HostPlaneC), C.c_int32], C.c_int),
     "dsmvc_gb_run_batch": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_void_p,
                             C.c_int32], C.c_int),
     "dsmvc_gb_stream_check": ([C.c_void_p, C.c_void_p], C.c_int),
@@ -187,7 +188,7 @@ SIGNATURES = {
     "dsmvc_gb_sweep_destroy": ([C.c_void_p], None),
     "dsmvc_gb_server_create": ([C.c_void_p, C.POINTER(ServerOptionsC), C.POINTER(C.c_void_p)],
                                C.c_int),
-    "dsmvc_gb_server_submit": ([C.c_void_p, C.POINTER(ServePlaneC), C.c_int32,
+    "dsmvc_gb_server_submit": ([C.c_void_p, C.POINTER(HostPlaneC), C.c_int32,
                                C.POINTER(C.c_uint64)], C.c_int),
     "dsmvc_gb_server_wait": ([C.c_void_p, C.c_uint64], C.c_int),
     "dsmvc_gb_server_poll": ([C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)], C.c_int),
@@ -452,6 +453,20 @@ class Executor:
             raise ValueError(f"unsupported sample type {x.dtype}")
         return out
 
+    def inverse_2d_planes(self, planes: Sequence[tuple]) -> None:
+        """dsmvc_gb_inverse_2d_planes: [(h, v, input, output[, conversion])]
+        with 2D numpy arrays (rows contiguous, same dtype in and out); the
+        planes are pipelined through three streams."""
+        arr = (HostPlaneC * len(planes))()
+        for i, pl in enumerate(planes):
+            h, v, x, out = pl[:4]
+            conversion = pl[4] if len(pl) > 4 else None
+            assert x.strides[1] == x.itemsize and out.strides[1] == out.itemsize and x.dtype == out.dtype
+            es = x.itemsize
+            arr[i] = HostPlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
+                                out.ctypes.data, out.strides[0] // es, SAMPLES[x.dtype], _conv(conversion))
+        _check(lib().dsmvc_gb_inverse_2d_planes(self._h, arr, len(planes)))
+
     # -- device-resident batches ------------------------------------------
     def run_batch(self, tasks: Sequence[PlaneTask], stream: int = 0, synchronize: bool = True):
         arr = _task_array(tasks)
@@ -587,7 +602,7 @@ class Server:
         self._held = {}
 
     def submit(self, planes: Sequence[tuple]) -> int:
-        arr = (ServePlaneC * len(planes))()
+        arr = (HostPlaneC * len(planes))()
         keep = []
         for i, pl in enumerate(planes):
             h, v, x, out = pl[:4]
@@ -595,7 +610,7 @@ class Server:
             assert x.strides[1] == x.itemsize and out.strides[1] == out.itemsize
             assert x.dtype == out.dtype
             es = x.itemsize
-            arr[i] = ServePlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
+            arr[i] = HostPlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
                                  out.ctypes.data, out.strides[0] // es, SAMPLES[x.dtype],
                                  _conv(conversion))
             keep += [h, v, x, out]
