@@ -52,6 +52,39 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def link_bandwidth(h2d_bytes, d2h_bytes):
+    """Host<->device copy bandwidth of pinned buffers of the step's sizes:
+    each direction alone and both at once on two streams (the roofline of
+    the end-to-end figure)."""
+    import torch
+    up_h = torch.empty(h2d_bytes, dtype=torch.uint8, pin_memory=True)
+    up_d = torch.empty(h2d_bytes, dtype=torch.uint8, device="cuda")
+    dn_h = torch.empty(d2h_bytes, dtype=torch.uint8, pin_memory=True)
+    dn_d = torch.empty(d2h_bytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def both():
+        with torch.cuda.stream(s1):
+            up_d.copy_(up_h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            dn_h.copy_(dn_d, non_blocking=True)
+
+    t_up = timed(lambda: up_d.copy_(up_h, non_blocking=True))
+    t_dn = timed(lambda: dn_h.copy_(dn_d, non_blocking=True))
+    t_both = timed(both)
+    return {"h2d_gbs": h2d_bytes / t_up / 1e9, "d2h_gbs": d2h_bytes / t_dn / 1e9,
+            "concurrent_gbs": (h2d_bytes + d2h_bytes) / t_both / 1e9}
+
+
 def plane_requests(gb):
     """Luma and chroma (4:2:0, left-aligned chroma placement) requests, as
     prepare_filter_requests builds them (src/vs_plugin.cpp:656-705)."""
@@ -863,6 +896,7 @@ def main():
             for _ in range(args.e2e_steps):
                 list(pool.map(call, calls))
             e2e_calls = world * args.e2e_steps * pix_step / (time.perf_counter() - t0) / 1e6
+    link = link_bandwidth(h2d, d2h) if calls else None
 
     hbm, peak_kind = peaks()
     total_ms = sum(k["milliseconds"] for k in ktimes)
@@ -886,7 +920,10 @@ def main():
         "clocks": clocks.summary(),
         "e2e": {"value": e2e, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "dsmvc_gb_inverse_2d_planes (192 pinned planes)",
-                "per_plane_calls_16_threads": e2e_calls},
+                "per_plane_calls_16_threads": e2e_calls,
+                "link": link,
+                "link_frac": (((h2d + d2h) / (pix_step / (e2e * 1e6)) / 1e9) / link["concurrent_gbs"])
+                if link and e2e else None},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
