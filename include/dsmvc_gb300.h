@@ -363,9 +363,8 @@ int dsmvc_gb_sweep_run_plain(dsmvc_gb_sweep *sweep, void *stream);
 int dsmvc_gb_sweep_scores(dsmvc_gb_sweep *sweep, float *scores, void *stream);
 int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *out);
 /* Runs the sweep once without its graph, timing its stages with CUDA
- * events; `milliseconds[4]` receives the descale passes, the row
- * re-upscale, the column re-upscale with the error sums and the score
- * reduction. */
+ * events; `milliseconds[3]` receives the descale passes, the re-upscale with
+ * the error sums and the score reduction. */
 int dsmvc_gb_sweep_profile(dsmvc_gb_sweep *sweep, void *stream, double *milliseconds);
 void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep);
 

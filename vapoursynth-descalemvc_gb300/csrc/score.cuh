@@ -4,11 +4,12 @@
 //
 // The forward operator of an axis is A (source x destination), the matrix
 // whose transpose the plan stores as a CSR by destination.  Upscaling a
-// descaled plane Y (rows x cols) back to the source size is A_v * Y * A_h^T:
-// a row pass Z = Y * A_h^T (rows x width), then a column pass A_v * Z fused
-// with |. - frame| and a per-CTA partial sum.  Partial sums are reduced in a
-// fixed order, so a score does not depend on launch shapes or on the other
-// candidates of the sweep.
+// descaled plane Y (rows x cols) back to the source size is A_v * Y * A_h^T.
+// One kernel computes, per column tile and segment of source rows, the row
+// pass Z = Y * A_h^T for the descaled rows the segment needs (in shared
+// memory), then A_v * Z, |. - frame| and one partial sum per block of 16
+// rows.  Partial sums are reduced in a fixed order, so a score does not
+// depend on launch shapes or on the other candidates of the sweep.
 #pragma once
 
 #include <cstdint>
@@ -27,17 +28,14 @@ struct ScoreJob {
     const float *descaled;          // rows x cols
     std::int64_t descaled_stride;
     std::int32_t rows, cols;
-    float *upscaled_rows;           // rows x width scratch
-    std::int64_t upscaled_stride;
     const float *frame;             // height x width source plane
     std::int64_t frame_stride;
     std::int32_t width, height;
     ForwardCsr h, v;                // forward operators of the two axes
     float *partials;                // row blocks x column tiles
-    std::int32_t first_block_rows;  // row-pass blocks before this job
-    std::int32_t first_block_cols;  // column-pass blocks before this job
-    std::int32_t segment_rows;      // source rows per column-pass block (a multiple of kScoreRowBlock)
-    std::int32_t column_tiles;      // ceil(width / threads of the column pass)
+    std::int32_t first_block;       // scoring blocks before this job
+    std::int32_t segment_rows;      // source rows per scoring block (a multiple of kScoreRowBlock)
+    std::int32_t column_tiles;      // ceil(width / kScoreThreads)
 };
 
 } // namespace dsmvc_gb::dev
@@ -47,12 +45,11 @@ namespace dsmvc_gb {
 constexpr int kScoreThreads = 256;
 constexpr int kScoreRowBlock = 16;   // rows per partial sum
 
-// Row pass: one block per descaled row; `max_cols` bounds every job's cols
-// (the row is staged in shared memory).
-int launch_upscale_rows(const dev::ScoreJob *jobs, int job_count, int total_blocks, int max_cols,
-                        void *stream);
-// Column pass + absolute error: one block per (column tile, row segment).
-int launch_upscale_columns_l1(const dev::ScoreJob *jobs, int job_count, int total_blocks, void *stream);
+// Fused re-upscale + absolute error: one block per (column tile, row
+// segment); `max_span_rows` bounds the descaled rows any segment touches
+// (their row-pass values are staged in shared memory).
+int launch_score_tiles(const dev::ScoreJob *jobs, int job_count, int total_blocks, int max_span_rows,
+                       void *stream);
 // scores[i] = sum of job i's partials / (width * height), one block per job,
 // in a fixed order.
 int launch_score_finalize(const dev::ScoreJob *jobs, int job_count, float *scores, void *stream);

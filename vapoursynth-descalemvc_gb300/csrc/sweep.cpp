@@ -6,7 +6,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <climits>
+#include <cstdint>
+#include <iterator>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -72,7 +76,8 @@ HostForward forward_csr(const AxisPlan &p) {
 
 } // namespace
 
-constexpr int kSegments[] = {16, 32, 64, 128, 256};   // multiples of kScoreRowBlock
+constexpr int kSegments[] = {16, 32, 64, 128};        // multiples of kScoreRowBlock
+constexpr int kMaxSpanRows = 200;   // staged row-pass rows per scoring block (200 KiB)
 
 struct Sweep::Impl {
     Executor *executor = nullptr;
@@ -88,14 +93,19 @@ struct Sweep::Impl {
         int first = 0, count = 0;
         std::vector<PlaneTask> tasks;
         std::unique_ptr<PreparedBatch> batch;
-        int row_blocks = 0, column_blocks = 0, max_cols = 0;
+        int column_blocks = 0;
+        std::array<int, 4> max_span{};   // per entry of kSegments
     };
     std::vector<Wave> waves;
-    std::vector<std::size_t> y_offset, z_offset, partial_offset;   // within a wave's buffers
-    Buffer forward_mem, y_mem, z_mem, partial_mem, scratch_mem, job_mem, plain_job_mem, score_mem;
+    std::vector<std::size_t> y_offset, partial_offset;   // within a wave's buffers
+    Buffer forward_mem, y_mem, partial_mem, scratch_mem, job_mem, plain_job_mem, score_mem;
+    // Per vertical plan and segment length: the most descaled rows one
+    // segment of source rows touches.
+    std::map<const AxisPlan *, std::array<int, 4>> spans;
     std::size_t scratch_capacity = 0;
     std::map<const AxisPlan *, dev::ForwardCsr> forward;
-    int segment_rows = 64;
+    int segment_rows = 32;
+    int best_segment = 32;
     BatchTuning tuning;
     double tune_ms = 0.0;
     cudaGraph_t graph = nullptr;
@@ -135,6 +145,22 @@ struct Sweep::Impl {
             c.indices = reinterpret_cast<const std::int32_t *>(put(f.indices.data(), f.indices.size() * 4));
             c.weights = reinterpret_cast<const float *>(put(f.weights.data(), f.weights.size() * 4));
             forward[p] = c;
+            std::array<int, 4> sp{};
+            for (std::size_t k = 0; k < sp.size(); ++k) {
+                const int seg = kSegments[k];
+                const int rows = static_cast<int>(f.offsets.size()) - 1;
+                for (int r0 = 0; r0 < rows; r0 += seg) {
+                    int lo = INT32_MAX, hi = -1;
+                    for (int r = r0; r < std::min(rows, r0 + seg); ++r) {
+                        if (f.offsets[r] < f.offsets[r + 1]) {
+                            lo = std::min(lo, f.indices[f.offsets[r]]);
+                            hi = std::max(hi, f.indices[f.offsets[r + 1] - 1]);
+                        }
+                    }
+                    if (hi >= lo) sp[k] = std::max(sp[k], hi - lo + 1);
+                }
+            }
+            spans[p] = sp;
         }
         check(cudaMemcpy(forward_mem.data(), blob.data(), blob.size(), cudaMemcpyHostToDevice),
               "uploading forward operators");
@@ -148,42 +174,38 @@ struct Sweep::Impl {
     void plan_waves() {
         const std::size_t budget = options.memory_budget ? options.memory_budget : (32ULL << 30);
         const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kScoreRowBlock) * 4);
-        std::size_t y_bytes = 0, z_bytes = 0, p_bytes = 0, s_bytes = 0;
-        std::size_t y_max = 0, z_max = 0, p_max = 0, s_max = 0;
+        std::size_t y_bytes = 0, p_bytes = 0, s_bytes = 0;
+        std::size_t y_max = 0, p_max = 0, s_max = 0;
         y_offset.resize(candidates.size());
-        z_offset.resize(candidates.size());
         partial_offset.resize(candidates.size());
         Wave cur;
         for (std::size_t i = 0; i < candidates.size(); ++i) {
             const auto &[h, v] = candidates[i];
             const std::size_t y = align_up(static_cast<std::size_t>(h->destination_size) * v->destination_size * 4);
-            const std::size_t z = align_up(static_cast<std::size_t>(v->destination_size) * width * 4);
             PlaneTask probe;
             probe.horizontal = h;
             probe.vertical = v;
             const std::size_t s = Executor::batch_scratch_bound({probe});
-            if (cur.count > 0 && y_bytes + z_bytes + p_bytes + s_bytes + y + z + partials + s > budget) {
+            if (cur.count > 0 && y_bytes + p_bytes + s_bytes + y + partials + s > budget) {
                 waves.push_back(std::move(cur));
                 cur = Wave{};
-                y_bytes = z_bytes = p_bytes = s_bytes = 0;
+                y_bytes = p_bytes = s_bytes = 0;
             }
             if (cur.count == 0) cur.first = static_cast<int>(i);
             ++cur.count;
             y_offset[i] = y_bytes;
-            z_offset[i] = z_bytes;
             partial_offset[i] = p_bytes;
             y_bytes += y;
-            z_bytes += z;
             p_bytes += partials;
             s_bytes += s;
             y_max = std::max(y_max, y_bytes);
-            z_max = std::max(z_max, z_bytes);
+            const auto &sp = spans.at(v);
+            for (std::size_t k = 0; k < sp.size(); ++k) cur.max_span[k] = std::max(cur.max_span[k], sp[k]);
             p_max = std::max(p_max, p_bytes);
             s_max = std::max(s_max, s_bytes);
         }
         if (cur.count > 0) waves.push_back(std::move(cur));
         y_mem.allocate(y_max);
-        z_mem.allocate(z_max);
         partial_mem.allocate(p_max);
         scratch_mem.allocate(s_max);
         scratch_capacity = s_max;
@@ -210,8 +232,7 @@ struct Sweep::Impl {
     std::vector<dev::ScoreJob> score_jobs(int seg, bool plain) {
         std::vector<dev::ScoreJob> jobs(candidates.size());
         for (auto &w : waves) {
-            int rows = 0, cols = 0;
-            w.max_cols = 0;
+            int cols = 0;
             for (int k = 0; k < w.count; ++k) {
                 const std::size_t i = static_cast<std::size_t>(w.first + k);
                 const AxisPlan *h = candidates[i].first, *v = candidates[i].second;
@@ -220,8 +241,6 @@ struct Sweep::Impl {
                 j.descaled_stride = h->destination_size;
                 j.rows = v->destination_size;
                 j.cols = h->destination_size;
-                j.upscaled_rows = reinterpret_cast<float *>(z_mem.data() + z_offset[i]);
-                j.upscaled_stride = width;
                 j.frame = frame;
                 j.frame_stride = frame_stride;
                 j.width = width;
@@ -231,13 +250,9 @@ struct Sweep::Impl {
                 j.partials = reinterpret_cast<float *>(partial_mem.data() + partial_offset[i]);
                 j.segment_rows = seg;
                 j.column_tiles = column_tiles();
-                j.first_block_rows = plain ? 0 : rows;
-                j.first_block_cols = plain ? 0 : cols;
-                rows += j.rows;
+                j.first_block = plain ? 0 : cols;
                 cols += j.column_tiles * segments(seg);
-                w.max_cols = std::max(w.max_cols, j.cols);
             }
-            w.row_blocks = rows;
             w.column_blocks = cols;
         }
         return jobs;
@@ -257,11 +272,16 @@ struct Sweep::Impl {
         return reinterpret_cast<float *>(score_mem.data()) + w.first;
     }
 
+    [[nodiscard]] int span_rows(const Wave &w) const {
+        for (std::size_t k = 0; k < std::size(kSegments); ++k)
+            if (kSegments[k] == segment_rows) return w.max_span[k];
+        return 0;
+    }
+
     // A wave's scores are reduced before the next wave reuses its buffers
-    // (descaled planes, row-pass planes and partial sums).
+    // (descaled planes and partial sums).
     void enqueue_scoring(const Wave &w, cudaStream_t s) {
-        check(launch_upscale_rows(wave_jobs(w), w.count, w.row_blocks, w.max_cols, s), "launching upscale rows");
-        check(launch_upscale_columns_l1(wave_jobs(w), w.count, w.column_blocks, s), "launching upscale columns");
+        check(launch_score_tiles(wave_jobs(w), w.count, w.column_blocks, span_rows(w), s), "launching scoring");
         check(launch_score_finalize(wave_jobs(w), w.count, wave_scores(w), s), "launching score finalize");
     }
 
@@ -315,16 +335,22 @@ struct Sweep::Impl {
         tuning.clear();
         for (const auto &[k, v] : best) tuning[k] = v.second;
         float best_ms = 0.0F;
-        for (const int seg : kSegments) {
-            upload_jobs(job_mem, score_jobs(seg, false));
+        const int fallback = segment_rows;
+        bool any = false;
+        for (std::size_t k = 0; k < std::size(kSegments); ++k) {
+            if (w.max_span[k] > kMaxSpanRows) continue;
+            upload_jobs(job_mem, score_jobs(kSegments[k], false));
+            segment_rows = kSegments[k];
             const float ms = time_ms([&] {
-                check(launch_upscale_columns_l1(wave_jobs(w), w.count, w.column_blocks, stream), "launching");
+                check(launch_score_tiles(wave_jobs(w), w.count, w.column_blocks, span_rows(w), stream), "launching");
             }, 3);
-            if (seg == kSegments[0] || ms < best_ms) {
+            if (!any || ms < best_ms) {
                 best_ms = ms;
-                segment_rows = seg;
+                any = true;
+                best_segment = kSegments[k];
             }
         }
+        segment_rows = any ? best_segment : fallback;
         tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
 
@@ -334,6 +360,11 @@ struct Sweep::Impl {
         plan_waves();
         score_mem.allocate(candidates.size() * sizeof(float));
         if (options.autotune) autotune();
+        // Every wave's row span at the chosen segment must fit the staging.
+        for (const auto &w : waves) {
+            while (span_rows(w) > kMaxSpanRows && segment_rows > kSegments[0]) segment_rows /= 2;
+            if (span_rows(w) > kMaxSpanRows) throw std::length_error("candidate too far from its source size to score");
+        }
         for (auto &w : waves)
             w.batch = executor->prepare_batch(w.tasks, &tuning, scratch_mem.data(), scratch_capacity);
         upload_jobs(plain_job_mem, score_jobs(segment_rows, true));
@@ -405,11 +436,13 @@ void Sweep::run_plain(void *stream) {
     for (const auto &w : m.waves) {
         for (int k = 0; k < w.count; ++k) {
             const std::size_t i = static_cast<std::size_t>(w.first + k);
-            const AxisPlan *h = m.candidates[i].first, *v = m.candidates[i].second;
+            const AxisPlan *v = m.candidates[i].second;
             m.executor->run_batch({w.tasks[static_cast<std::size_t>(k)]}, stream, false);
             const int col_blocks = m.column_tiles() * m.segments(m.segment_rows);
-            check(launch_upscale_rows(jobs + i, 1, v->destination_size, h->destination_size, s), "launching");
-            check(launch_upscale_columns_l1(jobs + i, 1, col_blocks, s), "launching");
+            int span = 0;
+            for (std::size_t q = 0; q < std::size(kSegments); ++q)
+                if (kSegments[q] == m.segment_rows) span = m.spans.at(v)[q];
+            check(launch_score_tiles(jobs + i, 1, col_blocks, span, s), "launching");
             check(launch_score_finalize(jobs + i, 1, reinterpret_cast<float *>(m.score_mem.data()) + i, s),
                   "launching");
             check(cudaStreamSynchronize(s), "synchronizing");
@@ -417,25 +450,23 @@ void Sweep::run_plain(void *stream) {
     }
 }
 
-std::array<double, 4> Sweep::stage_milliseconds(void *stream) {
+std::array<double, 3> Sweep::stage_milliseconds(void *stream) {
     auto &m = *impl_;
     auto s = static_cast<cudaStream_t>(stream);
-    std::array<cudaEvent_t, 8> ev{};
+    std::array<cudaEvent_t, 4> ev{};
     for (auto &e : ev) check(cudaEventCreate(&e), "creating event");
-    std::array<double, 4> out{};
+    std::array<double, 3> out{};
     try {
         for (const auto &w : m.waves) {
             check(cudaEventRecord(ev[0], s), "recording event");
             w.batch->launch(s);
             check(cudaEventRecord(ev[1], s), "recording event");
-            check(launch_upscale_rows(m.wave_jobs(w), w.count, w.row_blocks, w.max_cols, s), "launching");
+            check(launch_score_tiles(m.wave_jobs(w), w.count, w.column_blocks, m.span_rows(w), s), "launching");
             check(cudaEventRecord(ev[2], s), "recording event");
-            check(launch_upscale_columns_l1(m.wave_jobs(w), w.count, w.column_blocks, s), "launching");
-            check(cudaEventRecord(ev[3], s), "recording event");
             check(launch_score_finalize(m.wave_jobs(w), w.count, m.wave_scores(w), s), "launching");
-            check(cudaEventRecord(ev[4], s), "recording event");
-            check(cudaEventSynchronize(ev[4]), "waiting for event");
-            for (int k = 0; k < 4; ++k) {
+            check(cudaEventRecord(ev[3], s), "recording event");
+            check(cudaEventSynchronize(ev[3]), "waiting for event");
+            for (int k = 0; k < 3; ++k) {
                 float ms = 0.0F;
                 check(cudaEventElapsedTime(&ms, ev[static_cast<std::size_t>(k)], ev[static_cast<std::size_t>(k + 1)]),
                       "reading event");
@@ -464,9 +495,9 @@ SweepInfo Sweep::info() const {
     SweepInfo i;
     i.candidates = static_cast<int>(m.candidates.size());
     i.waves = static_cast<int>(m.waves.size());
-    i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.z_mem.bytes + m.partial_mem.bytes
+    i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.partial_mem.bytes
         + m.scratch_mem.bytes + m.job_mem.bytes + m.plain_job_mem.bytes + m.score_mem.bytes;
-    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 3;
+    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 2;
     i.tune_milliseconds = m.tune_ms;
     i.segment_rows = m.segment_rows;
     i.tuning = m.tuning;

@@ -8,7 +8,8 @@
 // (docs/release-benchmark.md, "getfnative" case).  Here the candidates are
 // packed into waves that fit a device-memory budget; each wave is one
 // prepared batch (every descale of the wave in one launch per pass) plus two
-// scoring launches, and the waves share their buffers.  CTA sizes of every
+// scoring launches (a fused re-upscale and error sum, then the per-candidate
+// reduction), and the waves share their buffers.  CTA sizes of every
 // launch group and the row segment of the scoring pass are chosen by timing
 // the alternatives on the first wave (autotuning).  Scores do not depend on
 // the chosen launch shapes: each candidate's arithmetic is the same whatever
@@ -63,9 +64,9 @@ public:
     // Waits for `stream` and copies the scores (candidate order) to `host`.
     void read_scores(float *host, void *stream);
     // Runs the sweep once without the graph, with CUDA events between its
-    // stages, and returns their milliseconds: descale passes, row
-    // re-upscale, column re-upscale with the error sums, score reduction.
-    [[nodiscard]] std::array<double, 4> stage_milliseconds(void *stream);
+    // stages, and returns their milliseconds: descale passes, re-upscale
+    // with the error sums, score reduction.
+    [[nodiscard]] std::array<double, 3> stage_milliseconds(void *stream);
     [[nodiscard]] const float *device_scores() const;
     [[nodiscard]] SweepInfo info() const;
 

@@ -569,9 +569,9 @@ class Sweep:
 
     def profile(self, stream: int = 0) -> dict:
         """Stage milliseconds of one ungraphed run."""
-        ms = (C.c_double * 4)()
+        ms = (C.c_double * 3)()
         _check(lib().dsmvc_gb_sweep_profile(self._h, C.c_void_p(stream or None), ms))
-        return dict(zip(("descale", "upscale_rows", "upscale_columns_l1", "finalize"), list(ms)))
+        return dict(zip(("descale", "score", "finalize"), list(ms)))
 
     def info(self) -> dict:
         i = SweepInfoC()
