@@ -11,6 +11,7 @@
 // destination column) into the output, with integer conversion fused into
 // the load of the first pass and the store of the second.
 #include "executor.hpp"
+#include "copy.hpp"
 #include "stream.cuh"
 #include "stream_plan.hpp"
 
@@ -901,7 +902,7 @@ void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdi
         ws.staging.reserve(in_bytes + out_bytes);
         char *din = ws.staging.data();
         char *dout = din + in_bytes;
-        cuda_check(cudaMemcpy2DAsync(din, plan.source_size * 4, input, is * 4, plan.source_size * 4,
+        cuda_check(copy_plane(din, plan.source_size * 4, input, is * 4, plan.source_size * 4,
                                      rows, cudaMemcpyHostToDevice, ws.stream), "uploading rows");
         PlaneTask t;
         t.horizontal = &plan;
@@ -912,7 +913,7 @@ void Executor::inverse_rows(const AxisPlan &plan, const float *input, std::ptrdi
         t.output_stride = plan.destination_size;
         t.vectors = rows;
         impl_->enqueue(ws, {t});
-        cuda_check(cudaMemcpy2DAsync(output, os * 4, dout, plan.destination_size * 4,
+        cuda_check(copy_plane(output, os * 4, dout, plan.destination_size * 4,
                                      plan.destination_size * 4, rows, cudaMemcpyDeviceToHost, ws.stream),
                    "downloading rows");
         impl_->finish(ws);
@@ -938,7 +939,7 @@ void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::pt
         ws.staging.reserve(in_bytes + out_bytes);
         char *din = ws.staging.data();
         char *dout = din + in_bytes;
-        cuda_check(cudaMemcpy2DAsync(din, columns * 4, input, is * 4, columns * 4, plan.source_size,
+        cuda_check(copy_plane(din, columns * 4, input, is * 4, columns * 4, plan.source_size,
                                      cudaMemcpyHostToDevice, ws.stream), "uploading columns");
         PlaneTask t;
         t.vertical = &plan;
@@ -949,7 +950,7 @@ void Executor::inverse_columns(const AxisPlan &plan, const float *input, std::pt
         t.output_stride = columns;
         t.vectors = columns;
         impl_->enqueue(ws, {t});
-        cuda_check(cudaMemcpy2DAsync(output, os * 4, dout, columns * 4, columns * 4,
+        cuda_check(copy_plane(output, os * 4, dout, columns * 4, columns * 4,
                                      plan.destination_size, cudaMemcpyDeviceToHost, ws.stream),
                    "downloading columns");
         impl_->finish(ws);
@@ -1025,7 +1026,7 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
                 at += align_up(in_row(p) * static_cast<std::size_t>(p.vertical->source_size));
                 char *dout = at;
                 at += align_up(out_row(p) * static_cast<std::size_t>(p.vertical->destination_size));
-                cuda_check(cudaMemcpy2DAsync(din, in_row(p), p.input, p.input_stride * es, in_row(p),
+                cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
                                              p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
                            "uploading plane");
                 PlaneTask t;
@@ -1046,7 +1047,7 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
             for (std::size_t i = groups[g].first, k = 0; i < groups[g].second; ++i, ++k) {
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
-                cuda_check(cudaMemcpy2DAsync(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
+                cuda_check(copy_plane(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
                                              p.vertical->destination_size, cudaMemcpyDeviceToHost, ws.stream),
                            "downloading plane");
             }
@@ -1075,7 +1076,7 @@ void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample samp
         ws.staging.reserve(in_bytes + out_bytes);
         char *din = ws.staging.data();
         char *dout = din + in_bytes;
-        cuda_check(cudaMemcpy2DAsync(din, in_row, input, is * es, in_row, v.source_size,
+        cuda_check(copy_plane(din, in_row, input, is * es, in_row, v.source_size,
                                      cudaMemcpyHostToDevice, ws.stream), "uploading plane");
         PlaneTask t;
         t.horizontal = &h;
@@ -1089,7 +1090,7 @@ void Executor::inverse_2d(const AxisPlan &h, const AxisPlan &v, dev::Sample samp
         t.sample = sample;
         t.conversion = conv;
         impl_->enqueue(ws, {t});
-        cuda_check(cudaMemcpy2DAsync(output, os * es, dout, out_row, out_row, v.destination_size,
+        cuda_check(copy_plane(output, os * es, dout, out_row, out_row, v.destination_size,
                                      cudaMemcpyDeviceToHost, ws.stream), "downloading plane");
         impl_->finish(ws);
     } catch (...) {

@@ -26,6 +26,8 @@ __global__ void __launch_bounds__(kScoreThreads)
 score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     extern __shared__ float zt[];                  // [rows of the segment's span][kScoreThreads]
     __shared__ float warp_sums[kScoreThreads / 32];
+    __shared__ float seg_w[kScoreSegmentEntries];
+    __shared__ int seg_j[kScoreSegmentEntries];
     __shared__ int span[2];
     const int b = static_cast<int>(blockIdx.x);
     const ScoreJob &job = jobs[find_job(jobs, count, b)];
@@ -50,12 +52,36 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     }
     __syncthreads();
     const int j_lo = span[0], nj = span[1] - span[0] + 1;
+    // The segment's A_v entries (weights and staged-row offsets) in shared
+    // memory when they fit; they are read by every thread.
+    const std::uint32_t v0 = job.v.offsets[r0], v1 = job.v.offsets[r1];
+    const bool staged = v1 - v0 <= kScoreSegmentEntries;
+    if (staged) {
+        for (std::uint32_t e = v0 + tid; e < v1; e += kScoreThreads) {
+            seg_w[e - v0] = job.v.weights[e];
+            seg_j[e - v0] = (job.v.indices[e] - j_lo) * kScoreThreads;
+        }
+    }
     if (s < job.width) {
+        // This column's A_h entries in registers (a tail beyond eight, rare,
+        // reads them again from memory); the order of the sum is ascending.
         const std::uint32_t e0 = job.h.offsets[s], e1 = job.h.offsets[s + 1];
+        const int ne = static_cast<int>(e1 - e0);
+        constexpr int R = 8;
+        float hw[R];
+        int hc[R];
+#pragma unroll
+        for (int e = 0; e < R; ++e) {
+            hw[e] = e < ne ? job.h.weights[e0 + e] : 0.0f;
+            hc[e] = e < ne ? job.h.indices[e0 + e] : 0;
+        }
         for (int jj = 0; jj < nj; ++jj) {
             const float *y = job.descaled + static_cast<std::int64_t>(j_lo + jj) * job.descaled_stride;
             float acc = 0.0f;
-            for (std::uint32_t e = e0; e < e1; ++e) acc = fmaf(job.h.weights[e], y[job.h.indices[e]], acc);
+#pragma unroll
+            for (int e = 0; e < R; ++e)
+                if (e < ne) acc = fmaf(hw[e], y[hc[e]], acc);
+            for (std::uint32_t e = e0 + R; e < e1; ++e) acc = fmaf(job.h.weights[e], y[job.h.indices[e]], acc);
             zt[jj * kScoreThreads + tid] = acc;
         }
     }
@@ -70,8 +96,12 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
             for (int r = ra; r < rz; ++r) {
                 const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
                 float acc = 0.0f;
-                for (std::uint32_t e = e0; e < e1; ++e)
-                    acc = fmaf(job.v.weights[e], zt[(job.v.indices[e] - j_lo) * kScoreThreads + tid], acc);
+                if (staged) {
+                    for (std::uint32_t e = e0 - v0; e < e1 - v0; ++e) acc = fmaf(seg_w[e], zt[seg_j[e] + tid], acc);
+                } else {
+                    for (std::uint32_t e = e0; e < e1; ++e)
+                        acc = fmaf(job.v.weights[e], zt[(job.v.indices[e] - j_lo) * kScoreThreads + tid], acc);
+                }
                 sum += fabsf(acc - f[static_cast<std::int64_t>(r) * job.frame_stride]);
             }
         }

@@ -1,5 +1,6 @@
 // Request loop (server.hpp).
 #include "server.hpp"
+#include "copy.hpp"
 
 #include "../../include/dsmvc_gb300.h"
 
@@ -163,7 +164,7 @@ struct Server::Impl {
                 const auto &pn = pl.req->planes[i];
                 const std::size_t es = sample_bytes(pn.sample);
                 const auto &h = *pn.horizontal, &v = *pn.vertical;
-                check(cudaMemcpy2DAsync(pn.output, pn.output_stride * es, pl.out[i], h.destination_size * es,
+                check(copy_plane(pn.output, pn.output_stride * es, pl.out[i], h.destination_size * es,
                                         h.destination_size * es, v.destination_size, cudaMemcpyDeviceToHost, s),
                       "downloading a request plane");
             }
@@ -180,7 +181,7 @@ struct Server::Impl {
                     p += align_up(static_cast<std::size_t>(h.source_size) * v.source_size * es);
                     char *dout = p;
                     p += align_up(static_cast<std::size_t>(h.destination_size) * v.destination_size * es);
-                    check(cudaMemcpy2DAsync(din, h.source_size * es, pn.input, pn.input_stride * es,
+                    check(copy_plane(din, h.source_size * es, pn.input, pn.input_stride * es,
                                             h.source_size * es, v.source_size, cudaMemcpyHostToDevice, s),
                           "uploading a request plane");
                     PlaneTask t;

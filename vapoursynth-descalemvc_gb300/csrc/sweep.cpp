@@ -77,7 +77,7 @@ HostForward forward_csr(const AxisPlan &p) {
 } // namespace
 
 constexpr int kSegments[] = {16, 32, 64, 128};        // multiples of kScoreRowBlock
-constexpr int kMaxSpanRows = 200;   // staged row-pass rows per scoring block (200 KiB)
+constexpr int kMaxSpanRows = 192;   // staged row-pass rows per scoring block (192 KiB + 16 KiB)
 
 struct Sweep::Impl {
     Executor *executor = nullptr;
