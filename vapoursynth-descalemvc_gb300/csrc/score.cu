@@ -140,8 +140,10 @@ score_finalize_kernel(const ScoreJob *__restrict__ jobs, float *scores) {
 int launch_score_tiles(const dev::ScoreJob *jobs, int count, int blocks, int max_span_rows, void *stream) {
     if (blocks <= 0) return 0;
     const int smem = max_span_rows * kScoreThreads * static_cast<int>(sizeof(float));
+    // The kernel's static shared memory counts against the default 48 KiB
+    // too, so the dynamic limit is raised for any size not configured yet.
     static int configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
+    if (smem > configured) {
         const cudaError_t e = cudaFuncSetAttribute(score_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    smem);
         if (e != cudaSuccess) return static_cast<int>(e);
