@@ -881,13 +881,13 @@ def main():
 
     e2e = e2e_calls = None
     if calls:
-        planes = [(c[0], c[1], c[2], c[4], c[3]) for c in calls]
-        ex.inverse_2d_planes(planes)  # warm-up
+        planes = ex.host_planes([(c[0], c[1], c[2], c[4], c[3]) for c in calls])
+        planes.run()  # warm-up
         if dist is not None:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            ex.inverse_2d_planes(planes)
+            planes.run()
         e2e_s = time.perf_counter() - t0
         e2e = world * args.e2e_steps * pix_step / e2e_s / 1e6
         with cf.ThreadPoolExecutor(max_workers=16) as pool:

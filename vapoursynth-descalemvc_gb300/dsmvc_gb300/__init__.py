@@ -457,15 +457,12 @@ class Executor:
         """dsmvc_gb_inverse_2d_planes: [(h, v, input, output[, conversion])]
         with 2D numpy arrays (rows contiguous, same dtype in and out); the
         planes are pipelined through three streams."""
-        arr = (HostPlaneC * len(planes))()
-        for i, pl in enumerate(planes):
-            h, v, x, out = pl[:4]
-            conversion = pl[4] if len(pl) > 4 else None
-            assert x.strides[1] == x.itemsize and out.strides[1] == out.itemsize and x.dtype == out.dtype
-            es = x.itemsize
-            arr[i] = HostPlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
-                                out.ctypes.data, out.strides[0] // es, SAMPLES[x.dtype], _conv(conversion))
-        _check(lib().dsmvc_gb_inverse_2d_planes(self._h, arr, len(planes)))
+        self.host_planes(planes).run()
+
+    def host_planes(self, planes: Sequence[tuple]) -> "HostPlanes":
+        """The plane descriptors of inverse_2d_planes built once, for
+        callers that run the same buffers repeatedly (a frame ring)."""
+        return HostPlanes(self, planes)
 
     # -- device-resident batches ------------------------------------------
     def run_batch(self, tasks: Sequence[PlaneTask], stream: int = 0, synchronize: bool = True):
@@ -495,6 +492,27 @@ class Executor:
         return [{"name": buf[i].name.decode(), "launches": buf[i].launches,
                  "milliseconds": buf[i].milliseconds, "bytes": buf[i].bytes}
                 for i in range(min(n.value, 64))]
+
+
+class HostPlanes:
+    """A descriptor array for dsmvc_gb_inverse_2d_planes; keeps its plans
+    and arrays alive."""
+
+    def __init__(self, executor: Executor, planes: Sequence[tuple]):
+        arr = (HostPlaneC * len(planes))()
+        keep = []
+        for i, pl in enumerate(planes):
+            h, v, x, out = pl[:4]
+            conversion = pl[4] if len(pl) > 4 else None
+            assert x.strides[1] == x.itemsize and out.strides[1] == out.itemsize and x.dtype == out.dtype
+            es = x.itemsize
+            arr[i] = HostPlaneC(h.handle.value, v.handle.value, x.ctypes.data, x.strides[0] // es,
+                                out.ctypes.data, out.strides[0] // es, SAMPLES[x.dtype], _conv(conversion))
+            keep += [h, v, x, out]
+        self._arr, self._keep, self._executor, self.count = arr, keep, executor, len(planes)
+
+    def run(self) -> None:
+        _check(lib().dsmvc_gb_inverse_2d_planes(self._executor._h, self._arr, self.count))
 
 
 def _task_array(tasks: Sequence[PlaneTask]):
