@@ -560,6 +560,7 @@ std::size_t AxisPlan::storage_bytes() const noexcept {
 }
 
 bool AxisPlan::valid() const noexcept {
+    if (validated) return true;
     if (source_size <= 0 || destination_size <= 0 || support <= 0 || half_bandwidth < 0
         || half_bandwidth >= destination_size || !(active_length > 0.0)
         || !std::isfinite(active_length) || !std::isfinite(shift) || !std::isfinite(normal_rcond)
@@ -655,6 +656,7 @@ AxisPlan build_axis_plan(const AxisRequest &request, const CustomKernel &custom)
         }
     }
     if (!p.valid()) throw std::runtime_error("failed to build inverse axis plan");
+    p.validated = true;
     return p;
 }
 

@@ -77,6 +77,10 @@ struct AxisPlan {
 
     // Largest number of A^T entries in one destination row.
     std::int32_t max_row_entries = 0;
+    // Set by build_axis_plan once the full check has passed: plans are
+    // immutable afterwards, so valid() answers at once (executor calls check
+    // every plan they are given).
+    bool validated = false;
 
     [[nodiscard]] bool requires_float64() const noexcept {
         return !ldlt_bands_f64.empty();
