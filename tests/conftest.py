@@ -61,6 +61,15 @@ def seq_executor(gb):
 
 
 @pytest.fixture(scope="session")
+def exact_executor(gb):
+    """An executor whose admitted 2D planes use the two-pass transposing
+    kernels (DSMVC_GB_EXACT=1)."""
+    ex = _executor_with(gb, "DSMVC_GB_EXACT", "1")
+    yield ex
+    ex.close()
+
+
+@pytest.fixture(scope="session")
 def paired_executor(gb):
     """An executor whose admitted 2D planes use the paired transposing
     kernels (DSMVC_GB_PAIRED=1)."""

@@ -351,3 +351,53 @@ def test_device_batch_matches_host_calls(gb, executor):
         if sample == "u16":
             got = got.view(np.uint16)
         assert np.array_equal(got, want)
+
+
+WIDE_2D = [
+    ("spline64-blur-hb9", (384, 256, 256.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0),
+     (216, 144, 144.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0)),
+    ("lanczos4-blur-hb9", (300, 197, 197.0, 0.1, "lanczos", 4, 0, 0.5, 1.1, "mirror", 0),
+     (170, 121, 121.0, 0.0, "lanczos", 4, 0, 0.5, 1.1, "mirror", 0)),
+    ("lanczos6-hb11", (240, 200, 200.0, 0.0, "lanczos", 6, 0, 0.5, 1.0, "symmetric", 0),
+     (135, 112, 112.0, 0.0, "lanczos", 6, 0, 0.5, 1.0, "symmetric", 0)),
+]
+
+
+@pytest.mark.parametrize("name,hq,vq", CASES_2D + WIDE_2D, ids=[c[0] for c in CASES_2D + WIDE_2D])
+def test_two_pass_kernels_are_bit_exact(gb, exact_executor, name, hq, vq):
+    """The two-pass transposing kernels run the reference CUDA operation
+    order without approximation: Float32 output equals the oracle's CUDA
+    order bit for bit, integer output too; the kernels run (profiled names)
+    whenever the plans are not Float64."""
+    h, oh = plans(gb, exact_executor, hq)
+    v, ov = plans(gb, exact_executor, vq)
+    x = image(v.source_size, h.source_size, 61)
+    exact_executor.profile(True)
+    got = exact_executor.inverse_2d(h, v, x)
+    names = {k["name"] for k in exact_executor.kernel_times()}
+    exact_executor.profile(False)
+    if not (h.requires_float64 or v.requires_float64):
+        assert any(n.startswith("tsolve_f32/rows") for n in names), names
+        assert any(n.startswith("tsolve_f32/columns") for n in names), names
+        assert np.array_equal(got, O.inverse_2d_gpu_order(oh, ov, x))
+        xi = make_input(v.source_size, h.source_size, "u16", 62)
+        conv = gb.integer_conversion(16, False, False)
+        goti = exact_executor.inverse_2d(h, v, xi, conv)
+        assert np.array_equal(goti, O.inverse_2d_gpu_order(oh, ov, xi, conv))
+
+
+@pytest.mark.parametrize("name,hq,vq", WIDE_2D, ids=[c[0] for c in WIDE_2D])
+def test_wide_bands_use_two_pass_kernels(gb, executor, name, hq, vq):
+    """Half-bandwidths 9 and 11 (no chunk-delayed kernel, or factors that
+    decay too slowly for it) run on the two-pass kernels by default."""
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = image(v.source_size, h.source_size, 63)
+    executor.profile(True)
+    got = executor.inverse_2d(h, v, x)
+    names = {k["name"] for k in executor.kernel_times()}
+    executor.profile(False)
+    assert any(n.startswith("tsolve_f32") for n in names), names
+    scalar = O.inverse_2d(oh, ov, x)
+    err = np.abs(got.astype(np.float64) - scalar)
+    assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS

@@ -87,6 +87,7 @@ struct DevicePlan {
     bool stream = false;
     bool stream_u16 = false, stream_u8 = false;
     bool stream_t = false;          // transposing 2D kernels admitted
+    bool stream_x = false;          // two-pass transposing 2D kernels admitted
     dev::StreamPlanView stream_view{};
     bool stream_p = false;          // paired transposing 2D kernels admitted
     dev::StreamPlanView stream_view2{};
@@ -106,9 +107,9 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         {f64 ? p.transpose_weights_f64.data() : nullptr, f64 ? p.transpose_weights_f64.size() * 8 : 0},
         {f64 ? p.ldlt_bands_f64.data() : nullptr, f64 ? p.ldlt_bands_f64.size() * 8 : 0},
     };
-    const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing,
-                                             stream_supports(p.half_bandwidth));
-    if (pack.eligible) {
+    const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
+                                             tsolve_supports(p.half_bandwidth));
+    if (pack.eligible || pack.exact) {
         parts.push_back({pack.forward.data(), pack.forward.size() * 4});
         parts.push_back({pack.backward.data(), pack.backward.size() * 4});
         if (pack.paired) {
@@ -142,11 +143,12 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     v.inv_diag = reinterpret_cast<const float *>(base + offsets[5]);
     v.weights64 = f64 ? reinterpret_cast<const double *>(base + offsets[6]) : nullptr;
     v.bands64 = f64 ? reinterpret_cast<const double *>(base + offsets[7]) : nullptr;
-    if (pack.eligible) {
-        dp->stream = true;
-        dp->stream_u16 = pack.ring_ok_u16;
-        dp->stream_u8 = pack.ring_ok_u8;
-        dp->stream_t = pack.ring_ok_transposed;
+    if (pack.eligible || pack.exact) {
+        dp->stream = pack.eligible;
+        dp->stream_u16 = pack.eligible && pack.ring_ok_u16;
+        dp->stream_u8 = pack.eligible && pack.ring_ok_u8;
+        dp->stream_t = pack.eligible && pack.ring_ok_transposed;
+        dp->stream_x = pack.exact;
         auto &sv = dp->stream_view;
         sv.source_size = p.source_size;
         sv.destination_size = p.destination_size;
@@ -311,6 +313,10 @@ struct Executor::Impl {
     // kernels (64 vectors per warp); the unpaired ones (32 per warp) are the
     // default, faster on GB300 at the occupancy the paired ones reach.
     bool allow_paired = false;
+    // DSMVC_GB_EXACT=1 runs every admitted 2D pass on the two-pass
+    // transposing kernels; otherwise they serve the plans the chunk-delayed
+    // kernels do not admit (slowly decaying factors, half-bandwidths 9, 11).
+    bool prefer_exact = false;
     // Default CTA size of the transposing kernels (DSMVC_GB_TSTREAM_THREADS,
     // 32..256 in multiples of 32); batches may tune it per launch group.
     int tstream_threads = kTStreamThreads;
@@ -459,7 +465,8 @@ bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
 }
 
 std::string kernel_name(const GroupKey &k) {
-    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32"};
+    static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32",
+                                  "tsolve_f32"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -475,7 +482,10 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         // Float32 2D planes keep the intermediate transposed (destination
         // column-major): both passes then read adjacent samples and write
         // adjacent vectors.
-        bool transposed = false, h_t = false, v_t = false;
+        // 2D passes: 0 sequential, 3 chunk-delayed, 4 paired chunk-delayed,
+        // 5 two-pass transposing.
+        bool transposed = false;
+        int h_kind = 0, v_kind = 0;
         std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0;
     };
     std::vector<Route> routes(tasks.size());
@@ -495,14 +505,21 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         const std::size_t es = r.f64 ? 8 : 4;
         if (h && v && !r.f64) {
             r.transposed = true;
-            r.h_t = allow_stream && r.h->stream && r.h->stream_t
-                && (task.sample == dev::Sample::f32 || task.sample == dev::Sample::u16
-                    || task.sample == dev::Sample::u8);
-            r.v_t = allow_stream && r.v->stream && r.v->stream_t;
+            auto pass_kind = [&](const DevicePlan &dp) {
+                if (!allow_stream) return 0;
+                const bool delayed = dp.stream && dp.stream_t;
+                if (dp.stream_x && (prefer_exact || !delayed)) return 5;
+                if (delayed) return allow_paired && dp.stream_p ? 4 : 3;
+                return 0;
+            };
+            r.h_kind = pass_kind(*r.h);
+            r.v_kind = pass_kind(*r.v);
             r.mid_stride = (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4;
             r.mid = bytes;
             bytes += align_up(r.mid_stride * static_cast<std::size_t>(h->destination_size) * 4);
-            if (!r.v_t && task.sample != dev::Sample::f32) {
+            // Forward values of the second pass when the output cannot hold
+            // them (integer samples): the sequential and two-pass kernels.
+            if ((r.v_kind == 0 || r.v_kind == 5) && task.sample != dev::Sample::f32) {
                 r.fwd_stride = static_cast<std::size_t>(h->destination_size);
                 r.fwd = bytes;
                 bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 4);
@@ -547,16 +564,15 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             hi.bytes = static_cast<std::uint64_t>(v->source_size) * h->source_size * sample_bytes(task.sample);
             vi.bytes = static_cast<std::uint64_t>(h->destination_size) * v->destination_size
                 * sample_bytes(task.sample);
-            if (r.h_t) {
-                // Paired kernels (two vectors per lane) where admitted.
-                const bool pair = allow_paired && r.h->stream_p;
+            if (r.h_kind) {
                 auto &j = hi.stream;
-                j.plan = pair ? r.h->stream_view2 : r.h->stream_view;
+                j.plan = r.h_kind == 4 ? r.h->stream_view2 : r.h->stream_view;
                 j.in = task.input; j.in_elem = 1; j.in_vec = task.input_stride;
                 j.out = mid; j.out_elem = pitch; j.out_vec = 1;
+                j.y = mid; j.y_elem = pitch;                // forward values in place
                 j.vectors = v->source_size;
                 j.conv = conv;
-                groups[{0, pair ? 4 : 3, h->half_bandwidth, task.sample, dev::Sample::f32,
+                groups[{0, r.h_kind, h->half_bandwidth, task.sample, dev::Sample::f32,
                         j.plan.window == 8 ? 1 : 0}].push_back(hi);
             } else {
                 auto &j = hi.axis;
@@ -568,15 +584,21 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.conv = conv;
                 groups[{0, 0, h->half_bandwidth, task.sample, dev::Sample::f32}].push_back(hi);
             }
-            if (r.v_t) {
-                const bool pair = allow_paired && r.v->stream_p;
+            if (r.v_kind) {
                 auto &j = vi.stream;
-                j.plan = pair ? r.v->stream_view2 : r.v->stream_view;
+                j.plan = r.v_kind == 4 ? r.v->stream_view2 : r.v->stream_view;
                 j.in = mid; j.in_elem = 1; j.in_vec = pitch;
                 j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
+                if (r.fwd_stride) {
+                    j.y = reinterpret_cast<float *>(base + r.fwd);
+                    j.y_elem = static_cast<std::int64_t>(r.fwd_stride);
+                } else {
+                    j.y = static_cast<float *>(task.output);   // Float32 output: in place
+                    j.y_elem = task.output_stride;
+                }
                 j.vectors = h->destination_size;
                 j.conv = conv;
-                groups[{1, pair ? 4 : 3, v->half_bandwidth, dev::Sample::f32, task.sample,
+                groups[{1, r.v_kind, v->half_bandwidth, dev::Sample::f32, task.sample,
                         j.plan.window == 8 ? 1 : 0}].push_back(vi);
             } else {
                 auto &j = vi.axis;
@@ -743,7 +765,10 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         }
         const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.kind == 4) {
+        if (l.kind == 5) {
+            rc = launch_tsolve(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
+                               l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
+        } else if (l.kind == 4) {
             rc = launch_tstream2(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
                                  l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
         } else if (l.kind == 3) {
@@ -816,6 +841,8 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         impl_->allow_stream = false;
     if (const char *env = std::getenv("DSMVC_GB_PAIRED"))
         impl_->allow_paired = std::string(env) == "1";
+    if (const char *env = std::getenv("DSMVC_GB_EXACT"))
+        impl_->prefer_exact = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);

@@ -66,6 +66,30 @@ int launch_tstream2(const dev::StreamJob *jobs, int job_count, int total_blocks,
 #undef DSMVC_PAIRED
 }
 
+int launch_tsolve_hb1(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tsolve_hb3(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tsolve_hb5(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tsolve_hb7(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tsolve_hb9(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tsolve_hb11(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+
+bool tsolve_supports(int half_bandwidth) {
+    return half_bandwidth >= 1 && half_bandwidth <= 11 && half_bandwidth % 2 == 1;
+}
+
+int launch_tsolve(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
+                  int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
+    switch (half_bandwidth) {
+    case 1: return launch_tsolve_hb1(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 3: return launch_tsolve_hb3(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 5: return launch_tsolve_hb5(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 7: return launch_tsolve_hb7(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 9: return launch_tsolve_hb9(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    case 11: return launch_tsolve_hb11(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+    default: return static_cast<int>(cudaErrorInvalidValue);
+    }
+}
+
 int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
                    int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
     switch (half_bandwidth) {

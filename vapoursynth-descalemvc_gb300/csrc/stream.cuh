@@ -38,6 +38,10 @@ struct StreamJob {
     std::int32_t vectors;
     std::int32_t first_block;       // transposing kernels: the job's first warp
     Conversion conv;
+    // Two-pass transposing kernels: the Float32 forward-value plane, laid
+    // out like `out` (destination j of vector v at y[j * y_elem + v]).
+    float *y;
+    std::int64_t y_elem;
 };
 
 } // namespace dsmvc_gb::dev
@@ -71,6 +75,13 @@ int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, 
 int launch_tstream2(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
                     int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
                     void *stream);
+
+// Two-pass transposing 2D passes (tsolve_impl.cuh): exact forward and
+// backward sweeps through the jobs' forward-value planes; half-bandwidths
+// 1..11 (odd).
+bool tsolve_supports(int half_bandwidth);
+int launch_tsolve(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
+                  int window, dev::Sample in, dev::Sample out, int record_floats, void *stream);
 
 // `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,

@@ -44,10 +44,10 @@ bool ring_fits_grouped(const std::vector<int> &s0, int window, int size, int rin
 
 } // namespace
 
-StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supported) {
+StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supported, bool hb_supported_exact) {
     StreamPack out;
     const int n = p.destination_size, m = p.source_size, hb = p.half_bandwidth;
-    if (!hb_supported) {
+    if (!hb_supported && !hb_supported_exact) {
         out.reason = "half-bandwidth without a streaming kernel";
         return out;
     }
@@ -83,10 +83,10 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.ring_ok_u16 = ring_fits(s0, window, m, 8, ring);
     out.ring_ok_u8 = ring_fits(s0, window, m, 16, ring);
     out.ring_ok_transposed = ring_fits_grouped(s0, window, m, ring);
-    if (!out.ring_ok_f32) {
-        out.reason = "gather windows advance faster than the ring";
-        return out;
-    }
+    // The two-pass transposing kernels need only the grouped feed.
+    out.exact = hb_supported_exact && out.ring_ok_transposed;
+    if (!out.ring_ok_f32) out.reason = "gather windows advance faster than the ring";
+    else if (!hb_supported) out.reason = "half-bandwidth without a chunk-delayed kernel";
 
     // Backward warm-up accuracy: the carry entering a chunk's end, pushed
     // through the chunk's homogeneous backward recurrence, must vanish.
@@ -111,10 +111,10 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
         }
     }
     out.backward_transfer = worst;
-    if (!(worst <= std::ldexp(1.0, -26))) {
+    if (out.reason.empty() && !(worst <= std::ldexp(1.0, -26)))
         out.reason = "backward carry decays too slowly for one chunk";
-        return out;
-    }
+    const bool delayed = out.reason.empty();
+    if (!delayed && !out.exact) return out;
 
     const int low = round4(hb);
     out.window = window;
@@ -157,9 +157,9 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
                 ? p.upper_l[static_cast<std::size_t>(d - 1) * w + static_cast<std::size_t>(j)] : 0.0F;
         }
     }
-    out.eligible = true;
+    out.eligible = delayed;
 
-    if (out.ring_ok_transposed && window <= 16) {
+    if (delayed && out.ring_ok_transposed && window <= 16) {
         const int pl = round4(2 * hb);
         out.paired = true;
         out.paired_forward_stride = 4 + 2 * window + pl;

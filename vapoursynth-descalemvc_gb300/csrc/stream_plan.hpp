@@ -11,8 +11,9 @@
 namespace dsmvc_gb {
 
 struct StreamPack {
-    bool eligible = false;          // the plan may use the streaming kernels
-    std::string reason;             // why not, when not
+    bool eligible = false;          // the plan may use the chunk-delayed streaming kernels
+    bool exact = false;             // the plan may use the two-pass transposing kernels
+    std::string reason;             // why not chunk-delayed, when not
     int window = 0;                 // dense gather window (multiple of 4)
     int forward_stride = 0;         // floats per forward record
     int backward_stride = 0;        // floats per backward record
@@ -44,7 +45,10 @@ struct StreamPack {
 // the zero-carry backward warm-up over one chunk leaves a carry influence
 // below 2^-26 per carry slot (computed in double for every chunk of the
 // plan), which keeps the warm-up error within about one float ULP.
+// Records are built when either family admits the plan; the two-pass
+// transposing kernels (tsolve_impl.cuh) need only the window, monotone
+// window starts and the grouped ring replay.
 StreamPack pack_stream_plan(const AxisPlan &plan, int chunk, int ring,
-                            bool half_bandwidth_supported);
+                            bool half_bandwidth_supported, bool half_bandwidth_supported_exact = false);
 
 } // namespace dsmvc_gb
