@@ -190,6 +190,7 @@ typedef struct dsmvc_gb_stream_info {
     double backward_transfer;    /* carry influence after one chunk */
     char reason[96];             /* why not eligible */
     int32_t ring_ok_transposed;  /* the 2D passes' warp-wide block feed fits */
+    int32_t exact;               /* two-pass transposing kernels admitted */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,

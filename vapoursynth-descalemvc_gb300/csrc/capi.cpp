@@ -242,7 +242,8 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         const auto &p = plan_of(plan);
         if (!info) throw std::invalid_argument("output is null");
         const auto pack = dsmvc_gb::pack_stream_plan(p, dsmvc_gb::kStreamChunk, dsmvc_gb::kStreamRing,
-                                                     dsmvc_gb::stream_supports(p.half_bandwidth));
+                                                     dsmvc_gb::stream_supports(p.half_bandwidth),
+                                                     dsmvc_gb::tsolve_supports(p.half_bandwidth));
         *info = {};
         info->eligible = pack.eligible ? 1 : 0;
         info->window = pack.window;
@@ -251,6 +252,7 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->ring_ok_u16 = pack.ring_ok_u16 ? 1 : 0;
         info->ring_ok_u8 = pack.ring_ok_u8 ? 1 : 0;
         info->ring_ok_transposed = pack.ring_ok_transposed ? 1 : 0;
+        info->exact = pack.exact ? 1 : 0;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;
         info->backward_transfer = pack.backward_transfer;

@@ -88,6 +88,7 @@ struct DevicePlan {
     bool stream_u16 = false, stream_u8 = false;
     bool stream_t = false;          // transposing 2D kernels admitted
     bool stream_x = false;          // two-pass transposing 2D kernels admitted
+    bool stream_xg = false;         // ... with the grouped refill of window 8
     dev::StreamPlanView stream_view{};
     bool stream_p = false;          // paired transposing 2D kernels admitted
     dev::StreamPlanView stream_view2{};
@@ -149,6 +150,7 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         dp->stream_u8 = pack.eligible && pack.ring_ok_u8;
         dp->stream_t = pack.eligible && pack.ring_ok_transposed;
         dp->stream_x = pack.exact;
+        dp->stream_xg = pack.exact && pack.ring_ok_transposed && pack.window == 8;
         auto &sv = dp->stream_view;
         sv.source_size = p.source_size;
         sv.destination_size = p.destination_size;
@@ -464,6 +466,13 @@ bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
     return in == dev::Sample::f32;
 }
 
+// Launch-group variant of a transposing pass: 1 runs the window-8 kernels
+// (compile-time gather; for the two-pass kernels also the grouped refill).
+int compiled_window(const DevicePlan &dp, int kind) {
+    if (kind == 5) return dp.stream_xg ? 1 : 0;
+    return dp.stream_view.window == 8 ? 1 : 0;
+}
+
 std::string kernel_name(const GroupKey &k) {
     static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32",
                                   "tsolve_f32"};
@@ -573,7 +582,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.vectors = v->source_size;
                 j.conv = conv;
                 groups[{0, r.h_kind, h->half_bandwidth, task.sample, dev::Sample::f32,
-                        j.plan.window == 8 ? 1 : 0}].push_back(hi);
+                        compiled_window(*r.h, r.h_kind)}].push_back(hi);
             } else {
                 auto &j = hi.axis;
                 j.plan = r.h->view;
@@ -599,7 +608,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.vectors = h->destination_size;
                 j.conv = conv;
                 groups[{1, r.v_kind, v->half_bandwidth, dev::Sample::f32, task.sample,
-                        j.plan.window == 8 ? 1 : 0}].push_back(vi);
+                        compiled_window(*r.v, r.v_kind)}].push_back(vi);
             } else {
                 auto &j = vi.axis;
                 j.plan = r.v->view;

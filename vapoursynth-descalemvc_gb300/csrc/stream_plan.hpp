@@ -13,6 +13,7 @@ namespace dsmvc_gb {
 struct StreamPack {
     bool eligible = false;          // the plan may use the chunk-delayed streaming kernels
     bool exact = false;             // the plan may use the two-pass transposing kernels
+                                    // (per-destination refill; grouped when ring_ok_transposed)
     std::string reason;             // why not chunk-delayed, when not
     int window = 0;                 // dense gather window (multiple of 4)
     int forward_stride = 0;         // floats per forward record

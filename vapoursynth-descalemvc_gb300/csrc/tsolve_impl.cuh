@@ -15,6 +15,8 @@
 //
 // Nothing is approximated, so the results equal the reference CUDA kernels'
 // bit for bit, for any decay of the factors and half-bandwidths up to 11.
+// The ring is refilled per destination (windows up to 16 samples), or per
+// group of four destinations for window 8 where the host's replay admits it.
 // The forward plane is the output itself where it is a Float32 plane with
 // the output's layout (the first pass's intermediate, Float32 outputs), else
 // a caller scratch plane.  Registers hold one chunk at a time.
@@ -88,13 +90,17 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
             float y[LC];
 #pragma unroll
             for (int t = 0; t < LC; ++t) {
-                if (t % 4 == 0) {
-                    const int s_last = __float_as_int(fwd[(t + 3) * fs]);
-                    const int need = max(s_last, __float_as_int(fwd[t * fs])) + kw;
-                    feed.ensure(min(need, p.source_size));
+                if constexpr (K > 0) {
+                    // Window 8: one refill per group of four destinations.
+                    if (t % 4 == 0) {
+                        const int s_last = __float_as_int(fwd[(t + 3) * fs]);
+                        const int need = max(s_last, __float_as_int(fwd[t * fs])) + kw;
+                        feed.ensure(min(need, p.source_size));
+                    }
                 }
                 const float *rec = fwd + t * fs;
                 const float4 hdr = tlds4(rec);
+                if constexpr (K == 0) feed.ensure(min(__float_as_int(hdr.x) + kw, p.source_size));
                 const float *win = feed.ring + lane + __float_as_int(hdr.z);
                 float sum = 0.0f;
                 if constexpr (K > 0) {
