@@ -82,11 +82,13 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.ring_ok_f32 = ring_fits(s0, window, m, 4, ring);
     out.ring_ok_u16 = ring_fits(s0, window, m, 8, ring);
     out.ring_ok_u8 = ring_fits(s0, window, m, 16, ring);
-    out.ring_ok_transposed = ring_fits_grouped(s0, window, m, ring);
+    // The transposing kernels keep the ring's first 16 rows twice: windows of
+    // up to 16 samples.
+    out.ring_ok_transposed = ring_fits_grouped(s0, window, m, ring) && window <= 16;
     // The two-pass transposing kernels refill their ring per destination in
     // blocks of 16 (per group of four destinations with window 8 when the
     // grouped replay holds).
-    out.exact = hb_supported_exact && out.ring_ok_u8;
+    out.exact = hb_supported_exact && out.ring_ok_u8 && window <= 16;
     if (!out.ring_ok_f32) out.reason = "gather windows advance faster than the ring";
     else if (!hb_supported) out.reason = "half-bandwidth without a chunk-delayed kernel";
 

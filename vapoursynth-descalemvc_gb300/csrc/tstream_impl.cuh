@@ -9,8 +9,9 @@
 //  * Loads: blocks of 16 source samples of all 32 vectors are fetched by the
 //    whole warp with 16-byte coalesced loads (2 lanes per u16 vector, 4 per
 //    f32 vector, 1 per u8 vector), converted to float and scattered into a
-//    shared ring of 32 sample rows, stored twice so that any window of up to
-//    32 consecutive samples is contiguous.  Ring rows are 34 floats apart:
+//    shared ring of 32 sample rows whose first 16 rows are stored again
+//    after it, so that any window of up to 16 consecutive samples is
+//    contiguous (the host admits windows up to 16).  Rows are 34 floats apart:
 //    the scatter of every load pattern and the per-lane reads of one sample
 //    row are both free of bank conflicts.  The next block is in flight while
 //    the current one is consumed.
@@ -41,7 +42,8 @@ using dev::StreamJob;
 
 constexpr int kTRing = kStreamRing;        // sample rows per ring
 constexpr int kTPitch = kTRingPitch;       // floats between ring rows
-constexpr int kTRingFloats = 2 * kTRing * kTPitch;
+constexpr int kTDup = 16;                  // leading rows stored again after the ring
+constexpr int kTRingFloats = (kTRing + kTDup) * kTPitch;
 constexpr int kTChunk = kStreamChunk;
 constexpr int kTMaxThreads = 256;         // CTA sizes 32..256 (a multiple of 32)
 constexpr int kTBlock = 16;                // samples per warp load block
@@ -106,9 +108,10 @@ struct WarpFeeder {
     bool pend_ok;
 
     __device__ __forceinline__ void put(int s, int v, float x) {
-        float *r = ring + (s & (kTRing - 1)) * kTPitch + v;
+        const int row = s & (kTRing - 1);
+        float *r = ring + row * kTPitch + v;
         r[0] = x;
-        r[kTRing * kTPitch] = x;
+        if (row < kTDup) r[kTRing * kTPitch] = x;
     }
 
     __device__ __forceinline__ void issue() {
@@ -134,7 +137,9 @@ struct WarpFeeder {
         while (have < need) {
             if (pend_ok) {
                 // A block starts on a multiple of 16, so a lane's SPL samples
-                // occupy consecutive ring rows without wrapping.
+                // occupy consecutive ring rows without wrapping, and all of
+                // the block is in the duplicated rows or none of it is.
+                const bool dup = (have & (kTRing - 1)) < kTDup;
 #pragma unroll
                 for (int i = 0; i < NI; ++i) {
                     const int v = i * VPI + lane / LPV;
@@ -144,7 +149,7 @@ struct WarpFeeder {
                     for (int k = 0; k < SPL; ++k) {
                         const float x = tin(vals[k], conv);
                         r[k * kTPitch] = x;
-                        r[(kTRing + k) * kTPitch] = x;
+                        if (dup) r[(kTRing + k) * kTPitch] = x;
                     }
                 }
                 have += kTBlock;
