@@ -105,7 +105,7 @@ typedef struct dsmvc_gb_planner_stats {
 
 /* Executor counters.  The plan cache holds device copies of plans that were
  * not prepared (an LRU keyed by plan identity, DSMVC_GB_PLAN_CACHE_MB =
- * 16..4096 MiB, default 256; the reference's packed-plan cache,
+ * 16..4096 MiB, default 2048; the reference's packed-plan cache,
  * src/cuda/cuda_executor.cpp:1936-2020, DSMVC_CUDA_PLAN_CACHE_MB). */
 typedef struct dsmvc_gb_executor_stats {
     uint64_t launches;

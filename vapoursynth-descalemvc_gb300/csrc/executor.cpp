@@ -269,7 +269,7 @@ struct Executor::Impl {
     std::unordered_map<const AxisPlan *, CacheEntry> cache;
     std::list<const AxisPlan *> cache_lru;
     std::size_t cache_bytes = 0;
-    std::size_t cache_capacity = 256ULL << 20;
+    std::size_t cache_capacity = 2048ULL << 20;
     bool sealed = false;
     // Synchronous host calls take one of these slots (the reference's
     // execution slots, src/cuda/cuda_executor.cpp:1102-1160).

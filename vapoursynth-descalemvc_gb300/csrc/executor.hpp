@@ -82,7 +82,8 @@ struct ExecutorStats {
     std::size_t workspace_bytes = 0;
     // Device plan cache of plans that were not prepared (an LRU keyed by
     // plan identity and bounded by DSMVC_GB_PLAN_CACHE_MB, 16..4096 MiB,
-    // default 256; the counterpart of DSMVC_CUDA_PLAN_CACHE_MB).
+    // default 2048: evicting frees device memory, which waits for the whole
+    // device; the counterpart of DSMVC_CUDA_PLAN_CACHE_MB).
     std::uint64_t plan_cache_hits = 0;
     std::uint64_t plan_cache_misses = 0;
     std::uint64_t plan_cache_evictions = 0;
