@@ -401,3 +401,37 @@ def test_wide_bands_use_two_pass_kernels(gb, executor, name, hq, vq):
     scalar = O.inverse_2d(oh, ov, x)
     err = np.abs(got.astype(np.float64) - scalar)
     assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+
+
+F64_TRANSPOSED = [
+    ("bicubic-forced", (300, 200, 200.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2),
+     (170, 113, 113.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2)),
+    ("lanczos3-forced-repeat", (257, 190, 190.0, 0.3, "lanczos", 3, 0, 0.5, 1.0, "repeat", 2),
+     (143, 101, 101.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 2)),
+    ("spline64-blur-hb9-forced", (384, 256, 256.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2),
+     (216, 144, 144.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2)),
+]
+
+
+@pytest.mark.parametrize("sample", ["f32", "u16"])
+@pytest.mark.parametrize("name,hq,vq", F64_TRANSPOSED, ids=[c[0] for c in F64_TRANSPOSED])
+def test_float64_transposing_kernels(gb, executor, sample, name, hq, vq):
+    """Both axes retaining Float64: the Float64 two-pass transposing kernels
+    run (profiled names) and give the CPU scalar Float64 route's output bit
+    for bit (the contract is <= 1 float ULP)."""
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    assert h.requires_float64 and v.requires_float64
+    x = make_input(v.source_size, h.source_size, sample, 71)
+    conv = gb.integer_conversion(16, False, False) if sample == "u16" else None
+    executor.profile(True)
+    got = executor.inverse_2d(h, v, x, conv)
+    names = {k["name"] for k in executor.kernel_times()}
+    executor.profile(False)
+    assert any(n.startswith("tsolve_f64/rows") for n in names), names
+    assert any(n.startswith("tsolve_f64/columns") for n in names), names
+    want = O.inverse_2d(oh, ov, x, conv)
+    if sample == "u16":
+        assert np.array_equal(got, want)
+    else:
+        assert max_ulp(got, want) == 0

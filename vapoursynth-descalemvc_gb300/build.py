@@ -30,7 +30,8 @@ NVCCFLAGS = ARCH + ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
 HOST_SOURCES = ["planner.cpp", "stream_plan.cpp", "executor.cpp", "sweep.cpp", "server.cpp",
                 "capi.cpp"]
 TSTREAM2_SOURCES = [f"tstream2_hb{hb}_k{k}.cu" for hb in (1, 3, 5, 7) for k in (0, 8)]
-TSOLVE_SOURCES = [f"tsolve_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)]
+TSOLVE_SOURCES = ([f"tsolve_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)]
+                  + [f"tsolve64_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)])
 CUDA_SOURCES = TSTREAM2_SOURCES + TSOLVE_SOURCES + ["kernels.cu", "stream.cu", "stream_hb1.cu", "stream_hb3.cu", "stream_hb5.cu",
                 "stream_hb7.cu", "tstream_hb1.cu", "tstream_hb3.cu",
                 "tstream_hb5.cu", "tstream_hb7.cu", "noalloc.cu", "score.cu",

@@ -89,6 +89,8 @@ struct DevicePlan {
     bool stream_t = false;          // transposing 2D kernels admitted
     bool stream_x = false;          // two-pass transposing 2D kernels admitted
     bool stream_xg = false;         // ... with the grouped refill of window 8
+    bool stream64 = false;          // Float64 two-pass transposing kernels admitted
+    dev::StreamPlanView stream_view64{};
     dev::StreamPlanView stream_view{};
     bool stream_p = false;          // paired transposing 2D kernels admitted
     dev::StreamPlanView stream_view2{};
@@ -110,13 +112,22 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     };
     const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
                                              tsolve_supports(p.half_bandwidth));
+    const StreamPack64 pack64 = pack_stream_plan64(p, kStreamChunk, kStreamRing, tsolve_supports(p.half_bandwidth));
+    std::size_t at_records = 0, at_paired = 0, at_records64 = 0;
     if (pack.eligible || pack.exact) {
+        at_records = parts.size();
         parts.push_back({pack.forward.data(), pack.forward.size() * 4});
         parts.push_back({pack.backward.data(), pack.backward.size() * 4});
         if (pack.paired) {
+            at_paired = parts.size();
             parts.push_back({pack.paired_forward.data(), pack.paired_forward.size() * 4});
             parts.push_back({pack.paired_backward.data(), pack.paired_backward.size() * 4});
         }
+    }
+    if (pack64.eligible) {
+        at_records64 = parts.size();
+        parts.push_back({pack64.forward.data(), pack64.forward.size() * 8});
+        parts.push_back({pack64.backward.data(), pack64.backward.size() * 8});
     }
     std::size_t total = 0;
     std::vector<std::size_t> offsets;
@@ -158,17 +169,29 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         sv.window = pack.window;
         sv.forward_stride = pack.forward_stride;
         sv.backward_stride = pack.backward_stride;
-        sv.forward = reinterpret_cast<const float *>(base + offsets[8]);
-        sv.backward = reinterpret_cast<const float *>(base + offsets[9]);
+        sv.forward = reinterpret_cast<const float *>(base + offsets[at_records]);
+        sv.backward = reinterpret_cast<const float *>(base + offsets[at_records + 1]);
         if (pack.paired) {
             dp->stream_p = true;
             auto &pv = dp->stream_view2;
             pv = sv;
             pv.forward_stride = pack.paired_forward_stride;
             pv.backward_stride = pack.paired_backward_stride;
-            pv.forward = reinterpret_cast<const float *>(base + offsets[10]);
-            pv.backward = reinterpret_cast<const float *>(base + offsets[11]);
+            pv.forward = reinterpret_cast<const float *>(base + offsets[at_paired]);
+            pv.backward = reinterpret_cast<const float *>(base + offsets[at_paired + 1]);
         }
+    }
+    if (pack64.eligible) {
+        dp->stream64 = true;
+        auto &xv = dp->stream_view64;
+        xv.source_size = p.source_size;
+        xv.destination_size = p.destination_size;
+        xv.half_bandwidth = p.half_bandwidth;
+        xv.window = pack64.window;
+        xv.forward_stride = pack64.forward_stride;
+        xv.backward_stride = pack64.backward_stride;
+        xv.forward = reinterpret_cast<const float *>(base + offsets[at_records64]);
+        xv.backward = reinterpret_cast<const float *>(base + offsets[at_records64 + 1]);
     }
     dp->bytes = total;
     dp->keep = std::move(keep);
@@ -475,7 +498,7 @@ int compiled_window(const DevicePlan &dp, int kind) {
 
 std::string kernel_name(const GroupKey &k) {
     static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32",
-                                  "tsolve_f32"};
+                                  "tsolve_f32", "tsolve_f64"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -494,6 +517,9 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         // 2D passes: 0 sequential, 3 chunk-delayed, 4 paired chunk-delayed,
         // 5 two-pass transposing.
         bool transposed = false;
+        // Float64 planes whose plans both admit the Float64 two-pass
+        // transposing kernels (kind 6): a transposed Float64 intermediate.
+        bool transposed64 = false;
         int h_kind = 0, v_kind = 0;
         std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0;
     };
@@ -512,7 +538,15 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             r.v_stream = r.v && r.v->stream;
         }
         const std::size_t es = r.f64 ? 8 : 4;
-        if (h && v && !r.f64) {
+        if (h && v && r.f64 && allow_stream && r.h->stream64 && r.v->stream64) {
+            r.transposed64 = true;
+            r.mid_stride = (static_cast<std::size_t>(v->source_size) + 1) / 2 * 2;
+            r.mid = bytes;
+            bytes += align_up(r.mid_stride * static_cast<std::size_t>(h->destination_size) * 8);
+            r.fwd_stride = static_cast<std::size_t>(h->destination_size);
+            r.fwd = bytes;
+            bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 8);
+        } else if (h && v && !r.f64) {
             r.transposed = true;
             auto pass_kind = [&](const DevicePlan &dp) {
                 if (!allow_stream) return 0;
@@ -566,6 +600,31 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         const dev::Conversion conv = to_dev(task.conversion);
         const dev::Sample mid_kind = r.f64 ? dev::Sample::f64 : dev::Sample::f32;
         const int seq_kind = r.f64 ? 1 : 0;
+        if (r.transposed64) {
+            void *mid = base + r.mid;
+            const auto pitch = static_cast<std::int64_t>(r.mid_stride);
+            Item hi, vi;
+            hi.bytes = static_cast<std::uint64_t>(v->source_size) * h->source_size * sample_bytes(task.sample);
+            vi.bytes = static_cast<std::uint64_t>(h->destination_size) * v->destination_size
+                * sample_bytes(task.sample);
+            auto &a = hi.stream;
+            a.plan = r.h->stream_view64;
+            a.in = task.input; a.in_elem = 1; a.in_vec = task.input_stride;
+            a.out = mid; a.out_elem = pitch; a.out_vec = 1;
+            a.y = static_cast<float *>(mid); a.y_elem = pitch;   // Float64 forward values in place
+            a.vectors = v->source_size;
+            a.conv = conv;
+            groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}].push_back(hi);
+            auto &b = vi.stream;
+            b.plan = r.v->stream_view64;
+            b.in = mid; b.in_elem = 1; b.in_vec = pitch;
+            b.out = task.output; b.out_elem = task.output_stride; b.out_vec = 1;
+            b.y = reinterpret_cast<float *>(base + r.fwd); b.y_elem = static_cast<std::int64_t>(r.fwd_stride);
+            b.vectors = h->destination_size;
+            b.conv = conv;
+            groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}].push_back(vi);
+            continue;
+        }
         if (r.transposed) {
             float *mid = reinterpret_cast<float *>(base + r.mid);
             const auto pitch = static_cast<std::int64_t>(r.mid_stride);
@@ -774,7 +833,10 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         }
         const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.kind == 5) {
+        if (l.kind == 6) {
+            rc = launch_tsolve64(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
+                                 l.hb, l.in, l.out, l.record_floats, status, stream);
+        } else if (l.kind == 5) {
             rc = launch_tsolve(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
                                l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
         } else if (l.kind == 4) {

@@ -4,6 +4,7 @@
 #include "stream.cuh"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 
@@ -192,6 +193,72 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
             }
         }
     }
+    return out;
+}
+
+StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_supported) {
+    StreamPack64 out;
+    const int n = p.destination_size, m = p.source_size, hb = p.half_bandwidth;
+    if (!hb_supported || !p.requires_float64()) return out;
+    int span = 1;
+    for (int j = 0; j < n; ++j) {
+        const auto b = p.transpose_offsets[j], e = p.transpose_offsets[j + 1];
+        if (b < e) span = std::max(span, p.transpose_indices[e - 1] - p.transpose_indices[b] + 1);
+    }
+    const int window = round4(span);
+    if (window > 16 || window > m) return out;
+    std::vector<int> s0(static_cast<std::size_t>(n));
+    int previous = 0;
+    for (int j = 0; j < n; ++j) {
+        const auto b = p.transpose_offsets[j], e = p.transpose_offsets[j + 1];
+        int first = b < e ? p.transpose_indices[b] : previous;
+        first = std::min(first, m - window);
+        if (first < previous) return out;
+        s0[static_cast<std::size_t>(j)] = first;
+        previous = first;
+    }
+    if (!ring_fits(s0, window, m, 16, ring)) return out;
+    const int fs = (2 + window + hb + 1) / 2 * 2;          // doubles, even
+    const int bs = std::max(2, (hb + 1) / 2 * 2);
+    const auto padded = static_cast<std::size_t>((n + chunk - 1) / chunk) * static_cast<std::size_t>(chunk);
+    out.forward.assign(padded * static_cast<std::size_t>(fs), 0.0);
+    out.backward.assign(padded * static_cast<std::size_t>(bs), 0.0);
+    const auto w = static_cast<std::size_t>(n);
+    for (std::size_t j = 0; j < padded; ++j) {
+        double *f = out.forward.data() + j * static_cast<std::size_t>(fs);
+        const bool real = j < w;
+        const int start = real ? s0[j] : s0.back();
+        int count = 0;
+        if (real) {
+            for (auto k = p.transpose_offsets[j]; k < p.transpose_offsets[j + 1]; ++k) {
+                const int at = p.transpose_indices[k] - start;
+                f[2 + at] = p.transpose_weights_f64[k];
+                count = std::max(count, at + 1);
+            }
+            f[1] = p.ldlt_bands_f64[j] + DBL_EPSILON;      // band 0 holds D
+            for (int q = 0; q < hb; ++q) {
+                const int d = hb - q;                          // d = hb..1
+                if (static_cast<std::size_t>(d) <= j)
+                    f[2 + window + q] = p.ldlt_bands_f64[static_cast<std::size_t>(d) * w + j - static_cast<std::size_t>(d)];
+            }
+            double *b = out.backward.data() + j * static_cast<std::size_t>(bs);
+            const auto avail = std::min<std::size_t>(static_cast<std::size_t>(hb), w - j - 1);
+            for (int q = 0; q < hb; ++q) {
+                const int d = hb - q;
+                if (static_cast<std::size_t>(d) <= avail)
+                    b[q] = p.ldlt_bands_f64[static_cast<std::size_t>(d) * w + j];
+            }
+        } else {
+            f[1] = 1.0;
+        }
+        const long long head = static_cast<long long>(static_cast<std::uint32_t>(start))
+            | (static_cast<long long>(count) << 32);
+        std::memcpy(&f[0], &head, sizeof(head));
+    }
+    out.eligible = true;
+    out.window = window;
+    out.forward_stride = 2 * fs;
+    out.backward_stride = 2 * bs;
     return out;
 }
 
