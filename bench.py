@@ -52,6 +52,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(value, dist, device):
+    """The largest `value` over the ranks (the slowest replica's time)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, world, steps, elapsed_ms):
+    """Units of all replicas per second in millions: every rank processes
+    `units_per_step` per step (weak scaling), the job takes the slowest
+    rank's time."""
+    return world * steps * units_per_step / (elapsed_ms / 1e3) / 1e6
+
+
 def link_bandwidth(h2d_bytes, d2h_bytes):
     """Host<->device copy bandwidth of pinned buffers of the step's sizes:
     each direction alone and both at once on two streams (the roofline of
@@ -849,12 +866,9 @@ def main():
     ktimes = ex.kernel_times()
     ex.profile(False)
     launches = ex.stats()["launches"] - launches0
-    t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
     pix_step = pixels_per_frame() * FRAMES
-    value = world * args.steps * pix_step / (elapsed_ms / 1e3) / 1e6
+    value = whole_job_rate(pix_step, world, args.steps, elapsed_ms)
 
     # End to end: the step's 192 host planes (pinned) through the pipelined
     # multi-plane host call of the C ABI (uploads, kernels and downloads of
