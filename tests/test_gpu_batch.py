@@ -174,3 +174,45 @@ def test_pipelined_host_planes_equal_single_calls(gb):
     with pytest.raises(gb.DescaleError):
         ex.inverse_2d_planes(planes[:2] + [(h, v, bad, out)])
     ex.close()
+
+
+@pytest.mark.gpu
+def test_pipelined_planes_in_one_ring(gb, executor):
+    """Planes packed back to back in one host buffer per direction travel in
+    merged copies; a pitched plane (row padding on the host) in the middle
+    and planes of odd byte sizes break the runs.  Every output equals the
+    per-plane call, and the ring's bytes between planes stay untouched."""
+    geoms = [(CHROMA_H, CHROMA_V), (SMALL_H, SMALL_V),
+             ((97, 67, 67.0, 0.1, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 0),
+              (73, 51, 51.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "reflect101", 0))]
+    plans = [(gb.AxisPlan(product_request(gb, hq), cached=False),
+              gb.AxisPlan(product_request(gb, vq), cached=False)) for hq, vq in geoms]
+    order = [0, 1, 2, 0, 0, 2, 1, 1, 0, 2]
+    pitched = 4
+    conv = gb.integer_conversion(16, True, False)
+    sizes_in = [plans[k][1].source_size * plans[k][0].source_size for k in order]
+    sizes_out = [plans[k][1].destination_size * plans[k][0].destination_size for k in order]
+    ring_in = np.zeros(sum(sizes_in) + 64, np.uint16)
+    ring_out = np.full(sum(sizes_out) + 64, 0xABCD, np.uint16)
+    planes, want = [], []
+    at_in = at_out = 0
+    for i, k in enumerate(order):
+        h, v = plans[k]
+        x = make_input(v.source_size, h.source_size, "u16", 900 + i)
+        if i == pitched:
+            # Row padding on both sides: a pitched copy between the runs.
+            xin = np.zeros((v.source_size, h.source_size + 5), np.uint16)[:, :h.source_size]
+            xout = np.zeros((v.destination_size, h.destination_size + 3), np.uint16)[:, :h.destination_size]
+            xin[...] = x
+        else:
+            xin = ring_in[at_in:at_in + x.size].reshape(x.shape)
+            xin[...] = x
+            xout = ring_out[at_out:at_out + sizes_out[i]].reshape(v.destination_size, h.destination_size)
+            at_in += x.size
+            at_out += sizes_out[i]
+        planes.append((h, v, xin, xout, conv))
+        want.append(executor.inverse_2d(h, v, x, conv))
+    executor.inverse_2d_planes(planes)
+    for (_h, _v, _x, out, _c), w in zip(planes, want):
+        assert np.array_equal(out, w)
+    assert np.all(ring_out[at_out:] == 0xABCD)

@@ -1089,10 +1089,12 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
     if (group_bytes == 0) group_bytes = impl_->pipe_group_bytes;
     auto in_row = [](const HostPlane &p) { return static_cast<std::size_t>(p.horizontal->source_size) * sample_bytes(p.sample); };
     auto out_row = [](const HostPlane &p) { return static_cast<std::size_t>(p.horizontal->destination_size) * sample_bytes(p.sample); };
-    auto plane_bytes = [&](const HostPlane &p) {
-        return align_up(in_row(p) * static_cast<std::size_t>(p.vertical->source_size))
-            + align_up(out_row(p) * static_cast<std::size_t>(p.vertical->destination_size));
+    auto in_bytes = [&](const HostPlane &p) { return in_row(p) * static_cast<std::size_t>(p.vertical->source_size); };
+    auto out_bytes = [&](const HostPlane &p) {
+        return out_row(p) * static_cast<std::size_t>(p.vertical->destination_size);
     };
+    auto pack = [](std::size_t v) { return (v + 15) / 16 * 16; };
+    auto plane_bytes = [&](const HostPlane &p) { return pack(in_bytes(p)) + pack(out_bytes(p)); };
     // Groups of consecutive planes within the byte target (at least one).
     std::vector<std::pair<std::size_t, std::size_t>> groups;   // [first, last)
     std::size_t most = 0;
@@ -1107,26 +1109,57 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
     std::scoped_lock pipe_lock(impl_->pipe_mutex);
     for (auto &ws : impl_->pipe) {
         if (!ws) ws = std::make_unique<Workspace>(nullptr);
-        ws->staging.reserve(most);
+        ws->staging.reserve(most + kAlign);
     }
+    // A group's staging holds its inputs back to back, then its outputs back
+    // to back, each at a 16-byte boundary.  Planes whose rows are contiguous
+    // on the host and whose host buffers follow one another exactly (a frame
+    // ring in one allocation) travel in one copy per direction.
+    struct Run {
+        char *host = nullptr, *dev = nullptr;
+        std::size_t bytes = 0;
+    };
+    auto flush = [](Run &r, cudaMemcpyKind kind, cudaStream_t s, const char *what) {
+        if (r.bytes == 0) return;
+        const bool up = kind == cudaMemcpyHostToDevice;
+        cuda_check(cudaMemcpyAsync(up ? static_cast<void *>(r.dev) : static_cast<void *>(r.host),
+                                   up ? static_cast<const void *>(r.host) : static_cast<const void *>(r.dev),
+                                   r.bytes, kind, s), what);
+        r = Run{};
+    };
+    auto extend = [&](Run &r, const void *host, char *dev, std::size_t bytes, cudaMemcpyKind kind,
+                      cudaStream_t s, const char *what) {
+        char *h = static_cast<char *>(const_cast<void *>(host));
+        if (r.bytes && (r.host + r.bytes != h || r.dev + r.bytes != dev)) flush(r, kind, s, what);
+        if (r.bytes == 0) {
+            r.host = h;
+            r.dev = dev;
+        }
+        r.bytes += bytes;
+    };
     std::size_t used = 0;
     try {
         for (std::size_t g = 0; g < groups.size(); ++g) {
             Workspace &ws = *impl_->pipe[g % impl_->pipe.size()];
             used = std::max(used, g % impl_->pipe.size() + 1);
-            char *at = ws.staging.data();
+            std::size_t in_total = 0;
+            for (std::size_t i = groups[g].first; i < groups[g].second; ++i) in_total += pack(in_bytes(planes[i]));
+            char *din = ws.staging.data();
+            char *dout = din + in_total;
             std::vector<PlaneTask> tasks;
             std::vector<char *> outs;
+            Run run;
             for (std::size_t i = groups[g].first; i < groups[g].second; ++i) {
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
-                char *din = at;
-                at += align_up(in_row(p) * static_cast<std::size_t>(p.vertical->source_size));
-                char *dout = at;
-                at += align_up(out_row(p) * static_cast<std::size_t>(p.vertical->destination_size));
-                cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
-                                             p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
-                           "uploading plane");
+                if (static_cast<std::size_t>(p.input_stride) * es == in_row(p)) {
+                    extend(run, p.input, din, in_bytes(p), cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                } else {
+                    flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                    cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
+                                          p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
+                               "uploading plane");
+                }
                 PlaneTask t;
                 t.horizontal = p.horizontal;
                 t.vertical = p.vertical;
@@ -1140,15 +1173,25 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
                 t.conversion = p.conversion;
                 tasks.push_back(t);
                 outs.push_back(dout);
+                din += pack(in_bytes(p));
+                dout += pack(out_bytes(p));
             }
+            flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
             impl_->enqueue(ws, tasks);
             for (std::size_t i = groups[g].first, k = 0; i < groups[g].second; ++i, ++k) {
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
-                cuda_check(copy_plane(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
-                                             p.vertical->destination_size, cudaMemcpyDeviceToHost, ws.stream),
-                           "downloading plane");
+                if (static_cast<std::size_t>(p.output_stride) * es == out_row(p)) {
+                    extend(run, p.output, outs[k], out_bytes(p), cudaMemcpyDeviceToHost, ws.stream,
+                           "downloading planes");
+                } else {
+                    flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
+                    cuda_check(copy_plane(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
+                                          p.vertical->destination_size, cudaMemcpyDeviceToHost, ws.stream),
+                               "downloading plane");
+                }
             }
+            flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
         }
         for (std::size_t k = 0; k < used; ++k) impl_->finish(*impl_->pipe[k]);
     } catch (...) {
