@@ -191,6 +191,8 @@ typedef struct dsmvc_gb_stream_info {
     char reason[96];             /* why not eligible */
     int32_t ring_ok_transposed;  /* the 2D passes' warp-wide block feed fits */
     int32_t exact;               /* two-pass transposing kernels admitted */
+    int32_t segmentable;         /* 2D passes may split vectors into segments */
+    double forward_transfer;     /* history influence after one chunk */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,

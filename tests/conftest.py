@@ -38,18 +38,22 @@ def executor(gb):
     ex.close()
 
 
-def _executor_with(gb, name, value="0"):
+def _executor_with(gb, name, value="0", **more):
+    """An executor created under environment settings (name=value and
+    `more`), restored afterwards."""
     if not gb.cuda_available():
         pytest.skip("no CUDA device")
-    old = os.environ.get(name)
-    os.environ[name] = value
+    settings = {name: value, **more}
+    old = {k: os.environ.get(k) for k in settings}
+    os.environ.update(settings)
     try:
         return gb.Executor(0)
     finally:
-        if old is None:
-            del os.environ[name]
-        else:
-            os.environ[name] = old
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
 
 
 @pytest.fixture(scope="session")
@@ -74,5 +78,15 @@ def paired_executor(gb):
     """An executor whose admitted 2D planes use the paired transposing
     kernels (DSMVC_GB_PAIRED=1)."""
     ex = _executor_with(gb, "DSMVC_GB_PAIRED", "1")
+    yield ex
+    ex.close()
+
+
+@pytest.fixture(scope="session")
+def whole_executor(gb):
+    """An executor that never splits vectors into segments
+    (DSMVC_GB_SEGMENTS=1): its results do not depend on what else shares a
+    launch, so batched and single calls agree bit for bit."""
+    ex = _executor_with(gb, "DSMVC_GB_SEGMENTS", "1")
     yield ex
     ex.close()

@@ -142,16 +142,10 @@ def test_pipelined_host_planes_equal_single_calls(gb):
     """dsmvc_gb_inverse_2d_planes: many host planes pipelined through three
     streams in groups (1 MiB groups here, so most planes are in different
     groups) give exactly the per-plane calls' samples."""
-    import os
-    old = os.environ.get("DSMVC_GB_PIPELINE_MB")
-    os.environ["DSMVC_GB_PIPELINE_MB"] = "1"
-    try:
-        ex = gb.Executor(0)
-    finally:
-        if old is None:
-            del os.environ["DSMVC_GB_PIPELINE_MB"]
-        else:
-            os.environ["DSMVC_GB_PIPELINE_MB"] = old
+    from conftest import _executor_with
+    # Whole vectors (no segments), so that groups and single calls run the
+    # same arithmetic.
+    ex = _executor_with(gb, "DSMVC_GB_PIPELINE_MB", "1", DSMVC_GB_SEGMENTS="1")
     geoms = [(CHROMA_H, CHROMA_V, "u16"), (SMALL_H, SMALL_V, "f32"),
              ((97, 67, 67.0, 0.1, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 2),
               (73, 51, 51.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "reflect101", 2), "f32")]
@@ -177,7 +171,7 @@ def test_pipelined_host_planes_equal_single_calls(gb):
 
 
 @pytest.mark.gpu
-def test_pipelined_planes_in_one_ring(gb, executor):
+def test_pipelined_planes_in_one_ring(gb, whole_executor):
     """Planes packed back to back in one host buffer per direction travel in
     merged copies; a pitched plane (row padding on the host) in the middle
     and planes of odd byte sizes break the runs.  Every output equals the
@@ -194,6 +188,7 @@ def test_pipelined_planes_in_one_ring(gb, executor):
     sizes_out = [plans[k][1].destination_size * plans[k][0].destination_size for k in order]
     ring_in = np.zeros(sum(sizes_in) + 64, np.uint16)
     ring_out = np.full(sum(sizes_out) + 64, 0xABCD, np.uint16)
+    executor = whole_executor
     planes, want = [], []
     at_in = at_out = 0
     for i, k in enumerate(order):

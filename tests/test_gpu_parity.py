@@ -119,13 +119,17 @@ RANDOM_2D = _random_geometries(28, 99)
 
 
 @pytest.mark.parametrize("hq,vq", RANDOM_2D, ids=[f"g{i}" for i in range(len(RANDOM_2D))])
-def test_2d_random_geometries(gb, executor, paired_executor, hq, vq):
+def test_2d_random_geometries(gb, executor, whole_executor, paired_executor, hq, vq):
+    """Random geometries: the default executor (which splits a lone plane's
+    vectors into segments where admitted) within the reference tolerance of
+    the CPU scalar route; whole vectors on the unpaired and the paired
+    kernels bit for bit alike."""
     h, oh = plans(gb, executor, hq)
     v, ov = plans(gb, executor, vq)
     x = image(v.source_size, h.source_size, 11)
     scalar = O.inverse_2d(oh, ov, x)
     got = executor.inverse_2d(h, v, x)
-    assert np.array_equal(got, paired_executor.inverse_2d(h, v, x))
+    assert np.array_equal(whole_executor.inverse_2d(h, v, x), paired_executor.inverse_2d(h, v, x))
     err = np.abs(got.astype(np.float64) - scalar)
     assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS, (hq, vq, err.max())
     xi = make_input(v.source_size, h.source_size, "u16", 12)
@@ -253,11 +257,12 @@ FULL = [
 
 
 @pytest.mark.parametrize("name,hq,vq,sample", FULL, ids=[c[0] for c in FULL])
-def test_full_size_frames_use_streaming_kernels(gb, executor, paired_executor, name, hq, vq, sample):
+def test_full_size_frames_use_streaming_kernels(gb, executor, whole_executor, paired_executor, name, hq, vq,
+                                                sample):
     """Full-size frames of the benchmark configurations: the paired
     streaming kernels run (profiled kernel names), give the same samples as
-    the unpaired ones, and agree with the CPU scalar route within the
-    reference tolerance."""
+    the unpaired ones on whole vectors, and the default executor (segments)
+    agrees with the CPU scalar route within the reference tolerance."""
     h, oh = plans(gb, executor, hq)
     v, ov = plans(gb, executor, vq)
     assert h.stream_info()["eligible"] and v.stream_info()["eligible"]
@@ -276,7 +281,7 @@ def test_full_size_frames_use_streaming_kernels(gb, executor, paired_executor, n
     paired_executor.profile(False)
     assert any(n.startswith("tstream2_f32/rows") for n in names), names
     assert any(n.startswith("tstream2_f32/columns") for n in names), names
-    assert np.array_equal(got, paired)
+    assert np.array_equal(whole_executor.inverse_2d(h, v, x, conv), paired)
     scalar = O.inverse_2d(oh, ov, x, conv)
     if sample == "f32":
         err = np.abs(got.astype(np.float64) - scalar)
@@ -327,7 +332,10 @@ def test_float64_nonfinite_input_raises(gb, executor):
     assert np.all(np.isfinite(y))
 
 
-def test_device_batch_matches_host_calls(gb, executor):
+def test_device_batch_matches_host_calls(gb, whole_executor):
+    """Whole vectors: a device batch gives the host calls' samples bit for
+    bit (with segments, the split depends on the launch's size)."""
+    executor = whole_executor
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(21)
     tasks, expect, keep = [], [], []

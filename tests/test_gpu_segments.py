@@ -1,0 +1,71 @@
+"""Segments of the chunk-delayed transposing passes: a plane's vectors split
+into ranges of whole chunks served by different warps, each range's
+forward substitution started one chunk early from a zero history.
+
+Bars: against whole vectors, Float32 samples within 4e-7 of the largest
+output magnitude and integer samples within 1 code; against the CPU scalar
+route, the reference tolerance (max-abs 2e-5, mean-abs 1e-6; 1 code)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from common import F32_MAX_ABS, F32_MEAN_ABS, INT_MAX_CODES, make_input, oracle_request, product_request
+from conftest import _executor_with
+
+pytestmark = pytest.mark.gpu
+
+GEOMS = [
+    ("c1-luma-u16", (1920, 1440, 1440.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0),
+     (1080, 810, 810.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), "u16"),
+    ("c0-bicubic-f32", (1920, 1280, 1280.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1),
+     (1080, 720, 720.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "symmetric", 1), "f32"),
+    ("odd-bilinear-u8", (333, 217, 216.5, 0.25, "bilinear", 3, 0, 0.5, 1.0, "zero", 0),
+     (301, 200, 199.75, -0.3, "bilinear", 3, 0, 0.5, 1.0, "mirror", 0), "u8"),
+    ("spline36-tail-f32", (600, 449, 449.0, 0.1, "spline36", 3, 0, 0.5, 1.0, "reflect101", 0),
+     (500, 417, 417.0, 0.0, "spline36", 3, 0, 0.5, 1.0, "symmetric", 0), "f32"),
+]
+
+
+@pytest.fixture(scope="module", params=[2, 3, 7])
+def forced(gb, request):
+    ex = _executor_with(gb, "DSMVC_GB_SEGMENTS", str(request.param))
+    yield ex
+    ex.close()
+
+
+@pytest.mark.parametrize("name,hq,vq,sample", GEOMS, ids=[g[0] for g in GEOMS])
+def test_segments_match_whole_vectors(gb, forced, whole_executor, name, hq, vq, sample):
+    h = gb.AxisPlan(product_request(gb, hq), cached=False)
+    v = gb.AxisPlan(product_request(gb, vq), cached=False)
+    assert h.stream_info()["segmentable"] and v.stream_info()["segmentable"]
+    x = make_input(v.source_size, h.source_size, sample, 77)
+    conv = gb.integer_conversion(8 if sample == "u8" else 16, False, False) if sample != "f32" else None
+    got = forced.inverse_2d(h, v, x, conv)
+    whole = whole_executor.inverse_2d(h, v, x, conv)
+    scalar = O.inverse_2d(O.Plan(oracle_request(hq)), O.Plan(oracle_request(vq)), x, conv)
+    if sample == "f32":
+        assert np.abs(got - whole).max() <= 4e-7 * max(1.0, float(np.abs(whole).max()))
+        err = np.abs(got.astype(np.float64) - scalar)
+        assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+    else:
+        assert np.abs(got.astype(np.int64) - whole.astype(np.int64)).max() <= 1
+        assert np.abs(got.astype(np.int64) - scalar.astype(np.int64)).max() <= INT_MAX_CODES
+
+
+def test_segments_are_launched(gb, forced, whole_executor):
+    """The forced split multiplies the chunk-delayed jobs (the job table
+    grows); the automatic one splits a lone plane and keeps a large batch
+    whole."""
+    torch = pytest.importorskip("torch")
+    _name, hq, vq, _s = GEOMS[1]
+    h = gb.AxisPlan(product_request(gb, hq), cached=False)
+    v = gb.AxisPlan(product_request(gb, vq), cached=False)
+    dx = torch.zeros((v.source_size, h.source_size), dtype=torch.float32, device="cuda")
+    dy = torch.zeros((v.destination_size, h.destination_size), dtype=torch.float32, device="cuda")
+    task = gb.PlaneTask(h, v, dx.data_ptr(), h.source_size, dy.data_ptr(), h.destination_size, 0, 0, None)
+    sizes = {}
+    for label, ex in (("forced", forced), ("whole", whole_executor)):
+        b = ex.prepare_batch([task])
+        sizes[label] = b.info()["table_bytes"]
+        b.close()
+    assert sizes["forced"] > sizes["whole"]

@@ -126,3 +126,100 @@ def test_record_layout(gb):
             assert rec[4 + K + q] == (-lower[d - 1, j] if d <= j else 0.0)
             du = q + 1  # half-bandwidth 3: ascending
             assert info["backward"][j, q] == (upper[du - 1, j] if du <= min(hb, p.destination_size - j - 1) else 0.0)
+
+
+def forward_transfer(p, chunk):
+    """Largest state left by a unit history pushed through one chunk's
+    homogeneous forward recurrence (chunks 1 .. chunks-2), in float64."""
+    n, hb = p.destination_size, p.half_bandwidth
+    lower = p.array("lower_ld").astype(np.float64).reshape(hb, n)
+    inv = p.array("inverse_diagonal").astype(np.float64)
+    chunks = (n + chunk - 1) // chunk
+    worst = 0.0
+    for k in range(1, chunks - 1):
+        lo = k * chunk
+        for e in range(hb):
+            y = {lo - 1 - e: 1.0}
+            for t in range(lo, lo + chunk):
+                y[t] = -inv[t] * sum(lower[d - 1, t] * y.get(t - d, 0.0) for d in range(1, min(hb, t) + 1))
+            worst = max(worst, max(abs(y[lo + chunk - 1 - q]) for q in range(hb)))
+    return worst
+
+
+def emulate_segment(info, plan, x, ca, cb):
+    """Chunks [ca, cb) of the kernel's segment algorithm: forward from chunk
+    ca - 1 with a zero history, stored backward passes over [ca, cb) with the
+    warm-up of chunk cb (or the exact end of the vector)."""
+    fwd, bwd = info["forward"], info["backward"]
+    K, hb, n, LC = info["window"], plan.half_bandwidth, plan.destination_size, info["chunk"]
+    chunks = (n + LC - 1) // LC
+    V = x.shape[0]
+    c0 = max(ca - 1, 0)
+    ce = cb if cb < chunks else chunks - 1
+    y = {}
+    for j in range(c0 * LC, min((ce + 1) * LC, n)):
+        rec = fwd[j]
+        s0 = int(rec[:1].view(np.int32)[0])
+        s = np.zeros(V, np.float32)
+        for k in range(K):
+            s = fma32(rec[4 + k], x[:, s0 + k], s)
+        for q in range(hb):
+            d = hb - q
+            s = fma32(rec[4 + K + q], y.get(j - d, np.zeros(V, np.float32)), s)
+        y[j] = s * rec[1]
+
+    def back(lo, hi, carry):
+        xs = {hi + e: carry[e] for e in range(hb)}
+        for j in range(hi - 1, lo - 1, -1):
+            if j >= n:
+                xs[j] = np.zeros(V, np.float32)
+                continue
+            s = np.zeros(V, np.float32)
+            for q in range(hb):
+                d = q + 1 if hb == 3 else hb - q
+                s = fma32(bwd[j, q], xs.get(j + d, np.zeros(V, np.float32)), s)
+            xs[j] = (y[j] - s).astype(np.float32)
+        return xs
+
+    zero = [np.zeros(V, np.float32)] * hb
+    res = {}
+    for c in range(ca, cb):
+        lo, hi = c * LC, (c + 1) * LC
+        if c + 1 == chunks:
+            carry = zero
+        else:
+            nxt = back(hi, hi + LC, zero)
+            carry = [nxt[hi + e] for e in range(hb)]
+        xs = back(lo, hi, carry)
+        for j in range(lo, min(hi, n)):
+            res[j] = xs[j]
+    return res
+
+
+@pytest.mark.parametrize("name,req,eligible", CASES[:6], ids=[c[0] for c in CASES[:6]])
+def test_segment_admission_and_emulation(gb, name, req, eligible):
+    """The forward warm-up check equals a float64 restatement, and segments
+    computed as the kernels do (zero history one chunk early, stored
+    backward passes over whole chunks) agree with the oracle like the
+    unsegmented passes."""
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info(records=True)
+    want_ft = forward_transfer(p, info["chunk"])
+    assert info["forward_transfer"] == pytest.approx(want_ft, rel=1e-9, abs=1e-300)
+    assert bool(info["segmentable"]) == bool(info["eligible"] and info["ring_ok_transposed"]
+                                             and want_ft <= 2.0 ** -26)
+    chunks = (p.destination_size + info["chunk"] - 1) // info["chunk"]
+    if not info["segmentable"] or chunks < 4:
+        return
+    o = O.Plan(oracle_request(req))
+    rng = np.random.default_rng(4)
+    x = rng.random((3, p.source_size), dtype=np.float32)
+    want = np.stack([o.inverse_axis_f32_gpu(r) for r in x])
+    scale = float(np.max(np.abs(want)))
+    whole = emulate(info, o, x)
+    bounds = [0, 1, chunks // 2, chunks - 1, chunks]
+    for ca, cb in zip(bounds, bounds[1:]):
+        seg = emulate_segment(info, o, x, ca, cb)
+        for j, v in seg.items():
+            assert np.max(np.abs(v - want[:, j])) <= 4e-7 * scale
+            assert np.max(np.abs(v - whole[:, j])) <= 2e-7 * scale

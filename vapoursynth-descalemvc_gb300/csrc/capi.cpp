@@ -253,6 +253,8 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->ring_ok_u8 = pack.ring_ok_u8 ? 1 : 0;
         info->ring_ok_transposed = pack.ring_ok_transposed ? 1 : 0;
         info->exact = pack.exact ? 1 : 0;
+        info->segmentable = pack.segmentable ? 1 : 0;
+        info->forward_transfer = pack.forward_transfer;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;
         info->backward_transfer = pack.backward_transfer;

@@ -94,6 +94,10 @@ struct DevicePlan {
     dev::StreamPlanView stream_view{};
     bool stream_p = false;          // paired transposing 2D kernels admitted
     dev::StreamPlanView stream_view2{};
+    // Chunk-delayed transposing passes may split vectors into segments
+    // (stream_plan.hpp); the ring's first block of each chunk.
+    bool stream_seg = false;
+    std::vector<int> chunk_first_block;
     std::size_t bytes = 0;
 };
 
@@ -160,6 +164,8 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         dp->stream_u16 = pack.eligible && pack.ring_ok_u16;
         dp->stream_u8 = pack.eligible && pack.ring_ok_u8;
         dp->stream_t = pack.eligible && pack.ring_ok_transposed;
+        dp->stream_seg = dp->stream_t && pack.segmentable;
+        if (dp->stream_seg) dp->chunk_first_block = pack.chunk_first_block;
         dp->stream_x = pack.exact;
         dp->stream_xg = pack.exact && pack.ring_ok_transposed && pack.window == 8;
         auto &sv = dp->stream_view;
@@ -345,6 +351,13 @@ struct Executor::Impl {
     // Default CTA size of the transposing kernels (DSMVC_GB_TSTREAM_THREADS,
     // 32..256 in multiples of 32); batches may tune it per launch group.
     int tstream_threads = kTStreamThreads;
+    // Segments of the chunk-delayed transposing passes (DSMVC_GB_SEGMENTS):
+    // 0 automatic (a launch group whose warps leave the GPU's resident warp
+    // slots unfilled splits its vectors into up to slots / warps ranges of
+    // at least kMinSegmentChunks chunks), 1 never, N >= 2 exactly N per job
+    // where admitted and long enough.
+    int segment_mode = 0;
+    int warp_slots = 0;      // SMs x resident warps of the transposing kernels
     std::vector<Record> records;
 
     // Prepared plans first, then the cache (plans with owners), else a
@@ -504,6 +517,53 @@ std::string kernel_name(const GroupKey &k) {
 
 } // namespace
 
+namespace {
+
+// Jobs of a chunk-delayed transposing launch group (sorted by plan), split
+// into segments of whole chunks.  Automatic mode: when the group's warps fill
+// fewer than `slots` resident warp slots, up to slots / warps segments per
+// job; each segment spans at least kMinSegmentChunks chunks, and only plans
+// whose forward warm-up is admitted split.  Per plan, the jobs come segment
+// by segment, so that only plan and segment changes round up to whole CTAs.
+template <class Item>
+std::vector<Item> segment_items(const std::vector<Item> &items, int vectors_per_warp, int mode, int slots) {
+    if (mode == 1) return items;
+    int segments = mode;
+    if (mode == 0) {
+        long warps = 0;
+        for (const auto &it : items) warps += (it.stream.vectors + vectors_per_warp - 1) / vectors_per_warp;
+        if (warps <= 0 || slots <= 0) return items;
+        segments = static_cast<int>(std::min<long>(slots / warps, 64));
+        if (segments < 2) return items;
+    }
+    std::vector<Item> out;
+    out.reserve(items.size());
+    for (std::size_t i = 0; i < items.size();) {
+        std::size_t j = i;
+        while (j < items.size() && items[j].stream.plan.forward == items[i].stream.plan.forward) ++j;
+        const DevicePlan *dp = items[i].plan;
+        const int chunks = (items[i].stream.plan.destination_size + kStreamChunk - 1) / kStreamChunk;
+        const int s = dp && dp->stream_seg ? std::max(1, std::min(segments, chunks / kMinSegmentChunks)) : 1;
+        for (int k = 0; k < s; ++k) {
+            const int begin = static_cast<int>(static_cast<long>(k) * chunks / s);
+            const int end = static_cast<int>(static_cast<long>(k + 1) * chunks / s);
+            for (std::size_t q = i; q < j; ++q) {
+                Item it = items[q];
+                if (s > 1) {
+                    it.stream.chunk_begin = begin;
+                    it.stream.chunk_end = end;
+                    it.stream.first_sample = begin > 0 ? dp->chunk_first_block[static_cast<std::size_t>(begin - 1)] : 0;
+                }
+                out.push_back(it);
+            }
+        }
+        i = j;
+    }
+    return out;
+}
+
+} // namespace
+
 void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                              const std::function<char *(std::size_t)> &scratch, const Tuning *tuning) {
     auto &temporaries = out.temporaries;
@@ -591,6 +651,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         dev::AxisJob axis{};
         dev::StreamJob stream{};
         std::uint64_t bytes = 0;
+        const DevicePlan *plan = nullptr;   // chunk-delayed transposing passes
     };
     std::map<GroupKey, std::vector<Item>> groups;
     for (std::size_t t = 0; t < tasks.size(); ++t) {
@@ -640,6 +701,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.y = mid; j.y_elem = pitch;                // forward values in place
                 j.vectors = v->source_size;
                 j.conv = conv;
+                hi.plan = r.h;
                 groups[{0, r.h_kind, h->half_bandwidth, task.sample, dev::Sample::f32,
                         compiled_window(*r.h, r.h_kind)}].push_back(hi);
             } else {
@@ -666,6 +728,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 }
                 j.vectors = h->destination_size;
                 j.conv = conv;
+                vi.plan = r.v;
                 groups[{1, r.v_kind, v->half_bandwidth, dev::Sample::f32, task.sample,
                         compiled_window(*r.v, r.v_kind)}].push_back(vi);
             } else {
@@ -784,15 +847,18 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) {
                 return a.stream.plan.forward < b.stream.plan.forward;
             });
+        if (key.kind == 3) items = segment_items(items, vectors_per_warp, segment_mode, warp_slots);
         int warps = 0;
         const float *run_plan = nullptr;
+        int run_chunk = 0;
         for (auto &it : items) {
             const int vectors = is_stream ? it.stream.vectors : it.axis.vectors;
             if (vectors <= 0) continue;
             if (by_warp) {
-                if (warps && it.stream.plan.forward != run_plan)
+                if (warps && (it.stream.plan.forward != run_plan || it.stream.chunk_begin != run_chunk))
                     warps = (warps + warps_per_cta - 1) / warps_per_cta * warps_per_cta;
                 run_plan = it.stream.plan.forward;
+                run_chunk = it.stream.chunk_begin;
                 it.stream.first_block = warps;     // first warp of the job
                 warps += (vectors + vectors_per_warp - 1) / vectors_per_warp;
                 blocks = (warps + warps_per_cta - 1) / warps_per_cta;
@@ -923,6 +989,16 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);
         if (end && *end == '\0' && v >= 32 && v <= 256 && v % 32 == 0) impl_->tstream_threads = static_cast<int>(v);
+    }
+    if (const char *env = std::getenv("DSMVC_GB_SEGMENTS")) {
+        char *end = nullptr;
+        const long v = std::strtol(env, &end, 10);
+        if (end && *end == '\0' && v >= 0 && v <= 1024) impl_->segment_mode = static_cast<int>(v);
+    }
+    {
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "querying SMs");
+        impl_->warp_slots = sms * kTResidentWarps;
     }
     if (const char *env = std::getenv("DSMVC_GB_PLAN_CACHE_MB")) {
         char *end = nullptr;

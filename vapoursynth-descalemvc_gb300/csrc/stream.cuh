@@ -42,6 +42,18 @@ struct StreamJob {
     // out like `out` (destination j of vector v at y[j * y_elem + v]).
     float *y;
     std::int64_t y_elem;
+    // Chunk-delayed transposing kernels: the job's destinations are chunks
+    // [chunk_begin, chunk_end) of its vectors (chunk_end 0: all of them).
+    // A job starting past chunk 0 runs its forward substitution from chunk
+    // chunk_begin - 1 with a zero history, its ring from sample first_sample
+    // (a multiple of 16, at most that chunk's first window start), and stores
+    // nothing of that chunk; one ending before the last chunk also runs the
+    // forward substitution and backward warm-up of chunk chunk_end.  Every
+    // warp of a CTA serves the same plan and chunk range.
+    std::int32_t chunk_begin;
+    std::int32_t chunk_end;
+    std::int32_t first_sample;
+    std::int32_t reserved;
 };
 
 } // namespace dsmvc_gb::dev
@@ -65,6 +77,8 @@ constexpr int kPairedRingPitch = 66;
 // launch has the same window when window == 8 (unrolled gather).  `threads`
 // per CTA: 32..256, a multiple of 32 (one warp per 32 vectors).
 constexpr int kTStreamThreads = 128;   // default CTA size
+constexpr int kTResidentWarps = 16;    // resident warps per SM (128 registers a thread)
+constexpr int kMinSegmentChunks = 2;   // shortest segment, in chunks (StreamJob)
 int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
                    int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
                    void *stream);

@@ -118,6 +118,29 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
     out.backward_transfer = worst;
     if (out.reason.empty() && !(worst <= std::ldexp(1.0, -26)))
         out.reason = "backward carry decays too slowly for one chunk";
+
+    // Forward warm-up accuracy for segments: a unit history entering chunk k
+    // (y_{lo-1-e} = 1), pushed through the chunk's homogeneous forward
+    // recurrence y_t = -inv_t * sum_d lower_ld(d, t) y_{t-d}, must vanish.
+    // Chunk 0 needs no check (its history is the true, empty one).
+    double fworst = 0.0;
+    for (int k = 1; k + 1 < chunks; ++k) {
+        const int lo = k * chunk, hi = lo + chunk;
+        for (int e = 0; e < hb; ++e) {
+            std::fill(x.begin(), x.end(), 0.0);
+            x[static_cast<std::size_t>(hb - 1 - e)] = 1.0;  // x[i] holds y_{lo - hb + i}
+            for (int t = lo; t < hi; ++t) {
+                double s = 0.0;
+                for (int d = 1; d <= hb && d <= t; ++d)
+                    s += static_cast<double>(p.lower_ld[static_cast<std::size_t>(d - 1) * w + static_cast<std::size_t>(t)])
+                        * x[static_cast<std::size_t>(t - d - lo + hb)];
+                x[static_cast<std::size_t>(t - lo + hb)] = -s * static_cast<double>(p.inverse_diagonal[static_cast<std::size_t>(t)]);
+            }
+            for (int q = 0; q < hb; ++q)
+                fworst = std::max(fworst, std::abs(x[static_cast<std::size_t>(chunk + q)]));
+        }
+    }
+    out.forward_transfer = fworst;
     const bool delayed = out.reason.empty();
     if (!delayed && !out.exact) return out;
 
@@ -163,6 +186,9 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
         }
     }
     out.eligible = delayed;
+    out.segmentable = delayed && out.ring_ok_transposed && fworst <= std::ldexp(1.0, -26);
+    out.chunk_first_block.resize(static_cast<std::size_t>(chunks));
+    for (int k = 0; k < chunks; ++k) out.chunk_first_block[static_cast<std::size_t>(k)] = s0[static_cast<std::size_t>(k) * chunk] / 16 * 16;
 
     if (delayed && out.ring_ok_transposed && window <= 16) {
         const int pl = round4(2 * hb);

@@ -26,6 +26,16 @@ struct StreamPack {
     // The transposing 2D kernels' warp-wide block feeding fits the ring.
     bool ring_ok_transposed = false;
     double backward_transfer = 0.0; // max |carry -> state| over one chunk
+    // Segments: a transposing 2D pass may split its vectors' destinations
+    // into ranges of whole chunks served by different warps, each starting
+    // its forward substitution from a zero history one chunk early.  Admitted
+    // when that warm-up leaves a history influence below 2^-26 per slot
+    // (every chunk that can serve as warm-up, computed in double).
+    bool segmentable = false;
+    double forward_transfer = 0.0;  // max |history -> state| over one chunk
+    // Window start of each chunk's first destination, rounded down to the
+    // 16-sample feeding block: where a segment's warm-up starts its ring.
+    std::vector<int> chunk_first_block;
     // Records of ceil(destination_size / chunk) * chunk destinations (zero
     // records past the end).
     std::vector<float> forward;     // * forward_stride

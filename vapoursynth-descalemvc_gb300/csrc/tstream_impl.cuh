@@ -126,8 +126,9 @@ struct WarpFeeder {
         }
     }
 
-    __device__ __forceinline__ void start() {
-        have = 0;
+    // `first`: a multiple of 16 at most the first window start.
+    __device__ __forceinline__ void start(int first = 0) {
+        have = first;
         issue();
     }
 
@@ -311,12 +312,23 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     extern __shared__ __align__(16) float smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthreads = static_cast<int>(blockDim.x);
-    // Jobs are assigned warps; a CTA's warps share one plan (the host rounds
-    // plan changes up to whole CTAs), whose records the CTA copies once.
+    // Jobs are assigned warps; a CTA's warps share one plan and one chunk
+    // range (the host rounds changes of either up to whole CTAs), whose
+    // records the CTA copies once.
     const int cta_warp = static_cast<int>(blockIdx.x) * (nthreads >> 5);
     const StreamJob &job = jobs[find_tjob(jobs, job_count, cta_warp + warp)];
-    const dev::StreamPlanView p = jobs[find_tjob(jobs, job_count, cta_warp)].plan;
+    const StreamJob &lead = jobs[find_tjob(jobs, job_count, cta_warp)];
+    const dev::StreamPlanView p = lead.plan;
     const int n = p.destination_size;
+    const int chunks = (n + LC - 1) / LC;
+    // Chunks whose outputs this CTA stores: [ca, cb).  The forward
+    // substitution runs over [c0, ce]: from one chunk early (zero history)
+    // for a range past chunk 0, to one chunk late (the backward warm-up of
+    // the last stored chunk) for a range ending before the last chunk.
+    const int ca = lead.chunk_begin;
+    const int cb = lead.chunk_end > 0 ? lead.chunk_end : chunks;
+    const int c0 = ca > 0 ? ca - 1 : 0;
+    const int ce = cb < chunks ? cb : chunks - 1;
     const int per_buffer = kTChunk * record_floats;
     float *bufs = smem;
     float *ring = smem + 3 * per_buffer + warp * kTRingFloats;
@@ -344,45 +356,46 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
-    if (!idle) feed.start();
+    if (!idle) feed.start(c0 > 0 ? lead.first_sample : 0);
 
     Out *out = static_cast<Out *>(job.out) + (warp_first + (lane < warp_vectors ? lane : 0));
 
-    const int chunks = (n + LC - 1) / LC;
-    tstage(bufs, p, 0, tid, nthreads);
+    tstage(bufs + (c0 % 3) * per_buffer, p, c0, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid, nthreads);
+    if (c0 + 1 <= ce) tstage(bufs + ((c0 + 1) % 3) * per_buffer, p, c0 + 1, tid, nthreads);
     tcp_commit();
 
     float y[2 * LC];
     float carry[HB];
 #pragma unroll
     for (int t = 0; t < LC; ++t) y[t] = 0.0f;
-    for (int c = 0; c < chunks; ++c) {
+    for (int c = c0;; ++c) {
         tcp_wait_one();
         __syncthreads();
         const float *cur = bufs + (c % 3) * per_buffer;
         const float *prev = bufs + ((c + 2) % 3) * per_buffer;
-        const bool last = c + 1 == chunks;
         if (!idle) {
             tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
             const float *cur_b = cur + kTChunk * fwd_stride<HB, K>(p);
-            if (last) {
+            if (c + 1 == chunks) {
+                // The vector's last chunk: exact backward substitution from
+                // the end, stored when the chunk is the CTA's.
 #pragma unroll
                 for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
-                tbackward<HB, LC, K, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active, job.conv);
-            } else {
+                tbackward<HB, LC, K, LC>(y, carry, c * LC, p, cur_b, out, job.out_elem, active && c < cb,
+                                         job.conv);
+            } else if (c > ca) {
                 twarmup<HB, LC, K>(y, carry, p, cur_b);
             }
-            if (c > 0) {
+            if (c > ca) {
                 tbackward<HB, LC, K, 0>(y, carry, (c - 1) * LC, p, prev + kTChunk * fwd_stride<HB, K>(p), out,
                                         job.out_elem, active, job.conv);
             }
         }
-        if (last) break;
+        if (c == ce) break;
         // Every warp is done with chunk c-1's records: fetch chunk c+2.
         __syncthreads();
-        if (c + 2 < chunks) tstage(const_cast<float *>(prev), p, c + 2, tid, nthreads);
+        if (c + 2 <= ce) tstage(const_cast<float *>(prev), p, c + 2, tid, nthreads);
         tcp_commit();
 #pragma unroll
         for (int t = 0; t < LC; ++t) y[t] = y[LC + t];

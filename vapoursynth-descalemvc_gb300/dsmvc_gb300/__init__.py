@@ -87,7 +87,8 @@ class StreamInfoC(C.Structure):
                 ("ring_ok_u16", C.c_int32), ("ring_ok_u8", C.c_int32),
                 ("chunk", C.c_int32), ("ring", C.c_int32),
                 ("backward_transfer", C.c_double), ("reason", C.c_char * 96),
-                ("ring_ok_transposed", C.c_int32), ("exact", C.c_int32)]
+                ("ring_ok_transposed", C.c_int32), ("exact", C.c_int32),
+                ("segmentable", C.c_int32), ("forward_transfer", C.c_double)]
 
 
 class SweepOptionsC(C.Structure):
