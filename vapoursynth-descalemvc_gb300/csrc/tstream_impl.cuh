@@ -78,6 +78,21 @@ template <> __device__ __forceinline__ float tout<float>(float v, const Conversi
 
 __device__ __forceinline__ float4 tlds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
+// Predicated global stores of one output sample: no branch around the
+// store, and the address is known to be global.
+__device__ __forceinline__ void tst(float *p, float v, bool pred) {
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %2, 0;\n @q st.global.f32 [%0], %1;\n}\n"
+                 :: "l"(p), "f"(v), "r"(static_cast<int>(pred)));
+}
+__device__ __forceinline__ void tst(std::uint16_t *p, std::uint16_t v, bool pred) {
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %2, 0;\n @q st.global.u16 [%0], %1;\n}\n"
+                 :: "l"(p), "h"(v), "r"(static_cast<int>(pred)));
+}
+__device__ __forceinline__ void tst(std::uint8_t *p, std::uint8_t v, bool pred) {
+    asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %2, 0;\n @q st.global.u8 [%0], %1;\n}\n"
+                 :: "l"(p), "r"(static_cast<unsigned>(v)), "r"(static_cast<int>(pred)));
+}
+
 // Record strides (floats).  With a compile-time window they are constants,
 // so every record read is an immediate offset from the chunk's base.
 template <int HB, int K> __device__ __forceinline__ int fwd_stride(const dev::StreamPlanView &p) {
@@ -188,11 +203,9 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
     for (int t = 0; t < LC; ++t) {
         if (t % 4 == 0) {
             // Window end of the group's last destination: window starts
-            // never decrease, and records past the end of the vector repeat
-            // the last destination's start.
-            const int s_last = __float_as_int(fwd[(t + 3) * fs]);
-            const int need = max(s_last, __float_as_int(fwd[t * fs])) + kw;
-            feed.ensure(min(need, p.source_size));
+            // never decrease, records past the end of the vector repeat the
+            // last destination's start, and no window ends past the source.
+            feed.ensure(__float_as_int(fwd[(t + 3) * fs]) + kw);
         }
         const float *rec = fwd + t * fs;
         const float4 hdr = tlds4(rec);
@@ -231,7 +244,9 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
                 if (d >= 1) sum = fmaf(lv[e], y[LC + t - d], sum);
             }
         }
-        y[LC + t] = j0 + t < n ? sum * hdr.y : 0.0f;
+        // Records past the end of the vector are zero (inverse diagonal
+        // included), so their forward values are zero for finite data.
+        y[LC + t] = sum * hdr.y;
     }
 }
 
@@ -271,13 +286,16 @@ __device__ __forceinline__ void twarmup(const float (&y)[2 * LC], float (&carry)
 
 // Final backward substitution of the chunk held in y[B, B + LC) from
 // `carry` (x after the chunk); each x is stored as soon as it is known.
-// Leaves the chunk's first HB x values in `carry`.
+// Leaves the chunk's first HB x values in `carry`.  B == 0: a chunk before
+// the vector's last, every destination valid; B == LC: the last chunk,
+// destinations past the vector's end not stored.
 template <int HB, int LC, int K, int B, class Out>
 __device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB], int j0,
                                           const dev::StreamPlanView &p, const float *bwd, Out *out,
                                           std::int64_t out_elem, bool active, const Conversion &conv) {
     const int bs = bwd_stride<HB, K>(p);
-    const int n = p.destination_size;
+    const int valid = B == 0 ? LC : p.destination_size - j0;
+    Out *o = out + static_cast<std::int64_t>(j0 + LC - 1) * out_elem;
 #pragma unroll
     for (int t = LC - 1; t >= 0; --t) {
         const float *rec = bwd + t * bs;
@@ -299,14 +317,16 @@ __device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB]
         }
         const float x = y[B + t] - sum;
         y[B + t] = x;
-        if (active && j0 + t < n) out[static_cast<std::int64_t>(j0 + t) * out_elem] = tout<Out>(x, conv);
+        tst(o, tout<Out>(x, conv), active && (B == 0 || t < valid));
+        o -= out_elem;
     }
 #pragma unroll
     for (int d = 0; d < HB; ++d) carry[d] = y[B + d];
 }
 
+// At most 128 registers a thread: 16 warps per SM.
 template <int HB, int LC, int K, class In, class Out>
-__global__ void __launch_bounds__(kTMaxThreads)
+__global__ void __launch_bounds__(kTMaxThreads, 2 * 256 / kTMaxThreads)
 tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats) {
     static_assert(LC == kTChunk, "record chunks and register chunks coincide");
     extern __shared__ __align__(16) float smem[];
