@@ -193,11 +193,17 @@ typedef struct dsmvc_gb_stream_info {
     int32_t exact;               /* two-pass transposing kernels admitted */
     int32_t segmentable;         /* 2D passes may split vectors into segments */
     double forward_transfer;     /* history influence after one chunk */
+    int32_t group_union;         /* grouped records' union (12, 16), 0 if none */
+    int32_t group_stride;        /* floats per group of four destinations */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,
                               uint64_t forward_capacity, float *backward,
                               uint64_t backward_capacity);
+/* The grouped forward records of the 2D chunk-delayed kernels (one group
+ * per four destinations, group_stride floats each, whole chunks); `count`
+ * receives the floats needed, `out` may be NULL to query it. */
+int dsmvc_gb_plan_stream_groups(const dsmvc_gb_plan *plan, float *out, uint64_t capacity, uint64_t *count);
 /* planner_cache_stats / clear_planner_caches (engine.hpp:179-180). */
 int dsmvc_gb_planner_cache_stats(dsmvc_gb_planner_stats *out);
 void dsmvc_gb_clear_planner_caches(void);

@@ -223,3 +223,41 @@ def test_segment_admission_and_emulation(gb, name, req, eligible):
         for j, v in seg.items():
             assert np.max(np.abs(v - want[:, j])) <= 4e-7 * scale
             assert np.max(np.abs(v - whole[:, j])) <= 2e-7 * scale
+
+
+@pytest.mark.parametrize("name,req,eligible", CASES[:6], ids=[c[0] for c in CASES[:6]])
+def test_grouped_records(gb, name, req, eligible):
+    """Grouped records of the 2D chunk-delayed kernels restate the
+    per-destination records: each group of four destinations carries the
+    first window start, its ring offset and the union's refill target, the
+    four inverse diagonals, the four windows laid over the union (zeros
+    elsewhere) and the four records' lower factors."""
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info(records=True)
+    if not (info["eligible"] and info["ring_ok_transposed"]):
+        assert info["group_union"] == 0
+        return
+    fwd, K, hb = info["forward"], info["window"], p.half_bandwidth
+    starts = fwd[:, 0].copy().view(np.int32)
+    span = max(int(starts[g + 3]) + K - int(starts[g]) for g in range(0, len(starts), 4))
+    want_u = 12 if span <= 12 else 16 if span <= 16 else 0
+    assert info["group_union"] == want_u
+    if not want_u:
+        return
+    U = want_u
+    groups = info["groups"]
+    assert groups.shape == (len(starts) // 4, 8 + 4 * U + -(-4 * hb // 4) * 4)
+    assert info["group_stride"] == groups.shape[1]
+    for gi, grp in enumerate(groups):
+        g = 4 * gi
+        hdr = grp[:4].copy().view(np.int32)
+        base = int(starts[g])
+        assert hdr[0] == base and hdr[1] == (base % 32) * 34 and hdr[2] == int(starts[g + 3]) + K
+        for q in range(4):
+            rec = fwd[g + q]
+            assert grp[4 + q] == rec[1]
+            dense = np.zeros(U, np.float32)
+            at = int(starts[g + q]) - base
+            dense[at:at + K] = rec[4:4 + K]
+            assert np.array_equal(grp[8 + q * U:8 + (q + 1) * U], dense)
+            assert np.array_equal(grp[8 + 4 * U + q * hb:8 + 4 * U + (q + 1) * hb], rec[4 + K:4 + K + hb])

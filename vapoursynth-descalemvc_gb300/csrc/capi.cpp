@@ -255,6 +255,8 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->exact = pack.exact ? 1 : 0;
         info->segmentable = pack.segmentable ? 1 : 0;
         info->forward_transfer = pack.forward_transfer;
+        info->group_union = pack.group_union;
+        info->group_stride = pack.group_stride;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;
         info->backward_transfer = pack.backward_transfer;
@@ -263,6 +265,20 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
             std::copy(pack.forward.begin(), pack.forward.end(), forward);
         if (backward && backward_capacity >= pack.backward.size())
             std::copy(pack.backward.begin(), pack.backward.end(), backward);
+    });
+}
+
+int dsmvc_gb_plan_stream_groups(const dsmvc_gb_plan *plan, float *out, uint64_t capacity, uint64_t *count) {
+    return guarded([&] {
+        const auto &p = plan_of(plan);
+        const auto pack = dsmvc_gb::pack_stream_plan(p, dsmvc_gb::kStreamChunk, dsmvc_gb::kStreamRing,
+                                                     dsmvc_gb::stream_supports(p.half_bandwidth),
+                                                     dsmvc_gb::tsolve_supports(p.half_bandwidth));
+        if (count) *count = pack.forward_groups.size();
+        if (out) {
+            if (capacity < pack.forward_groups.size()) throw std::length_error("group buffer too small");
+            std::copy(pack.forward_groups.begin(), pack.forward_groups.end(), out);
+        }
     });
 }
 

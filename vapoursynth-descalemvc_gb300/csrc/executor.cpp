@@ -92,6 +92,10 @@ struct DevicePlan {
     bool stream64 = false;          // Float64 two-pass transposing kernels admitted
     dev::StreamPlanView stream_view64{};
     dev::StreamPlanView stream_view{};
+    // Grouped forward records of the chunk-delayed transposing kernels
+    // (StreamPack::forward_groups), when the plan has them: their union.
+    int stream_union = 0;
+    dev::StreamPlanView stream_view_g{};
     bool stream_p = false;          // paired transposing 2D kernels admitted
     dev::StreamPlanView stream_view2{};
     // Chunk-delayed transposing passes may split vectors into segments
@@ -117,11 +121,15 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
                                              tsolve_supports(p.half_bandwidth));
     const StreamPack64 pack64 = pack_stream_plan64(p, kStreamChunk, kStreamRing, tsolve_supports(p.half_bandwidth));
-    std::size_t at_records = 0, at_paired = 0, at_records64 = 0;
+    std::size_t at_records = 0, at_paired = 0, at_records64 = 0, at_groups = 0;
     if (pack.eligible || pack.exact) {
         at_records = parts.size();
         parts.push_back({pack.forward.data(), pack.forward.size() * 4});
         parts.push_back({pack.backward.data(), pack.backward.size() * 4});
+        if (pack.group_union) {
+            at_groups = parts.size();
+            parts.push_back({pack.forward_groups.data(), pack.forward_groups.size() * 4});
+        }
         if (pack.paired) {
             at_paired = parts.size();
             parts.push_back({pack.paired_forward.data(), pack.paired_forward.size() * 4});
@@ -177,6 +185,13 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         sv.backward_stride = pack.backward_stride;
         sv.forward = reinterpret_cast<const float *>(base + offsets[at_records]);
         sv.backward = reinterpret_cast<const float *>(base + offsets[at_records + 1]);
+        if (pack.group_union) {
+            dp->stream_union = pack.group_union;
+            dp->stream_view_g = sv;
+            dp->stream_view_g.window = pack.group_union;
+            dp->stream_view_g.forward_stride = pack.group_stride / 4;
+            dp->stream_view_g.forward = reinterpret_cast<const float *>(base + offsets[at_groups]);
+        }
         if (pack.paired) {
             dp->stream_p = true;
             auto &pv = dp->stream_view2;
@@ -484,7 +499,7 @@ struct GroupKey {
                      // 3 transposing streaming (2D)
     int hb;
     dev::Sample in, out;
-    int variant = 0; // kind 3: 1 when every job's window is 8
+    int variant = 0; // kind 3: the kernels' window (8, or 12 / 16 for grouped records), else 0
     bool operator<(const GroupKey &o) const {
         return std::tie(pass, kind, hb, in, out, variant)
             < std::tie(o.pass, o.kind, o.hb, o.in, o.out, o.variant);
@@ -502,11 +517,14 @@ bool stream_row_ok(const DevicePlan &dp, dev::Sample in) {
     return in == dev::Sample::f32;
 }
 
-// Launch-group variant of a transposing pass: 1 runs the window-8 kernels
-// (compile-time gather; for the two-pass kernels also the grouped refill).
+// Launch-group variant of a transposing pass.  Chunk-delayed kernels: the
+// union of grouped records (12, 16), else 8 for the window-8 kernels
+// (compile-time gather), else 0.  Paired and two-pass kernels: 1 runs the
+// window-8 kernels (for the two-pass ones also the grouped refill).
 int compiled_window(const DevicePlan &dp, int kind) {
     if (kind == 5) return dp.stream_xg ? 1 : 0;
-    return dp.stream_view.window == 8 ? 1 : 0;
+    if (kind == 3 && dp.stream_union) return dp.stream_union;
+    return dp.stream_view.window == 8 ? (kind == 3 ? 8 : 1) : 0;
 }
 
 std::string kernel_name(const GroupKey &k) {
@@ -695,7 +713,8 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 * sample_bytes(task.sample);
             if (r.h_kind) {
                 auto &j = hi.stream;
-                j.plan = r.h_kind == 4 ? r.h->stream_view2 : r.h->stream_view;
+                j.plan = r.h_kind == 4 ? r.h->stream_view2
+                       : r.h_kind == 3 && r.h->stream_union ? r.h->stream_view_g : r.h->stream_view;
                 j.in = task.input; j.in_elem = 1; j.in_vec = task.input_stride;
                 j.out = mid; j.out_elem = pitch; j.out_vec = 1;
                 j.y = mid; j.y_elem = pitch;                // forward values in place
@@ -716,7 +735,8 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             }
             if (r.v_kind) {
                 auto &j = vi.stream;
-                j.plan = r.v_kind == 4 ? r.v->stream_view2 : r.v->stream_view;
+                j.plan = r.v_kind == 4 ? r.v->stream_view2
+                       : r.v_kind == 3 && r.v->stream_union ? r.v->stream_view_g : r.v->stream_view;
                 j.in = mid; j.in_elem = 1; j.in_vec = pitch;
                 j.out = task.output; j.out_elem = task.output_stride; j.out_vec = 1;
                 if (r.fwd_stride) {
@@ -910,7 +930,7 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
                                  l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
         } else if (l.kind == 3) {
             rc = launch_tstream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,
-                                l.threads, l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats,
+                                l.threads, l.hb, l.variant, l.in, l.out, l.record_floats,
                                 stream);
         } else if (l.kind == 2) {
             rc = launch_stream(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks,

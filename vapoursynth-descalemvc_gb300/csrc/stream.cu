@@ -110,8 +110,22 @@ int launch_tsolve(const dev::StreamJob *jobs, int job_count, int total_blocks, i
     }
 }
 
+int launch_tstream_g_hb1(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_g_hb3(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_g_hb5(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+int launch_tstream_g_hb7(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
+
 int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
                    int window, dev::Sample in, dev::Sample out, int record_floats, void *stream) {
+    if (window > 8) {
+        switch (half_bandwidth) {
+        case 1: return launch_tstream_g_hb1(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+        case 3: return launch_tstream_g_hb3(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+        case 5: return launch_tstream_g_hb5(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+        case 7: return launch_tstream_g_hb7(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
+        default: return static_cast<int>(cudaErrorInvalidValue);
+        }
+    }
     switch (half_bandwidth) {
     case 1: return launch_tstream_hb1(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);
     case 3: return launch_tstream_hb3(jobs, job_count, total_blocks, threads, window, in, out, record_floats, stream);

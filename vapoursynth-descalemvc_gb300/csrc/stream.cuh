@@ -74,8 +74,10 @@ constexpr int kPairedRingPitch = 66;
 // (rows: f32/u8/u16 in, f32 out); otherwise columns (f32 in; f32/u8/u16 out).
 // Transposing 2D passes (tstream_impl.cuh): vectors with adjacent samples
 // in, destination-major output with the vectors adjacent.  Every job of one
-// launch has the same window when window == 8 (unrolled gather).  `threads`
-// per CTA: 32..256, a multiple of 32 (one warp per 32 vectors).
+// launch has the same window when window == 8 (unrolled gather); window 12
+// or 16: every job's plan view carries grouped records with that union
+// (StreamPack::forward_groups).  `threads` per CTA: 32..256, a multiple of
+// 32 (one warp per 32 vectors).
 constexpr int kTStreamThreads = 128;   // default CTA size
 constexpr int kTResidentWarps = 16;    // resident warps per SM (128 registers a thread)
 constexpr int kMinSegmentChunks = 2;   // shortest segment, in chunks (StreamJob)

@@ -186,6 +186,40 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
         }
     }
     out.eligible = delayed;
+    if (delayed && out.ring_ok_transposed) {
+        const auto fs = static_cast<std::size_t>(out.forward_stride);
+        auto start_of = [&](std::size_t j) {
+            int v;
+            std::memcpy(&v, &out.forward[j * fs], sizeof(int));
+            return v;
+        };
+        int span = 0;
+        for (std::size_t g = 0; g < padded; g += 4) span = std::max(span, start_of(g + 3) + window - start_of(g));
+        const int u = span <= 12 ? 12 : span <= 16 ? 16 : 0;
+        if (u) {
+            out.group_union = u;
+            out.group_stride = 8 + 4 * u + round4(4 * hb);
+            const auto gs = static_cast<std::size_t>(out.group_stride);
+            out.forward_groups.assign(padded / 4 * gs, 0.0F);
+            for (std::size_t g = 0; g < padded; g += 4) {
+                float *d = out.forward_groups.data() + g / 4 * gs;
+                const int base = start_of(g);
+                const int ring_offset = (base & (kStreamRing - 1)) * kTRingPitch;
+                const int need = start_of(g + 3) + window;
+                std::memcpy(&d[0], &base, sizeof(int));
+                std::memcpy(&d[1], &ring_offset, sizeof(int));
+                std::memcpy(&d[2], &need, sizeof(int));
+                for (std::size_t q = 0; q < 4; ++q) {
+                    const float *r = out.forward.data() + (g + q) * fs;
+                    d[4 + q] = r[1];
+                    const int at = start_of(g + q) - base;
+                    for (int k = 0; k < window; ++k) d[8 + q * u + static_cast<std::size_t>(at + k)] = r[4 + k];
+                    for (int i = 0; i < hb; ++i)
+                        d[8 + 4 * static_cast<std::size_t>(u) + q * static_cast<std::size_t>(hb) + i] = r[4 + window + i];
+                }
+            }
+        }
+    }
     out.segmentable = delayed && out.ring_ok_transposed && fworst <= std::ldexp(1.0, -26);
     out.chunk_first_block.resize(static_cast<std::size_t>(chunks));
     for (int k = 0; k < chunks; ++k) out.chunk_first_block[static_cast<std::size_t>(k)] = s0[static_cast<std::size_t>(k) * chunk] / 16 * 16;

@@ -31,6 +31,17 @@ struct StreamPack {
     // its forward substitution from a zero history one chunk early.  Admitted
     // when that warm-up leaves a history influence below 2^-26 per slot
     // (every chunk that can serve as warm-up, computed in double).
+    // Grouped forward records of the chunk-delayed transposing kernels
+    // (tstream_impl.cuh, K = group_union), when the window starts of every
+    // four consecutive destinations 4g..4g+3 span at most 12 (or 16) samples
+    // together with the window: per group, [window start of 4g, its ring
+    // offset, end of the union actually needed (the refill target), 0],
+    // the four inverse diagonals, the four windows' weights each laid over
+    // the union (zeros outside their own window), then the four records'
+    // lower factors back to back (use order d = hb..1), padded to 4.
+    int group_union = 0;            // 12 or 16; 0 when not grouped
+    int group_stride = 0;           // floats per group: 8 + 4 union + round4(4 hb)
+    std::vector<float> forward_groups;
     bool segmentable = false;
     double forward_transfer = 0.0;  // max |history -> state| over one chunk
     // Window start of each chunk's first destination, rounded down to the

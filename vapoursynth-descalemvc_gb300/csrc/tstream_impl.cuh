@@ -95,7 +95,11 @@ __device__ __forceinline__ void tst(std::uint8_t *p, std::uint8_t v, bool pred) 
 
 // Record strides (floats).  With a compile-time window they are constants,
 // so every record read is an immediate offset from the chunk's base.
+// K: 0 runtime window, 8 window-8 gather, 12 and 16 grouped gather over a
+// union of K samples (StreamPack::forward_groups; the stride is then a
+// group's floats over 4).
 template <int HB, int K> __device__ __forceinline__ int fwd_stride(const dev::StreamPlanView &p) {
+    if constexpr (K > 8) return (8 + 4 * K + (4 * HB + 3) / 4 * 4) / 4;
     return K > 0 ? 4 + K + (HB + 3) / 4 * 4 : p.forward_stride;
 }
 template <int HB, int K> __device__ __forceinline__ int bwd_stride(const dev::StreamPlanView &p) {
@@ -250,6 +254,64 @@ __device__ __forceinline__ void tforward(float (&y)[2 * LC], int j0, const dev::
     }
 }
 
+// Forward substitution of a chunk with grouped records: per group of four
+// destinations the union of their windows (U = K ring rows from the first
+// window's start) is read once, and each destination's weights, laid over
+// the union with zeros outside its window, apply as packed float2 FMAs
+// over pairs of union samples (even and odd union taps in the two halves,
+// then their sum -- the zeros add nothing, so each destination's gather
+// equals the per-destination one).  Rows of the union past the refill
+// target hold earlier finite samples or the ring's initial zeros.
+template <int HB, int LC, int U, class Feed>
+__device__ __forceinline__ void tforward_grouped(float (&y)[2 * LC], const float *fwd, Feed &feed, int lane) {
+    constexpr int GS = 8 + 4 * U + (4 * HB + 3) / 4 * 4;   // floats per group
+#pragma unroll
+    for (int t = 0; t < LC; t += 4) {
+        const float *gr = fwd + (t / 4) * GS;
+        const float4 h = tlds4(gr);
+        feed.ensure(__float_as_int(h.z));
+        const float *win = feed.ring + lane + __float_as_int(h.y);
+        float x[U];
+#pragma unroll
+        for (int i = 0; i < U; ++i) x[i] = win[i * kTPitch];
+        const float4 inv = tlds4(gr + 4);
+        float g[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int i = 0; i < U; i += 4) {
+                const float4 w = tlds4(gr + 8 + q * U + i);
+                acc = __ffma2_rn(make_float2(w.x, w.y), make_float2(x[i], x[i + 1]), acc);
+                acc = __ffma2_rn(make_float2(w.z, w.w), make_float2(x[i + 2], x[i + 3]), acc);
+            }
+            g[q] = acc.x + acc.y;
+        }
+        float lw[(4 * HB + 3) / 4 * 4];
+#pragma unroll
+        for (int i = 0; i < (4 * HB + 3) / 4 * 4; i += 4) {
+            const float4 l = tlds4(gr + 8 + 4 * U + i);
+            lw[i] = l.x;
+            lw[i + 1] = l.y;
+            lw[i + 2] = l.z;
+            lw[i + 3] = l.w;
+        }
+        const float iv[4] = {inv.x, inv.y, inv.z, inv.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float sum = g[q];
+#pragma unroll
+            for (int e = 0; e < HB; ++e) {
+                const int d = HB - e;                  // use order d = hb..1
+                sum = fmaf(lw[q * HB + e], y[LC + t + q - d], sum);
+            }
+            // Records past the end of the vector are zero (inverse diagonal
+            // included), so their forward values are zero for finite data.
+            y[LC + t + q] = sum * iv[q];
+        }
+    }
+}
+
 // Zero-carry backward warm-up over the chunk held in y[LC, 2 LC); leaves the
 // state entering the preceding chunk in `carry`.
 template <int HB, int LC, int K>
@@ -376,6 +438,11 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
+    if constexpr (K > 8) {
+        // The grouped gather reads whole unions: every ring row starts finite.
+        for (int i = lane; i < kTRingFloats; i += 32) ring[i] = 0.0f;
+        __syncwarp();
+    }
     if (!idle) feed.start(c0 > 0 ? lead.first_sample : 0);
 
     Out *out = static_cast<Out *>(job.out) + (warp_first + (lane < warp_vectors ? lane : 0));
@@ -395,7 +462,8 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
         const float *cur = bufs + (c % 3) * per_buffer;
         const float *prev = bufs + ((c + 2) % 3) * per_buffer;
         if (!idle) {
-            tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
+            if constexpr (K > 8) tforward_grouped<HB, LC, K>(y, cur, feed, lane);
+            else tforward<HB, LC, K>(y, c * LC, p, cur, feed, lane);
             const float *cur_b = cur + kTChunk * fwd_stride<HB, K>(p);
             if (c + 1 == chunks) {
                 // The vector's last chunk: exact backward substitution from
@@ -460,6 +528,15 @@ int tlaunch_hb(const StreamJob *jobs, int count, int blocks, int threads, int wi
                dev::Sample out, int record_floats, cudaStream_t s) {
     if (window == 8) return tlaunch_k<HB, kTChunk, 8>(jobs, count, blocks, threads, in, out, record_floats, s);
     return tlaunch_k<HB, kTChunk, 0>(jobs, count, blocks, threads, in, out, record_floats, s);
+}
+
+// Grouped records (window 12 or 16: the union).
+template <int HB>
+int tlaunch_hb_grouped(const StreamJob *jobs, int count, int blocks, int threads, int window, dev::Sample in,
+                       dev::Sample out, int record_floats, cudaStream_t s) {
+    if (window == 12) return tlaunch_k<HB, kTChunk, 12>(jobs, count, blocks, threads, in, out, record_floats, s);
+    if (window == 16) return tlaunch_k<HB, kTChunk, 16>(jobs, count, blocks, threads, in, out, record_floats, s);
+    return static_cast<int>(cudaErrorInvalidValue);
 }
 
 } // namespace

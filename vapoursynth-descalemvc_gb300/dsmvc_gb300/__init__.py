@@ -88,7 +88,8 @@ class StreamInfoC(C.Structure):
                 ("chunk", C.c_int32), ("ring", C.c_int32),
                 ("backward_transfer", C.c_double), ("reason", C.c_char * 96),
                 ("ring_ok_transposed", C.c_int32), ("exact", C.c_int32),
-                ("segmentable", C.c_int32), ("forward_transfer", C.c_double)]
+                ("segmentable", C.c_int32), ("forward_transfer", C.c_double),
+                ("group_union", C.c_int32), ("group_stride", C.c_int32)]
 
 
 class SweepOptionsC(C.Structure):
@@ -144,6 +145,7 @@ SIGNATURES = {
                               C.POINTER(C.c_uint64)], C.c_int),
     "dsmvc_gb_plan_stream_info": ([C.c_void_p, C.POINTER(StreamInfoC), C.c_void_p, C.c_uint64,
                                    C.c_void_p, C.c_uint64], C.c_int),
+    "dsmvc_gb_plan_stream_groups": ([C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "dsmvc_gb_planner_cache_stats": ([C.POINTER(PlannerStatsC)], C.c_int),
     "dsmvc_gb_clear_planner_caches": ([], None),
     "dsmvc_gb_executor_create": ([C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
@@ -324,6 +326,12 @@ class AxisPlan:
                                                    bwd.ctypes.data, bwd.size))
             out["forward"] = fwd.reshape(n, info.forward_stride)
             out["backward"] = bwd.reshape(n, info.backward_stride)
+            if info.group_union:
+                count = C.c_uint64()
+                _check(lib().dsmvc_gb_plan_stream_groups(self._h, None, 0, C.byref(count)))
+                groups = np.zeros(count.value, np.float32)
+                _check(lib().dsmvc_gb_plan_stream_groups(self._h, groups.ctypes.data, groups.size, C.byref(count)))
+                out["groups"] = groups.reshape(-1, info.group_stride)
         return out
 
     def hashes(self):
