@@ -129,6 +129,7 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         if (pack.group_union) {
             at_groups = parts.size();
             parts.push_back({pack.forward_groups.data(), pack.forward_groups.size() * 4});
+            parts.push_back({pack.backward_groups.data(), pack.backward_groups.size() * 4});
         }
         if (pack.paired) {
             at_paired = parts.size();
@@ -191,6 +192,8 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
             dp->stream_view_g.window = pack.group_union;
             dp->stream_view_g.forward_stride = pack.group_stride / 4;
             dp->stream_view_g.forward = reinterpret_cast<const float *>(base + offsets[at_groups]);
+            dp->stream_view_g.backward_stride = (4 * p.half_bandwidth + 3) / 4;
+            dp->stream_view_g.backward = reinterpret_cast<const float *>(base + offsets[at_groups + 1]);
         }
         if (pack.paired) {
             dp->stream_p = true;

@@ -218,6 +218,13 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
                         d[8 + 4 * static_cast<std::size_t>(u) + q * static_cast<std::size_t>(hb) + i] = r[4 + window + i];
                 }
             }
+            const auto bs = static_cast<std::size_t>(out.backward_stride);
+            const auto bg = static_cast<std::size_t>(round4(4 * hb));
+            out.backward_groups.assign(padded / 4 * bg, 0.0F);
+            for (std::size_t j = 0; j < padded; ++j)
+                for (int i = 0; i < hb; ++i)
+                    out.backward_groups[j / 4 * bg + (j % 4) * static_cast<std::size_t>(hb) + static_cast<std::size_t>(i)]
+                        = out.backward[j * bs + static_cast<std::size_t>(i)];
         }
     }
     out.segmentable = delayed && out.ring_ok_transposed && fworst <= std::ldexp(1.0, -26);

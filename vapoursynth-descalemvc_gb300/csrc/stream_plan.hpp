@@ -42,6 +42,9 @@ struct StreamPack {
     int group_union = 0;            // 12 or 16; 0 when not grouped
     int group_stride = 0;           // floats per group: 8 + 4 union + round4(4 hb)
     std::vector<float> forward_groups;
+    // Their backward records: per group, the four records' hb factors back
+    // to back (use order), padded to 4 (round4(4 hb) floats a group).
+    std::vector<float> backward_groups;
     bool segmentable = false;
     double forward_transfer = 0.0;  // max |history -> state| over one chunk
     // Window start of each chunk's first destination, rounded down to the

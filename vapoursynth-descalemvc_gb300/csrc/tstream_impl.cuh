@@ -102,7 +102,11 @@ template <int HB, int K> __device__ __forceinline__ int fwd_stride(const dev::St
     if constexpr (K > 8) return (8 + 4 * K + (4 * HB + 3) / 4 * 4) / 4;
     return K > 0 ? 4 + K + (HB + 3) / 4 * 4 : p.forward_stride;
 }
+// Backward records: per destination (round4(hb) floats, at least 4), or for
+// grouped records (K > 8) per group of four destinations, their hb
+// coefficients back to back padded to 4 (StreamPack::backward_groups).
 template <int HB, int K> __device__ __forceinline__ int bwd_stride(const dev::StreamPlanView &p) {
+    if constexpr (K > 8) return (4 * HB + 3) / 4;
     return K > 0 ? ((HB + 3) / 4 * 4 < 4 ? 4 : (HB + 3) / 4 * 4) : p.backward_stride;
 }
 
@@ -312,6 +316,26 @@ __device__ __forceinline__ void tforward_grouped(float (&y)[2 * LC], const float
     }
 }
 
+// The backward coefficients (use order) of destination t of a chunk, with
+// t visited in descending order: a group's are loaded at its last member.
+template <int HB, int K> struct TBackCoeffs {
+    static constexpr int N = K > 8 ? (4 * HB + 3) / 4 * 4 : (HB + 3) / 4 * 4;
+    float v[N];
+    __device__ __forceinline__ void at(const float *bwd, int bs, int t) {
+        if (K > 8 && t % 4 != 3) return;
+        const float *rec = K > 8 ? bwd + (t / 4) * N : bwd + t * bs;
+#pragma unroll
+        for (int i = 0; i < N; i += 4) {
+            const float4 u = tlds4(rec + i);
+            v[i] = u.x;
+            v[i + 1] = u.y;
+            v[i + 2] = u.z;
+            v[i + 3] = u.w;
+        }
+    }
+    __device__ __forceinline__ float operator()(int t, int pos) const { return v[K > 8 ? (t % 4) * HB + pos : pos]; }
+};
+
 // Zero-carry backward warm-up over the chunk held in y[LC, 2 LC); leaves the
 // state entering the preceding chunk in `carry`.
 template <int HB, int LC, int K>
@@ -321,24 +345,17 @@ __device__ __forceinline__ void twarmup(const float (&y)[2 * LC], float (&carry)
     float w[HB];
 #pragma unroll
     for (int d = 0; d < HB; ++d) w[d] = 0.0f;
+    TBackCoeffs<HB, K> u;
 #pragma unroll
     for (int t = LC - 1; t >= 0; --t) {
-        const float *rec = bwd + t * bs;
+        u.at(bwd, bs, t);
         float sum = 0.0f;
 #pragma unroll
-        for (int q = 0; q < HB; q += 4) {
-            const float4 u = tlds4(rec + q);
-            const float uv[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int pos = q + e;
-                if (pos < HB) {
-                    const int d = HB == 3 ? pos + 1 : HB - pos;
-                    // x_{t+d} beyond the chunk is the zero carry.
-                    const float xd = (t + d < LC) ? w[(t + d) % HB] : 0.0f;
-                    sum = fmaf(uv[e], xd, sum);
-                }
-            }
+        for (int pos = 0; pos < HB; ++pos) {
+            const int d = HB == 3 ? pos + 1 : HB - pos;
+            // x_{t+d} beyond the chunk is the zero carry.
+            const float xd = (t + d < LC) ? w[(t + d) % HB] : 0.0f;
+            sum = fmaf(u(t, pos), xd, sum);
         }
         w[t % HB] = y[LC + t] - sum;
     }
@@ -358,24 +375,17 @@ __device__ __forceinline__ void tbackward(float (&y)[2 * LC], float (&carry)[HB]
     const int bs = bwd_stride<HB, K>(p);
     const int valid = B == 0 ? LC : p.destination_size - j0;
     Out *o = out + static_cast<std::int64_t>(j0 + LC - 1) * out_elem;
+    TBackCoeffs<HB, K> u;
 #pragma unroll
     for (int t = LC - 1; t >= 0; --t) {
-        const float *rec = bwd + t * bs;
+        u.at(bwd, bs, t);
         float sum = 0.0f;
 #pragma unroll
-        for (int q = 0; q < HB; q += 4) {
-            const float4 u = tlds4(rec + q);
-            const float uv[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int pos = q + e;
-                if (pos < HB) {
-                    const int d = HB == 3 ? pos + 1 : HB - pos;
-                    const float xd = (t + d < LC) ? y[B + (t + d < LC ? t + d : 0)]
-                                                  : carry[t + d >= LC ? t + d - LC : 0];
-                    sum = fmaf(uv[e], xd, sum);
-                }
-            }
+        for (int pos = 0; pos < HB; ++pos) {
+            const int d = HB == 3 ? pos + 1 : HB - pos;
+            const float xd = (t + d < LC) ? y[B + (t + d < LC ? t + d : 0)]
+                                          : carry[t + d >= LC ? t + d - LC : 0];
+            sum = fmaf(u(t, pos), xd, sum);
         }
         const float x = y[B + t] - sum;
         y[B + t] = x;
