@@ -195,6 +195,10 @@ typedef struct dsmvc_gb_stream_info {
     double forward_transfer;     /* history influence after one chunk */
     int32_t group_union;         /* grouped records' union (12, 16), 0 if none */
     int32_t group_stride;        /* floats per group of four destinations */
+    int32_t f64_eligible;        /* Float64 two-pass transposing kernels admitted */
+    int32_t f64_segmentable;     /* ... and their segments */
+    int32_t f64_margin;          /* segment margin in chunks (0: none) */
+    double f64_margin_transfer;  /* influence left after that margin (4 if none) */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from common import F32_MAX_ABS, F32_MEAN_ABS, INT_MAX_CODES, make_input, oracle_request, product_request
+from common import F32_MAX_ABS, F32_MEAN_ABS, INT_MAX_CODES, make_input, max_ulp, oracle_request, product_request
 from conftest import _executor_with
 
 pytestmark = pytest.mark.gpu
@@ -69,3 +69,48 @@ def test_segments_are_launched(gb, forced, whole_executor):
         sizes[label] = b.info()["table_bytes"]
         b.close()
     assert sizes["forced"] > sizes["whole"]
+
+
+F64_GEOMS = [
+    ("bicubic-forced", (960, 640, 640.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "mirror", 2),
+     (540, 360, 360.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "mirror", 2)),
+    ("spline64-blur-forced", (1280, 853, 853.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2),
+     (720, 480, 480.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2)),
+]
+
+
+@pytest.mark.parametrize("sample", ["f32", "u16"])
+@pytest.mark.parametrize("name,hq,vq", F64_GEOMS, ids=[g[0] for g in F64_GEOMS])
+def test_float64_segments(gb, forced, whole_executor, name, hq, vq, sample):
+    """Float64 two-pass kernels in segments (forward and backward margins of
+    2-4 chunks, admitted below 2^-60): within the <= 1 float ULP / 1 code
+    contract of the CPU scalar Float64 route and of whole vectors."""
+    h = gb.AxisPlan(product_request(gb, hq), cached=False)
+    v = gb.AxisPlan(product_request(gb, vq), cached=False)
+    assert h.stream_info()["f64_segmentable"]
+    x = make_input(v.source_size, h.source_size, sample, 91)
+    conv = gb.integer_conversion(16, False, False) if sample == "u16" else None
+    got = forced.inverse_2d(h, v, x, conv)
+    whole = whole_executor.inverse_2d(h, v, x, conv)
+    want = O.inverse_2d(O.Plan(oracle_request(hq)), O.Plan(oracle_request(vq)), x, conv)
+    if sample == "u16":
+        assert np.abs(got.astype(np.int64) - want.astype(np.int64)).max() <= 1
+        assert np.abs(got.astype(np.int64) - whole.astype(np.int64)).max() <= 1
+    else:
+        assert max_ulp(got, want) <= 1 and max_ulp(got, whole) <= 1
+
+
+def test_float64_segments_are_launched(gb, forced, whole_executor):
+    torch = pytest.importorskip("torch")
+    _name, hq, vq = F64_GEOMS[0]
+    h = gb.AxisPlan(product_request(gb, hq), cached=False)
+    v = gb.AxisPlan(product_request(gb, vq), cached=False)
+    dx = torch.zeros((v.source_size, h.source_size), dtype=torch.float32, device="cuda")
+    dy = torch.zeros((v.destination_size, h.destination_size), dtype=torch.float32, device="cuda")
+    task = gb.PlaneTask(h, v, dx.data_ptr(), h.source_size, dy.data_ptr(), h.destination_size, 0, 0, None)
+    sizes = {}
+    for label, ex in (("forced", forced), ("whole", whole_executor)):
+        b = ex.prepare_batch([task])
+        sizes[label] = (b.info()["table_bytes"], b.info()["scratch_bytes"])
+        b.close()
+    assert sizes["forced"][0] > sizes["whole"][0] and sizes["forced"][1] > sizes["whole"][1]

@@ -261,3 +261,49 @@ def test_grouped_records(gb, name, req, eligible):
             dense[at:at + K] = rec[4:4 + K]
             assert np.array_equal(grp[8 + q * U:8 + (q + 1) * U], dense)
             assert np.array_equal(grp[8 + 4 * U + q * hb:8 + 4 * U + (q + 1) * hb], rec[4 + K:4 + K + hb])
+
+
+def f64_margin_transfer(p, chunk, margin):
+    """Influence left by a unit history (forward, undivided values) or carry
+    (backward) after `margin` chunks from every chunk boundary, in float64,
+    from the plan's Float64 LDL^T bands (band d at i: L(i + d, i))."""
+    n, hb = p.destination_size, p.half_bandwidth
+    bands = p.array("ldlt_bands_f64").reshape(hb + 1, n)
+    chunks = (n + chunk - 1) // chunk
+    span = margin * chunk
+    worst = 0.0
+    for k in range(1, chunks):
+        a = k * chunk
+        if a + span <= n:
+            for e in range(hb):
+                z = {a - 1 - e: 1.0}
+                for i in range(a, a + span):
+                    z[i] = -sum(bands[d, i - d] * z.get(i - d, 0.0) for d in range(1, min(hb, i) + 1))
+                worst = max(worst, max(abs(z[a + span - 1 - q]) for q in range(hb)))
+            for e in range(hb):
+                x = {a + span + e: 1.0}
+                for i in range(a + span - 1, a - 1, -1):
+                    x[i] = -sum(bands[d, i] * x.get(i + d, 0.0) for d in range(1, min(hb, n - i - 1) + 1))
+                worst = max(worst, max(abs(x[a + q]) for q in range(hb)))
+    return worst
+
+
+@pytest.mark.parametrize("req", [
+    (600, 400, 400.0, 0.0, "bicubic", 3, 0, 0.5, 1.0, "mirror", 2),
+    (500, 333, 333.0, 0.1, "spline64", 3, 0, 0.5, 1.1, "symmetric", 2),
+])
+def test_float64_segment_margins(gb, req):
+    """The Float64 segment margin: the smallest of 2..4 chunks leaving less
+    than 2^-60, its transfer equal to a float64 restatement."""
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info()
+    assert info["f64_eligible"]
+    chunks = -(-p.destination_size // info["chunk"])
+    want = 0
+    for margin in (2, 3, 4):
+        t = f64_margin_transfer(p, info["chunk"], margin)
+        if chunks >= 2 * margin and t <= 2.0 ** -60:
+            want = margin
+            break
+    assert info["f64_margin"] == want and bool(info["f64_segmentable"]) == (want > 0)
+    assert info["f64_margin_transfer"] == pytest.approx(t, rel=1e-9, abs=1e-300)

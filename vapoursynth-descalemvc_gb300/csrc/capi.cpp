@@ -257,6 +257,12 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->forward_transfer = pack.forward_transfer;
         info->group_union = pack.group_union;
         info->group_stride = pack.group_stride;
+        const auto pack64 = dsmvc_gb::pack_stream_plan64(p, dsmvc_gb::kStreamChunk, dsmvc_gb::kStreamRing,
+                                                         dsmvc_gb::tsolve_supports(p.half_bandwidth));
+        info->f64_eligible = pack64.eligible ? 1 : 0;
+        info->f64_segmentable = pack64.segmentable ? 1 : 0;
+        info->f64_margin = pack64.margin;
+        info->f64_margin_transfer = pack64.margin_transfer;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;
         info->backward_transfer = pack.backward_transfer;

@@ -90,6 +90,9 @@ struct DevicePlan {
     bool stream_x = false;          // two-pass transposing 2D kernels admitted
     bool stream_xg = false;         // ... with the grouped refill of window 8
     bool stream64 = false;          // Float64 two-pass transposing kernels admitted
+    bool stream64_seg = false;      // ... and their segments (StreamPack64::segmentable)
+    int margin64 = 0;
+    std::vector<int> chunk_first_block64;
     dev::StreamPlanView stream_view64{};
     dev::StreamPlanView stream_view{};
     // Grouped forward records of the chunk-delayed transposing kernels
@@ -207,6 +210,11 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     }
     if (pack64.eligible) {
         dp->stream64 = true;
+        dp->stream64_seg = pack64.segmentable;
+        if (pack64.segmentable) {
+            dp->margin64 = pack64.margin;
+            dp->chunk_first_block64 = pack64.chunk_first_block;
+        }
         auto &xv = dp->stream_view64;
         xv.source_size = p.source_size;
         xv.destination_size = p.destination_size;
@@ -540,6 +548,48 @@ std::string kernel_name(const GroupKey &k) {
 
 namespace {
 
+// Chunks of forward values the Float64 segments of one pass store: each
+// segment's range with `margin` chunks on either side (within the vector).
+std::size_t segment64_chunks(int destinations, int segments, int margin) {
+    const int chunks = (destinations + kStreamChunk - 1) / kStreamChunk;
+    std::size_t total = 0;
+    for (int k = 0; k < segments; ++k) {
+        const int begin = static_cast<int>(static_cast<long>(k) * chunks / segments);
+        const int end = static_cast<int>(static_cast<long>(k + 1) * chunks / segments);
+        total += static_cast<std::size_t>(std::min(end + margin, chunks) - std::max(begin - margin, 0));
+    }
+    return total;
+}
+
+// One Float64 two-pass job, or its segments: chunk ranges, each with its
+// forward-value region in `yseg` (rows of `pitch` doubles, starting at the
+// segment's first computed chunk) and its ring's first block.
+template <class Item>
+void push_segments64(std::vector<Item> &group, const Item &whole, const DevicePlan &dp, int destinations,
+                     int segments, char *yseg, std::int64_t pitch) {
+    if (segments <= 1) {
+        group.push_back(whole);
+        return;
+    }
+    const int chunks = (destinations + kStreamChunk - 1) / kStreamChunk;
+    std::size_t at = 0;
+    for (int k = 0; k < segments; ++k) {
+        const int begin = static_cast<int>(static_cast<long>(k) * chunks / segments);
+        const int end = static_cast<int>(static_cast<long>(k + 1) * chunks / segments);
+        const int first = std::max(begin - dp.margin64, 0);
+        const int last = std::min(end + dp.margin64, chunks);
+        Item it = whole;
+        it.stream.chunk_begin = begin;
+        it.stream.chunk_end = end;
+        it.stream.first_sample = dp.chunk_first_block64[static_cast<std::size_t>(first)];
+        it.stream.margin = dp.margin64;
+        it.stream.y = reinterpret_cast<float *>(yseg + at * kStreamChunk * static_cast<std::size_t>(pitch) * 8);
+        it.stream.y_elem = pitch;
+        at += static_cast<std::size_t>(last - first);
+        group.push_back(it);
+    }
+}
+
 // Jobs of a chunk-delayed transposing launch group (sorted by plan), split
 // into segments of whole chunks.  Automatic mode: when the group's warps fill
 // fewer than `slots` resident warp slots, up to slots / warps segments per
@@ -603,6 +653,10 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         bool transposed64 = false;
         int h_kind = 0, v_kind = 0;
         std::size_t mid = 0, mid_stride = 0, fwd = 0, fwd_stride = 0;
+        // Float64 segments per pass (1: whole vectors) and their forward-value
+        // scratch (each segment's own, margins included).
+        int seg_h = 1, seg_v = 1;
+        std::size_t yseg_h = 0, yseg_v = 0;
     };
     std::vector<Route> routes(tasks.size());
     std::size_t bytes = 0;
@@ -665,6 +719,41 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             bytes += align_up(r.fwd_stride * lines * 8);
         }
     }
+    // Float64 segments: each pass's kind-6 warps decide the split (as for the
+    // chunk-delayed kernels); every segment writes its forward values, its
+    // margins included, to a scratch region of its own.
+    {
+        long warps64[2] = {0, 0};
+        for (std::size_t t = 0; t < tasks.size(); ++t) {
+            if (!routes[t].transposed64) continue;
+            warps64[0] += (tasks[t].vertical->source_size + 31) / 32;
+            warps64[1] += (tasks[t].horizontal->destination_size + 31) / 32;
+        }
+        auto split = [&](const DevicePlan &dp, int destinations, long warps) {
+            if (!dp.stream64_seg || segment_mode == 1) return 1;
+            const int chunks = (destinations + kStreamChunk - 1) / kStreamChunk;
+            int s = segment_mode >= 2 ? segment_mode
+                                      : (warps > 0 ? static_cast<int>(std::min<long>(warp_slots / warps, 64)) : 1);
+            return std::max(1, std::min(s, chunks / (2 * dp.margin64)));
+        };
+        for (std::size_t t = 0; t < tasks.size(); ++t) {
+            auto &r = routes[t];
+            if (!r.transposed64) continue;
+            const AxisPlan *h = tasks[t].horizontal, *v = tasks[t].vertical;
+            r.seg_h = split(*r.h, h->destination_size, warps64[0]);
+            if (r.seg_h > 1) {
+                r.yseg_h = bytes;
+                bytes += align_up(segment64_chunks(h->destination_size, r.seg_h, r.h->margin64) * kStreamChunk
+                                  * r.mid_stride * 8);
+            }
+            r.seg_v = split(*r.v, v->destination_size, warps64[1]);
+            if (r.seg_v > 1) {
+                r.yseg_v = bytes;
+                bytes += align_up(segment64_chunks(v->destination_size, r.seg_v, r.v->margin64) * kStreamChunk
+                                  * r.fwd_stride * 8);
+            }
+        }
+    }
     out.scratch_bytes = bytes;
     char *base = scratch(std::max<std::size_t>(bytes, kAlign));
 
@@ -696,7 +785,8 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             a.y = static_cast<float *>(mid); a.y_elem = pitch;   // Float64 forward values in place
             a.vectors = v->source_size;
             a.conv = conv;
-            groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}].push_back(hi);
+            push_segments64(groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}], hi, *r.h,
+                            h->destination_size, r.seg_h, base + r.yseg_h, pitch);
             auto &b = vi.stream;
             b.plan = r.v->stream_view64;
             b.in = mid; b.in_elem = 1; b.in_vec = pitch;
@@ -704,7 +794,8 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             b.y = reinterpret_cast<float *>(base + r.fwd); b.y_elem = static_cast<std::int64_t>(r.fwd_stride);
             b.vectors = h->destination_size;
             b.conv = conv;
-            groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}].push_back(vi);
+            push_segments64(groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}], vi, *r.v,
+                            v->destination_size, r.seg_v, base + r.yseg_v, static_cast<std::int64_t>(r.fwd_stride));
             continue;
         }
         if (r.transposed) {
@@ -1448,7 +1539,9 @@ std::size_t PreparedBatch::table_bytes() const { return impl_->compiled.table.si
 std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
     // Per task: the intermediate plane (destinations of the first pass x
     // sources of the second, rows padded to 4) plus a forward plane of the
-    // output's size, in the route's sample width.
+    // output's size, in the route's sample width; Float64 2D planes also the
+    // forward values of their segments (margins included, at most twice a
+    // pass's whole chunks of forward values).
     std::size_t bytes = kAlign;
     for (const auto &t : tasks) {
         const AxisPlan *h = t.horizontal, *v = t.vertical;
@@ -1459,6 +1552,11 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
         const std::size_t vs = v ? (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4 : static_cast<std::size_t>(t.vectors);
         const std::size_t vd = v ? static_cast<std::size_t>(v->destination_size) : static_cast<std::size_t>(t.vectors);
         bytes += align_up(hd * vs * es) + align_up(hd * vd * es);
+        if (f64 && h && v) {
+            const std::size_t hc = (hd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
+            const std::size_t vc = (vd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
+            bytes += align_up(2 * hc * vs * 8) + align_up(2 * vc * hd * 8);
+        }
     }
     return bytes;
 }

@@ -53,7 +53,13 @@ struct StreamJob {
     std::int32_t chunk_begin;
     std::int32_t chunk_end;
     std::int32_t first_sample;
-    std::int32_t reserved;
+    // Float64 two-pass kernels: a segment's forward and backward margins, in
+    // chunks (StreamPack64::margin); such a segment sweeps forward from
+    // `margin` chunks before its range (zero history, ring from first_sample)
+    // and backward from `margin` chunks after it (zero carry), within the
+    // vector, storing its forward values from its first computed chunk on
+    // at y (rows of y_elem).
+    std::int32_t margin;
 };
 
 } // namespace dsmvc_gb::dev

@@ -326,6 +326,59 @@ StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_
     out.window = window;
     out.forward_stride = 2 * fs;
     out.backward_stride = 2 * bs;
+
+    // Segment margins: a unit in any history slot entering position a (the
+    // forward recurrence of the undivided values, z_i = -sum_d L z_{i-d}) or
+    // any carry slot entering position a from above (x_i = -sum_d L x_{i+d}),
+    // pushed through `margin` chunks; the smallest margin of 2..4 chunks that
+    // leaves less than 2^-60 of it.
+    const int chunks = static_cast<int>(padded) / chunk;
+    auto transfer = [&](int margin) {
+        const int span64 = margin * chunk;
+        double worst = 0.0;
+        std::vector<double> z(static_cast<std::size_t>(span64 + hb));
+        for (int k = 1; k < chunks; ++k) {
+            const int a = k * chunk;
+            for (int e = 0; e < hb; ++e) {
+                std::fill(z.begin(), z.end(), 0.0);
+                z[static_cast<std::size_t>(hb - 1 - e)] = 1.0;          // z[i] holds position a - hb + i
+                const int hi = std::min(n, a + span64);
+                for (int i = a; i < hi; ++i) {
+                    const double *f = out.forward.data() + static_cast<std::size_t>(i) * static_cast<std::size_t>(fs);
+                    double s = 0.0;
+                    for (int q = 0; q < hb; ++q) s += f[2 + window + q] * z[static_cast<std::size_t>(i - (hb - q) - a + hb)];
+                    z[static_cast<std::size_t>(i - a + hb)] = -s;
+                }
+                if (hi == a + span64)
+                    for (int q = 0; q < hb; ++q) worst = std::max(worst, std::abs(z[static_cast<std::size_t>(span64 + q)]));
+            }
+            const int top = a + span64;                                   // carry enters below `top`
+            if (top > n) continue;
+            for (int e = 0; e < hb; ++e) {
+                std::fill(z.begin(), z.end(), 0.0);
+                z[static_cast<std::size_t>(span64 + e)] = 1.0;           // z[i] holds position a + i
+                for (int i = top - 1; i >= a; --i) {
+                    const double *b = out.backward.data() + static_cast<std::size_t>(i) * static_cast<std::size_t>(bs);
+                    double s = 0.0;
+                    for (int q = 0; q < hb; ++q) s += b[q] * z[static_cast<std::size_t>(i + (hb - q) - a)];
+                    z[static_cast<std::size_t>(i - a)] = -s;
+                }
+                for (int q = 0; q < hb; ++q) worst = std::max(worst, std::abs(z[static_cast<std::size_t>(q)]));
+            }
+        }
+        return worst;
+    };
+    for (int margin = 2; margin <= 4; ++margin) {
+        out.margin_transfer = transfer(margin);
+        if (chunks >= 2 * margin && out.margin_transfer <= std::ldexp(1.0, -60)) {
+            out.margin = margin;
+            break;
+        }
+    }
+    out.segmentable = out.margin > 0;
+    out.chunk_first_block.resize(static_cast<std::size_t>(chunks));
+    for (int k = 0; k < chunks; ++k)
+        out.chunk_first_block[static_cast<std::size_t>(k)] = s0[std::min<std::size_t>(static_cast<std::size_t>(k) * chunk, w - 1)] / 16 * 16;
     return out;
 }
 

@@ -90,6 +90,16 @@ struct StreamPack64 {
     int backward_stride = 0;
     std::vector<double> forward;
     std::vector<double> backward;
+    // Segments (chunk ranges served by separate warps): a segment runs its
+    // forward sweep from `margin` chunks before its range (zero history) and
+    // its backward sweep from as many chunks after it (zero carry).
+    // Admitted with the smallest margin of 2..4 chunks that, in double,
+    // leaves an influence below 2^-60 of a unit history or carry from every
+    // chunk boundary.
+    bool segmentable = false;
+    int margin = 0;                       // chunks
+    double margin_transfer = 0.0;         // at that margin (at 4 when none)
+    std::vector<int> chunk_first_block;   // window start of each chunk, rounded down to 16
 };
 StreamPack64 pack_stream_plan64(const AxisPlan &plan, int chunk, int ring, bool half_bandwidth_supported);
 

@@ -92,8 +92,9 @@ struct WarpFeeder64 {
         }
     }
 
-    __device__ __forceinline__ void start() {
-        have = 0;
+    // `first`: a multiple of 16 at most the first window start.
+    __device__ __forceinline__ void start(int first = 0) {
+        have = first;
         issue();
     }
 
@@ -132,8 +133,21 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
     const int nthreads = static_cast<int>(blockDim.x);
     const int cta_warp = static_cast<int>(blockIdx.x) * (nthreads >> 5);
     const StreamJob &job = jobs[find_tjob(jobs, job_count, cta_warp + warp)];
-    const dev::StreamPlanView p = jobs[find_tjob(jobs, job_count, cta_warp)].plan;
+    const StreamJob &lead = jobs[find_tjob(jobs, job_count, cta_warp)];
+    const dev::StreamPlanView p = lead.plan;
     const int n = p.destination_size;
+    const int chunks = (n + kTChunk - 1) / kTChunk;
+    // Chunks stored: [ca, cb); a segment (chunk_end > 0) sweeps forward over
+    // [fc0, fce] from a zero history and backward from a zero carry after
+    // fce, `margin` chunks beyond its range on either side (within the
+    // vector), with its forward values in its own region starting at chunk
+    // fc0.  Every warp of a CTA serves the same plan and range.
+    const bool segment = lead.chunk_end > 0;
+    const int ca = lead.chunk_begin;
+    const int cb = segment ? lead.chunk_end : chunks;
+    const int fc0 = segment ? max(ca - lead.margin, 0) : 0;
+    const int fce = segment ? min(cb + lead.margin, chunks) - 1 : chunks - 1;
+    const int ybase = fc0 * kTChunk;
     const int per_buffer = kTChunk * record_floats;
     float *bufs = smem;
     double *ring = reinterpret_cast<double *>(smem + 3 * per_buffer) + warp * kXRingDoubles;
@@ -160,24 +174,23 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
-    if (!idle) feed.start();
+    if (!idle) feed.start(fc0 > 0 ? lead.first_sample : 0);
 
     double *yplane = reinterpret_cast<double *>(job.y) + v;
     Out *out = static_cast<Out *>(job.out) + v;
     const int fs = p.forward_stride / 2, bs = p.backward_stride / 2;   // doubles
     const int kw = p.window;
-    const int chunks = (n + LC - 1) / LC;
     std::uint32_t flags = 0;
 
     // ---- forward sweep ---------------------------------------------------
-    tstage(bufs, p, 0, tid, nthreads);
+    tstage(bufs + (fc0 % 3) * per_buffer, p, fc0, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid, nthreads);
+    if (fc0 + 1 <= fce) tstage(bufs + ((fc0 + 1) % 3) * per_buffer, p, fc0 + 1, tid, nthreads);
     tcp_commit();
     double z[HB];                                        // undivided forward values, newest first
 #pragma unroll
     for (int d = 0; d < HB; ++d) z[d] = 0.0;
-    for (int c = 0; c < chunks; ++c) {
+    for (int c = fc0; c <= fce; ++c) {
         tcp_wait_one();
         __syncthreads();
         const double *fwd = reinterpret_cast<const double *>(bufs + (c % 3) * per_buffer);
@@ -202,11 +215,11 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
 #pragma unroll
                 for (int d = HB - 1; d > 0; --d) z[d] = z[d - 1];
                 z[0] = sum;
-                if (active) yplane[static_cast<std::int64_t>(j) * job.y_elem] = __ddiv_rn(sum, rec[1]);
+                if (active) yplane[static_cast<std::int64_t>(j - ybase) * job.y_elem] = __ddiv_rn(sum, rec[1]);
             }
         }
         __syncthreads();
-        if (c + 2 < chunks) tstage(bufs + ((c + 2) % 3) * per_buffer, p, c + 2, tid, nthreads);
+        if (c + 2 <= fce) tstage(bufs + ((c + 2) % 3) * per_buffer, p, c + 2, tid, nthreads);
         tcp_commit();
     }
     flags |= feed.flags;
@@ -214,25 +227,26 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
     // ---- backward sweep --------------------------------------------------
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
-    tstage(bufs, p, chunks - 1, tid, nthreads);
+    tstage(bufs, p, fce, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, chunks - 2, tid, nthreads);
+    if (fce - 1 >= ca) tstage(bufs + per_buffer, p, fce - 1, tid, nthreads);
     tcp_commit();
     double x[HB];                                        // following results, nearest first
 #pragma unroll
     for (int d = 0; d < HB; ++d) x[d] = 0.0;
-    for (int c = chunks - 1, k = 0; c >= 0; --c, ++k) {
+    for (int c = fce, k = 0; c >= ca; --c, ++k) {
         tcp_wait_one();
         __syncthreads();
         const double *bwd = reinterpret_cast<const double *>(bufs + (k % 3) * per_buffer) + kTChunk * fs;
         const int j0 = c * LC;
         if (!idle && active) {
             const int top = min(LC, n - j0) - 1;
-            double y_next = yplane[static_cast<std::int64_t>(j0 + top) * job.y_elem];
+            double y_next = yplane[static_cast<std::int64_t>(j0 + top - ybase) * job.y_elem];
+            const bool store = c < cb;
 #pragma unroll 1
             for (int t = top; t >= 0; --t) {
                 const double yt = y_next;
-                if (t > 0) y_next = yplane[static_cast<std::int64_t>(j0 + t - 1) * job.y_elem];
+                if (t > 0) y_next = yplane[static_cast<std::int64_t>(j0 + t - 1 - ybase) * job.y_elem];
                 const double *rec = bwd + t * bs;
                 double xt = yt;
 #pragma unroll
@@ -243,11 +257,11 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
 #pragma unroll
                 for (int d = HB - 1; d > 0; --d) x[d] = x[d - 1];
                 x[0] = xt;
-                out[static_cast<std::int64_t>(j0 + t) * job.out_elem] = xstore<Out>(xt, job.conv, flags);
+                if (store) out[static_cast<std::int64_t>(j0 + t) * job.out_elem] = xstore<Out>(xt, job.conv, flags);
             }
         }
         __syncthreads();
-        if (c - 2 >= 0) tstage(bufs + ((k + 2) % 3) * per_buffer, p, c - 2, tid, nthreads);
+        if (c - 2 >= ca) tstage(bufs + ((k + 2) % 3) * per_buffer, p, c - 2, tid, nthreads);
         tcp_commit();
     }
     if (flags && active) atomicOr(status, flags);

@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 from typing import Callable, Optional, Sequence
 
@@ -89,7 +90,9 @@ class StreamInfoC(C.Structure):
                 ("backward_transfer", C.c_double), ("reason", C.c_char * 96),
                 ("ring_ok_transposed", C.c_int32), ("exact", C.c_int32),
                 ("segmentable", C.c_int32), ("forward_transfer", C.c_double),
-                ("group_union", C.c_int32), ("group_stride", C.c_int32)]
+                ("group_union", C.c_int32), ("group_stride", C.c_int32),
+                ("f64_eligible", C.c_int32), ("f64_segmentable", C.c_int32),
+                ("f64_margin", C.c_int32), ("f64_margin_transfer", C.c_double)]
 
 
 class SweepOptionsC(C.Structure):
@@ -402,9 +405,14 @@ class Executor:
         _check(lib().dsmvc_gb_executor_create(int(device), C.byref(h)))
         self._h = h
         self._keep = []
+        # Batches, sweeps and request loops built on this executor: closed
+        # before it, whoever still holds them.
+        self._dependents = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
+            for d in list(getattr(self, "_dependents", ())):
+                d.close()
             _lib.dsmvc_gb_executor_destroy(self._h)
             self._h = None
 
@@ -544,6 +552,7 @@ class PreparedBatch:
         _check(lib().dsmvc_gb_batch_create(executor._h, _task_array(tasks), len(tasks), C.byref(h)))
         self._h = h
         self._executor = executor
+        executor._dependents.add(self)
         self._plans = [p for t in tasks for p in (t.horizontal, t.vertical) if p is not None]
 
     def launch(self, stream: int = 0) -> None:
@@ -581,6 +590,7 @@ class Sweep:
                                            int(frame_stride), C.byref(opts), C.byref(h)))
         self._h = h
         self._executor = executor
+        executor._dependents.add(self)
         self.count = n
 
     def run(self, stream: int = 0) -> None:
@@ -626,6 +636,7 @@ class Server:
         _check(lib().dsmvc_gb_server_create(executor._h, C.byref(opts), C.byref(h)))
         self._h = h
         self._executor = executor
+        executor._dependents.add(self)
         self._held = {}
 
     def submit(self, planes: Sequence[tuple]) -> int:
