@@ -313,7 +313,8 @@ def run_sweep(args, rank, world):
     base_h = int(rng.integers(600, 901))
     frame = synthetic.gray_frame(SWEEP_W, SWEEP_H, synthetic.sweep_width(base_h, SWEEP_W / SWEEP_H),
                                  base_h, seed=args.seed + 1)
-    cands = synthetic.native_resolution_candidates(SWEEP_W, SWEEP_H, SWEEP_HEIGHTS)
+    heights = range(SWEEP_HEIGHTS.start, SWEEP_HEIGHTS.stop, args.sweep_step)
+    cands = synthetic.native_resolution_candidates(SWEEP_W, SWEEP_H, heights)
     reqs = [r for c in cands for r in (c[3], c[4])]
     dframe = torch.from_numpy(frame).cuda()
     ex = gb.Executor(local)
@@ -375,7 +376,8 @@ def run_sweep(args, rank, world):
         for a, b, c in zip(idx, idx[1:], idx[2:]):
             dips[b] = float(scores[b] / min(scores[a], scores[c]))
     best = min(dips, key=dips.get)
-    base_idx = [i for i, c in enumerate(cands) if c[0] == "bicubic" and c[2] == base_h][0]
+    base_hits = [i for i, c in enumerate(cands) if c[0] == "bicubic" and c[2] == base_h]
+    base_idx = base_hits[0] if base_hits else None
 
     hbm, peak_kind = peaks()
     out_bytes = sum(c[1] * c[2] * 4 for c in cands)
@@ -782,6 +784,8 @@ def main():
     ap.add_argument("--serve-budget", type=int, default=8192, help="c4: arena MiB")
     ap.add_argument("--serve-streams", type=int, default=4)
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--sweep-step", type=int, default=1,
+                    help="c3: height step (1 = the full sweep; larger steps give small profiling cases)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="skip the end-to-end and CPU legs (profiling runs)")
     args = ap.parse_args()
