@@ -17,18 +17,34 @@ __device__ __forceinline__ int find_job(const ScoreJob *jobs, int count, int blo
     return lo;
 }
 
+// Row-pass value of one column over a staged-or-global descaled row: the
+// column's N entries (weights `w`, element offsets `c` from the row start)
+// in ascending order.
+template <int N>
+__device__ __forceinline__ float tap_sum(const float *__restrict__ y, const float (&w)[8], const int (&c)[8]) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int e = 0; e < N; ++e) acc = fmaf(w[e], __ldg(y + c[e]), acc);
+    return acc;
+}
+
 // Fused re-upscale and error sum of one column tile x one row segment of a
 // candidate: the row-pass values Z[j][s] = sum_c A_h[s, c] Y[j][c] of the
 // rows j the segment needs are computed into shared memory, then each
 // source row r of the segment is sum_j A_v[r, j] Z[j][s], compared with the
-// frame.  Errors are summed per block of kScoreRowBlock rows.
+// frame.  Errors are summed per block of kScoreRowBlock rows.  The row pass
+// runs an exact-length unrolled sum per column (entry counts 1..8, the
+// count being uniform away from the borders); the segment's A_v entries
+// and per-row entry ranges sit in shared memory, each entry one 8-byte
+// (weight, byte offset of its staged row) pair.  Every sum runs in
+// ascending entry order.
 __global__ void __launch_bounds__(kScoreThreads)
 score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     extern __shared__ float zt[];                  // [rows of the segment's span][kScoreThreads]
     __shared__ float warp_sums[kScoreThreads / 32];
-    __shared__ float seg_w[kScoreSegmentEntries];
-    __shared__ int seg_j[kScoreSegmentEntries];
-    __shared__ int span[2];
+    __shared__ float2 seg_e[kScoreSegmentEntries]; // (weight, byte offset of the staged row, as bits)
+    __shared__ int seg_r[kScoreMaxSegmentRows + 1];
+    __shared__ int span_lo[kScoreThreads / 32], span_hi[kScoreThreads / 32];
     const int b = static_cast<int>(blockIdx.x);
     const ScoreJob &job = jobs[find_job(jobs, count, b)];
     const int local = b - job.first_block;
@@ -37,30 +53,44 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     const int s = tile * kScoreThreads + tid;
     const int lane = tid & 31, warp = tid >> 5;
     const int r0 = segment * job.segment_rows, r1 = min(job.height, r0 + job.segment_rows);
-    if (tid == 0) {
-        // Descaled rows touched by the segment (A_v rows list ascending j).
+    {
+        // Descaled rows touched by the segment (A_v rows list ascending j):
+        // one segment row per thread, then a min / max reduction.
         int lo = job.rows, hi = -1;
-        for (int r = r0; r < r1; ++r) {
+        for (int r = r0 + tid; r < r1; r += kScoreThreads) {
             const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
             if (e0 < e1) {
                 lo = min(lo, job.v.indices[e0]);
                 hi = max(hi, job.v.indices[e1 - 1]);
             }
         }
-        span[0] = lo;
-        span[1] = hi;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            span_lo[warp] = lo;
+            span_hi[warp] = hi;
+        }
     }
     __syncthreads();
-    const int j_lo = span[0], nj = span[1] - span[0] + 1;
-    // The segment's A_v entries (weights and staged-row offsets) in shared
-    // memory when they fit; they are read by every thread.
+    int j_lo = span_lo[0], j_hi = span_hi[0];
+#pragma unroll
+    for (int w = 1; w < kScoreThreads / 32; ++w) {
+        j_lo = min(j_lo, span_lo[w]);
+        j_hi = max(j_hi, span_hi[w]);
+    }
+    const int nj = j_hi - j_lo + 1;
+    // The segment's A_v entries in shared memory when they fit; they are
+    // read by every thread.
     const std::uint32_t v0 = job.v.offsets[r0], v1 = job.v.offsets[r1];
-    const bool staged = v1 - v0 <= kScoreSegmentEntries;
+    const bool staged = v1 - v0 <= kScoreSegmentEntries && r1 - r0 <= kScoreMaxSegmentRows;
     if (staged) {
-        for (std::uint32_t e = v0 + tid; e < v1; e += kScoreThreads) {
-            seg_w[e - v0] = job.v.weights[e];
-            seg_j[e - v0] = (job.v.indices[e] - j_lo) * kScoreThreads;
-        }
+        for (std::uint32_t e = v0 + tid; e < v1; e += kScoreThreads)
+            seg_e[e - v0] = make_float2(job.v.weights[e],
+                                        __int_as_float((job.v.indices[e] - j_lo) * kScoreThreads * 4));
+        for (int r = r0 + tid; r <= r1; r += kScoreThreads) seg_r[r - r0] = static_cast<int>(job.v.offsets[r] - v0);
     }
     if (s < job.width) {
         // This column's A_h entries in registers (a tail beyond eight, rare,
@@ -70,39 +100,58 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
         constexpr int R = 8;
         float hw[R];
         int hc[R];
+        const int c0 = ne > 0 ? job.h.indices[e0] : 0;
 #pragma unroll
         for (int e = 0; e < R; ++e) {
             hw[e] = e < ne ? job.h.weights[e0 + e] : 0.0f;
-            hc[e] = e < ne ? job.h.indices[e0 + e] : 0;
+            hc[e] = e < ne ? job.h.indices[e0 + e] - c0 : 0;
         }
-        for (int jj = 0; jj < nj; ++jj) {
-            const float *y = job.descaled + static_cast<std::int64_t>(j_lo + jj) * job.descaled_stride;
-            float acc = 0.0f;
-#pragma unroll
-            for (int e = 0; e < R; ++e)
-                if (e < ne) acc = fmaf(hw[e], y[hc[e]], acc);
-            for (std::uint32_t e = e0 + R; e < e1; ++e) acc = fmaf(job.h.weights[e], y[job.h.indices[e]], acc);
-            zt[jj * kScoreThreads + tid] = acc;
+        const float *y = job.descaled + static_cast<std::int64_t>(j_lo) * job.descaled_stride + c0;
+        const std::int64_t ys = job.descaled_stride;
+        float *z = zt + tid;
+        switch (ne) {
+        case 0: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = 0.0f; break;
+        case 1: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<1>(y + jj * ys, hw, hc); break;
+        case 2: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<2>(y + jj * ys, hw, hc); break;
+        case 3: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<3>(y + jj * ys, hw, hc); break;
+        case 4: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<4>(y + jj * ys, hw, hc); break;
+        case 5: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<5>(y + jj * ys, hw, hc); break;
+        case 6: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<6>(y + jj * ys, hw, hc); break;
+        case 7: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<7>(y + jj * ys, hw, hc); break;
+        default:
+            for (int jj = 0; jj < nj; ++jj) {
+                const float *yr = y + jj * ys;
+                float acc = tap_sum<8>(yr, hw, hc);
+                for (std::uint32_t e = e0 + R; e < e1; ++e) acc = fmaf(job.h.weights[e], yr[job.h.indices[e] - c0], acc);
+                z[jj * kScoreThreads] = acc;
+            }
+            break;
         }
     }
     __syncthreads();
     const float *f = job.frame + s;
+    const char *zb = reinterpret_cast<const char *>(zt + tid);
     const int row_blocks = (job.height + kScoreRowBlock - 1) / kScoreRowBlock;
     const int seg_blocks = job.segment_rows / kScoreRowBlock;
     for (int rb = segment * seg_blocks; rb < min(row_blocks, (segment + 1) * seg_blocks); ++rb) {
         const int ra = rb * kScoreRowBlock, rz = min(job.height, ra + kScoreRowBlock);
         float sum = 0.0f;
         if (s < job.width) {
-            for (int r = ra; r < rz; ++r) {
-                const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
+            const float *fr = f + static_cast<std::int64_t>(ra) * job.frame_stride;
+            for (int r = ra; r < rz; ++r, fr += job.frame_stride) {
                 float acc = 0.0f;
                 if (staged) {
-                    for (std::uint32_t e = e0 - v0; e < e1 - v0; ++e) acc = fmaf(seg_w[e], zt[seg_j[e] + tid], acc);
+                    const int ea = seg_r[r - r0], ez = seg_r[r - r0 + 1];
+                    for (int e = ea; e < ez; ++e) {
+                        const float2 we = seg_e[e];
+                        acc = fmaf(we.x, *reinterpret_cast<const float *>(zb + __float_as_int(we.y)), acc);
+                    }
                 } else {
+                    const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
                     for (std::uint32_t e = e0; e < e1; ++e)
                         acc = fmaf(job.v.weights[e], zt[(job.v.indices[e] - j_lo) * kScoreThreads + tid], acc);
                 }
-                sum += fabsf(acc - f[static_cast<std::int64_t>(r) * job.frame_stride]);
+                sum += fabsf(acc - *fr);
             }
         }
 #pragma unroll

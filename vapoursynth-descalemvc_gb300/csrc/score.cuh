@@ -45,6 +45,7 @@ namespace dsmvc_gb {
 constexpr int kScoreThreads = 256;
 constexpr int kScoreRowBlock = 16;   // rows per partial sum
 constexpr int kScoreSegmentEntries = 2048;   // A_v entries of a segment staged in shared memory
+constexpr int kScoreMaxSegmentRows = 256;    // rows of a segment whose entry ranges are staged
 
 // Fused re-upscale + absolute error: one block per (column tile, row
 // segment); `max_span_rows` bounds the descaled rows any segment touches
