@@ -17,9 +17,8 @@ __device__ __forceinline__ int find_job(const ScoreJob *jobs, int count, int blo
     return lo;
 }
 
-// Row-pass value of one column over a staged-or-global descaled row: the
-// column's N entries (weights `w`, element offsets `c` from the row start)
-// in ascending order.
+// Row-pass value of one column over one descaled row: its N entries
+// (weights `w`, element offsets `c` from `y`) in ascending order.
 template <int N>
 __device__ __forceinline__ float tap_sum(const float *__restrict__ y, const float (&w)[8], const int (&c)[8]) {
     float acc = 0.0f;
@@ -28,22 +27,55 @@ __device__ __forceinline__ float tap_sum(const float *__restrict__ y, const floa
     return acc;
 }
 
+// The same for entries on consecutive columns y[0 .. N): immediate offsets.
+template <int N>
+__device__ __forceinline__ float tap_run(const float *__restrict__ y, const float (&w)[8]) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int e = 0; e < N; ++e) acc = fmaf(w[e], __ldg(y + e), acc);
+    return acc;
+}
+
+// Row pass of one column over descaled rows [0, nj) from y (row stride ys)
+// into z (stride kScoreThreads): `run` selects consecutive entries.
+template <int N>
+__device__ __forceinline__ void row_pass(float *z, const float *y, std::int64_t ys, int nj, bool run,
+                                         const float (&w)[8], const int (&c)[8]) {
+    if (run) {
+        for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_run<N>(y + jj * ys, w);
+    } else {
+        for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<N>(y + jj * ys, w, c);
+    }
+}
+
+// Column pass of one output row whose `count` entries (from `we`, each a
+// (weight, byte offset) pair) sit on consecutive staged rows from byte
+// offset `first` of this thread's column `zb`: immediate offsets.
+template <int N>
+__device__ __forceinline__ float col_run(const float2 *we, const char *zb) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int e = 0; e < N; ++e)
+        acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zb + e * kScoreThreads * 4), acc);
+    return acc;
+}
+
 // Fused re-upscale and error sum of one column tile x one row segment of a
 // candidate: the row-pass values Z[j][s] = sum_c A_h[s, c] Y[j][c] of the
 // rows j the segment needs are computed into shared memory, then each
 // source row r of the segment is sum_j A_v[r, j] Z[j][s], compared with the
-// frame.  Errors are summed per block of kScoreRowBlock rows.  The row pass
-// runs an exact-length unrolled sum per column (entry counts 1..8, the
-// count being uniform away from the borders); the segment's A_v entries
-// and per-row entry ranges sit in shared memory, each entry one 8-byte
-// (weight, byte offset of its staged row) pair.  Every sum runs in
-// ascending entry order.
+// frame.  Errors are summed per block of kScoreRowBlock rows.  Both passes
+// run exact-length unrolled sums, with immediate offsets where a column's
+// (row's) entries are consecutive, as they are away from the borders; the
+// segment's A_v entries sit in shared memory as (weight, byte offset of the
+// staged row) pairs with a per-row header (first entry, count, first
+// offset, consecutive).  Every sum runs in ascending entry order.
 __global__ void __launch_bounds__(kScoreThreads)
 score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     extern __shared__ float zt[];                  // [rows of the segment's span][kScoreThreads]
     __shared__ float warp_sums[kScoreThreads / 32];
     __shared__ float2 seg_e[kScoreSegmentEntries]; // (weight, byte offset of the staged row, as bits)
-    __shared__ int seg_r[kScoreMaxSegmentRows + 1];
+    __shared__ int4 seg_r[kScoreMaxSegmentRows];   // (first entry, count, first offset, consecutive)
     __shared__ int span_lo[kScoreThreads / 32], span_hi[kScoreThreads / 32];
     const int b = static_cast<int>(blockIdx.x);
     const ScoreJob &job = jobs[find_job(jobs, count, b)];
@@ -90,7 +122,14 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
         for (std::uint32_t e = v0 + tid; e < v1; e += kScoreThreads)
             seg_e[e - v0] = make_float2(job.v.weights[e],
                                         __int_as_float((job.v.indices[e] - j_lo) * kScoreThreads * 4));
-        for (int r = r0 + tid; r <= r1; r += kScoreThreads) seg_r[r - r0] = static_cast<int>(job.v.offsets[r] - v0);
+        for (int r = r0 + tid; r < r1; r += kScoreThreads) {
+            const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
+            const int n = static_cast<int>(e1 - e0);
+            const int first = n > 0 ? job.v.indices[e0] : j_lo;
+            const bool consecutive = n > 0 && job.v.indices[e1 - 1] - first == n - 1;
+            seg_r[r - r0] = make_int4(static_cast<int>(e0 - v0), n, (first - j_lo) * kScoreThreads * 4,
+                                      consecutive ? 1 : 0);
+        }
     }
     if (s < job.width) {
         // This column's A_h entries in registers (a tail beyond eight, rare,
@@ -106,18 +145,19 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
             hw[e] = e < ne ? job.h.weights[e0 + e] : 0.0f;
             hc[e] = e < ne ? job.h.indices[e0 + e] - c0 : 0;
         }
+        const bool run = ne > 0 && ne <= R && job.h.indices[e1 - 1] - c0 == ne - 1;
         const float *y = job.descaled + static_cast<std::int64_t>(j_lo) * job.descaled_stride + c0;
         const std::int64_t ys = job.descaled_stride;
         float *z = zt + tid;
         switch (ne) {
         case 0: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = 0.0f; break;
-        case 1: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<1>(y + jj * ys, hw, hc); break;
-        case 2: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<2>(y + jj * ys, hw, hc); break;
-        case 3: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<3>(y + jj * ys, hw, hc); break;
-        case 4: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<4>(y + jj * ys, hw, hc); break;
-        case 5: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<5>(y + jj * ys, hw, hc); break;
-        case 6: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<6>(y + jj * ys, hw, hc); break;
-        case 7: for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<7>(y + jj * ys, hw, hc); break;
+        case 1: row_pass<1>(z, y, ys, nj, run, hw, hc); break;
+        case 2: row_pass<2>(z, y, ys, nj, run, hw, hc); break;
+        case 3: row_pass<3>(z, y, ys, nj, run, hw, hc); break;
+        case 4: row_pass<4>(z, y, ys, nj, run, hw, hc); break;
+        case 5: row_pass<5>(z, y, ys, nj, run, hw, hc); break;
+        case 6: row_pass<6>(z, y, ys, nj, run, hw, hc); break;
+        case 7: row_pass<7>(z, y, ys, nj, run, hw, hc); break;
         default:
             for (int jj = 0; jj < nj; ++jj) {
                 const float *yr = y + jj * ys;
@@ -141,10 +181,27 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
             for (int r = ra; r < rz; ++r, fr += job.frame_stride) {
                 float acc = 0.0f;
                 if (staged) {
-                    const int ea = seg_r[r - r0], ez = seg_r[r - r0 + 1];
-                    for (int e = ea; e < ez; ++e) {
-                        const float2 we = seg_e[e];
-                        acc = fmaf(we.x, *reinterpret_cast<const float *>(zb + __float_as_int(we.y)), acc);
+                    const int4 h = seg_r[r - r0];
+                    const float2 *we = seg_e + h.x;
+                    const char *zr = zb + h.z;
+                    if (h.w) {
+                        switch (h.y) {
+                        case 1: acc = col_run<1>(we, zr); break;
+                        case 2: acc = col_run<2>(we, zr); break;
+                        case 3: acc = col_run<3>(we, zr); break;
+                        case 4: acc = col_run<4>(we, zr); break;
+                        case 5: acc = col_run<5>(we, zr); break;
+                        case 6: acc = col_run<6>(we, zr); break;
+                        case 7: acc = col_run<7>(we, zr); break;
+                        case 8: acc = col_run<8>(we, zr); break;
+                        default:
+                            for (int e = 0; e < h.y; ++e)
+                                acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zr + e * kScoreThreads * 4), acc);
+                            break;
+                        }
+                    } else {
+                        for (int e = 0; e < h.y; ++e)
+                            acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zb + __float_as_int(we[e].y)), acc);
                     }
                 } else {
                     const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
