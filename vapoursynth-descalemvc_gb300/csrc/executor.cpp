@@ -1285,15 +1285,47 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
     };
     auto pack = [](std::size_t v) { return (v + 15) / 16 * 16; };
     auto plane_bytes = [&](const HostPlane &p) { return pack(in_bytes(p)) + pack(out_bytes(p)); };
-    // Groups of consecutive planes within the byte target (at least one).
+    // Groups of consecutive planes.  Group boundaries sit at byte positions
+    // of the whole job: the first three groups grow (1/8, 1/4, 1/2 of
+    // group_bytes) and the last three shrink alike, so that the first upload
+    // and the last download, which nothing overlaps, stay short; the middle
+    // is cut into equal parts of at most group_bytes.  Jobs under twice the
+    // ramp split into four parts (1/6, 1/3, 1/3, 1/6).  A plane belongs to the
+    // part holding its middle byte; empty parts vanish.
+    std::size_t total = 0;
+    for (const auto &p : planes) total += plane_bytes(p);
+    std::vector<std::size_t> bounds;
+    const std::size_t up[3] = {group_bytes / 8, group_bytes / 8 + group_bytes / 4,
+                               group_bytes / 8 + group_bytes / 4 + group_bytes / 2};
+    if (total <= 2 * up[2]) {
+        bounds = {total / 6, total / 2, total - total / 6};
+    } else {
+        const std::size_t m0 = up[2], m1 = total - up[2];
+        const std::size_t parts = std::max<std::size_t>(1, (m1 - m0 + group_bytes - 1) / group_bytes);
+        bounds.assign(up, up + 3);
+        for (std::size_t k = 1; k < parts; ++k) bounds.push_back(m0 + (m1 - m0) * k / parts);
+        for (int k = 2; k >= 0; --k) bounds.push_back(total - up[k]);
+    }
     std::vector<std::pair<std::size_t, std::size_t>> groups;   // [first, last)
     std::size_t most = 0;
-    for (std::size_t i = 0; i < planes.size();) {
-        std::size_t j = i, bytes = 0;
-        while (j < planes.size() && (j == i || bytes + plane_bytes(planes[j]) <= group_bytes)) bytes += plane_bytes(planes[j++]);
-        groups.emplace_back(i, j);
+    {
+        std::size_t pos = 0, bi = 0, first = 0, bytes = 0;
+        for (std::size_t i = 0; i < planes.size(); ++i) {
+            const std::size_t pb = plane_bytes(planes[i]);
+            while (bi < bounds.size() && pos + pb / 2 >= bounds[bi]) {
+                if (i > first) {
+                    groups.emplace_back(first, i);
+                    most = std::max(most, bytes);
+                }
+                first = i;
+                bytes = 0;
+                ++bi;
+            }
+            bytes += pb;
+            pos += pb;
+        }
+        groups.emplace_back(first, planes.size());
         most = std::max(most, bytes);
-        i = j;
     }
     DeviceGuard guard(impl_->device);
     std::scoped_lock pipe_lock(impl_->pipe_mutex);
