@@ -315,7 +315,8 @@ struct Sweep::Impl {
         Wave &w = waves.front();
         std::map<std::array<int, 6>, std::pair<float, int>> best;
         const auto keys = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity)->groups();
-        for (const int threads : {32, 64, 128, 256}) {
+        // 32-thread CTAs never win on these kernels (one warp per record copy).
+        for (const int threads : {64, 128, 256}) {
             BatchTuning all;
             for (const auto &g : keys) {
                 const int most = g.kind >= 3 ? 256 : 128;
