@@ -211,3 +211,33 @@ def test_pipelined_planes_in_one_ring(gb, whole_executor):
     for (_h, _v, _x, out, _c), w in zip(planes, want):
         assert np.array_equal(out, w)
     assert np.all(ring_out[at_out:] == 0xABCD)
+
+
+@pytest.mark.gpu
+def test_pipelined_planes_direct_host_access(gb, whole_executor):
+    """DSMVC_GB_HOST_DIRECT=1: page-locked planes are read and written by the
+    kernels in place (no staging copies); pageable planes in the same call
+    still travel by copies.  Every output equals the copying executor's."""
+    torch = pytest.importorskip("torch")
+    from conftest import _executor_with
+    direct = _executor_with(gb, "DSMVC_GB_HOST_DIRECT", "1", DSMVC_GB_SEGMENTS="1")
+    conv = gb.integer_conversion(16, True, False)
+    h = gb.AxisPlan(product_request(gb, CHROMA_H), cached=False)
+    v = gb.AxisPlan(product_request(gb, CHROMA_V), cached=False)
+    planes, want = [], []
+    for i in range(6):
+        x = make_input(v.source_size, h.source_size, "u16", 700 + i)
+        if i % 3 != 2:
+            xin = torch.empty(x.shape, dtype=torch.int16, pin_memory=True).numpy().view(np.uint16)
+            out = torch.zeros((v.destination_size, h.destination_size), dtype=torch.int16,
+                              pin_memory=True).numpy().view(np.uint16)
+        else:
+            xin = np.empty_like(x)
+            out = np.zeros((v.destination_size, h.destination_size), np.uint16)
+        xin[...] = x
+        planes.append((h, v, xin, out, conv))
+        want.append(whole_executor.inverse_2d(h, v, x, conv))
+    direct.inverse_2d_planes(planes)
+    for (_h, _v, _x, out, _c), w in zip(planes, want):
+        assert np.array_equal(out, w)
+    direct.close()

@@ -343,6 +343,11 @@ struct Executor::Impl {
     std::mutex pipe_mutex;
     std::array<std::unique_ptr<Workspace>, 3> pipe;
     std::size_t pipe_group_bytes = 96ULL << 20;
+    // DSMVC_GB_HOST_DIRECT=1: planes of the multi-plane host call whose
+    // buffers are page-locked host memory are read and written by the
+    // kernels in place (mapped through unified addressing) instead of being
+    // staged by copies.
+    bool host_direct = false;
 
     // Optional per-launch CUDA-event timing (dsmvc_gb_profile).
     struct Record {
@@ -1094,6 +1099,7 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         impl_->allow_paired = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_EXACT"))
         impl_->prefer_exact = std::string(env) == "1";
+    if (const char *env = std::getenv("DSMVC_GB_HOST_DIRECT")) impl_->host_direct = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);
@@ -1359,13 +1365,30 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
         }
         r.bytes += bytes;
     };
+    // Device addresses of page-locked host buffers (DSMVC_GB_HOST_DIRECT=1):
+    // the kernels read such inputs and write such outputs in place.
+    auto mapped = [&](const void *ptr) -> void * {
+        if (!impl_->host_direct) return nullptr;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    };
+    std::vector<void *> direct_in(planes.size()), direct_out(planes.size());
+    for (std::size_t i = 0; i < planes.size(); ++i) {
+        direct_in[i] = mapped(planes[i].input);
+        direct_out[i] = mapped(planes[i].output);
+    }
     std::size_t used = 0;
     try {
         for (std::size_t g = 0; g < groups.size(); ++g) {
             Workspace &ws = *impl_->pipe[g % impl_->pipe.size()];
             used = std::max(used, g % impl_->pipe.size() + 1);
             std::size_t in_total = 0;
-            for (std::size_t i = groups[g].first; i < groups[g].second; ++i) in_total += pack(in_bytes(planes[i]));
+            for (std::size_t i = groups[g].first; i < groups[g].second; ++i)
+                if (!direct_in[i]) in_total += pack(in_bytes(planes[i]));
             char *din = ws.staging.data();
             char *dout = din + in_total;
             std::vector<PlaneTask> tasks;
@@ -1374,33 +1397,48 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
             for (std::size_t i = groups[g].first; i < groups[g].second; ++i) {
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
-                if (static_cast<std::size_t>(p.input_stride) * es == in_row(p)) {
-                    extend(run, p.input, din, in_bytes(p), cudaMemcpyHostToDevice, ws.stream, "uploading planes");
-                } else {
-                    flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
-                    cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
-                                          p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
-                               "uploading plane");
-                }
                 PlaneTask t;
                 t.horizontal = p.horizontal;
                 t.vertical = p.vertical;
                 t.horizontal_keep = p.horizontal_keep;
                 t.vertical_keep = p.vertical_keep;
-                t.input = din;
-                t.input_stride = p.horizontal->source_size;
-                t.output = dout;
-                t.output_stride = p.horizontal->destination_size;
                 t.sample = p.sample;
                 t.conversion = p.conversion;
+                if (direct_in[i]) {
+                    t.input = direct_in[i];
+                    t.input_stride = p.input_stride;
+                } else {
+                    if (static_cast<std::size_t>(p.input_stride) * es == in_row(p)) {
+                        extend(run, p.input, din, in_bytes(p), cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                    } else {
+                        flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                        cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
+                                              p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
+                                   "uploading plane");
+                    }
+                    t.input = din;
+                    t.input_stride = p.horizontal->source_size;
+                    din += pack(in_bytes(p));
+                }
+                if (direct_out[i]) {
+                    t.output = direct_out[i];
+                    t.output_stride = p.output_stride;
+                    outs.push_back(nullptr);
+                } else {
+                    t.output = dout;
+                    t.output_stride = p.horizontal->destination_size;
+                    outs.push_back(dout);
+                    dout += pack(out_bytes(p));
+                }
                 tasks.push_back(t);
-                outs.push_back(dout);
-                din += pack(in_bytes(p));
-                dout += pack(out_bytes(p));
             }
             flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
             impl_->enqueue(ws, tasks);
             for (std::size_t i = groups[g].first, k = 0; i < groups[g].second; ++i, ++k) {
+                if (!outs[k]) {
+                    flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
+                    continue;
+                }
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
                 if (static_cast<std::size_t>(p.output_stride) * es == out_row(p)) {
