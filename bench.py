@@ -369,13 +369,18 @@ def run_sweep(args, rank, world):
     plain_scores = sweep.scores(sid)
     plain = len(cands) / (time.perf_counter() - t3)
     # The native resolution shows as the sharpest dip of a kernel's score
-    # against its neighbouring heights.
-    dips = {}
+    # against its neighbouring heights.  Heights at an exact integer ratio of
+    # the source (1080 / 540 here) are left out: there a descale and its
+    # re-upscale fit smooth content closely for some kernels whatever the
+    # native resolution (Debilinear at 540 dips to 0.67, Debicubic and
+    # Delanczos do not dip there).
+    dips, by_height = {}, {}
     for k in synthetic.SWEEP_KERNELS:
         idx = [i for i, c in enumerate(cands) if c[0] == k]
         for a, b, c in zip(idx, idx[1:], idx[2:]):
             dips[b] = float(scores[b] / min(scores[a], scores[c]))
-    best = min(dips, key=dips.get)
+            by_height.setdefault(cands[b][2], {})[k] = dips[b]
+    best = min((i for i in dips if SWEEP_H % cands[i][2] != 0), key=dips.get)
     base_hits = [i for i, c in enumerate(cands) if c[0] == "bicubic" and c[2] == base_h]
     base_idx = base_hits[0] if base_hits else None
 
@@ -410,6 +415,8 @@ def run_sweep(args, rank, world):
                                "height": cands[best][2], "score": float(scores[best]),
                                "dip": dips[best]},
                   "found_base_height": cands[best][2] == base_h,
+                  "dips_at_detected_height": by_height.get(cands[best][2]),
+                  "dips_at_base_height": by_height.get(base_h),
                   "dip_at_base_bicubic": dips.get(base_idx),
                   "stages_ms": stages},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
