@@ -199,6 +199,8 @@ typedef struct dsmvc_gb_stream_info {
     int32_t f64_segmentable;     /* ... and their segments */
     int32_t f64_margin;          /* segment margin in chunks (0: none) */
     double f64_margin_transfer;  /* influence left after that margin (4 if none) */
+    int32_t exact_margin;        /* two-pass Float32 kernels' segment margin (0: none) */
+    double exact_margin_transfer;/* influence left after that margin (4 if none) */
 } dsmvc_gb_stream_info;
 int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan,
                               dsmvc_gb_stream_info *info, float *forward,

@@ -67,8 +67,9 @@ def seq_executor(gb):
 @pytest.fixture(scope="session")
 def exact_executor(gb):
     """An executor whose admitted 2D planes use the two-pass transposing
-    kernels (DSMVC_GB_EXACT=1)."""
-    ex = _executor_with(gb, "DSMVC_GB_EXACT", "1")
+    kernels (DSMVC_GB_EXACT=1) on whole vectors (DSMVC_GB_SEGMENTS=1): bit
+    for bit the reference CUDA operation order."""
+    ex = _executor_with(gb, "DSMVC_GB_EXACT", "1", DSMVC_GB_SEGMENTS="1")
     yield ex
     ex.close()
 

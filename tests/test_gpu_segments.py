@@ -114,3 +114,45 @@ def test_float64_segments_are_launched(gb, forced, whole_executor):
         sizes[label] = (b.info()["table_bytes"], b.info()["scratch_bytes"])
         b.close()
     assert sizes["forced"][0] > sizes["whole"][0] and sizes["forced"][1] > sizes["whole"][1]
+
+
+TWO_PASS_GEOMS = [
+    ("spline64-blur-hb9", (768, 512, 512.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0),
+     (432, 288, 288.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0), "f32"),
+    ("c1-luma-exact-u16", (1920, 1440, 1440.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0),
+     (1080, 810, 810.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "repeat", 0), "u16"),
+]
+
+
+@pytest.fixture(scope="module", params=[2, 5])
+def forced_exact(gb, request):
+    ex = _executor_with(gb, "DSMVC_GB_EXACT", "1", DSMVC_GB_SEGMENTS=str(request.param))
+    yield ex
+    ex.close()
+
+
+@pytest.mark.parametrize("name,hq,vq,sample", TWO_PASS_GEOMS, ids=[g[0] for g in TWO_PASS_GEOMS])
+def test_two_pass_segments(gb, forced_exact, exact_executor, name, hq, vq, sample):
+    """Two-pass Float32 kernels in segments (margins of 1-4 chunks admitted
+    below 2^-26): within 4e-7 of the largest magnitude (1 code) of whole
+    vectors, which follow the reference CUDA order bit for bit, and within
+    the reference tolerance of the CPU scalar route."""
+    h = gb.AxisPlan(product_request(gb, hq), cached=False)
+    v = gb.AxisPlan(product_request(gb, vq), cached=False)
+    assert h.stream_info()["exact_margin"] and v.stream_info()["exact_margin"]
+    x = make_input(v.source_size, h.source_size, sample, 93)
+    conv = gb.integer_conversion(16, False, False) if sample != "f32" else None
+    forced_exact.profile(True)
+    got = forced_exact.inverse_2d(h, v, x, conv)
+    names = {k["name"] for k in forced_exact.kernel_times()}
+    forced_exact.profile(False)
+    assert any(n.startswith("tsolve_f32") for n in names), names
+    whole = exact_executor.inverse_2d(h, v, x, conv)
+    scalar = O.inverse_2d(O.Plan(oracle_request(hq)), O.Plan(oracle_request(vq)), x, conv)
+    if sample == "f32":
+        assert np.abs(got - whole).max() <= 4e-7 * max(1.0, float(np.abs(whole).max()))
+        err = np.abs(got.astype(np.float64) - scalar)
+        assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS
+    else:
+        assert np.abs(got.astype(np.int64) - whole.astype(np.int64)).max() <= 1
+        assert np.abs(got.astype(np.int64) - scalar.astype(np.int64)).max() <= INT_MAX_CODES

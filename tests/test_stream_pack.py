@@ -307,3 +307,49 @@ def test_float64_segment_margins(gb, req):
             break
     assert info["f64_margin"] == want and bool(info["f64_segmentable"]) == (want > 0)
     assert info["f64_margin_transfer"] == pytest.approx(t, rel=1e-9, abs=1e-300)
+
+
+def exact_margin_transfer(info, p, margin):
+    """Influence left by a unit history (forward) or carry (backward) after
+    `margin` chunks of the packed Float32 records, in float64."""
+    fwd, bwd, K, hb = info["forward"], info["backward"], info["window"], p.half_bandwidth
+    n, chunk = p.destination_size, info["chunk"]
+    chunks = -(-n // chunk)
+    span = margin * chunk
+    worst = 0.0
+    for k in range(1, chunks):
+        a = k * chunk
+        if a + span > n:
+            break
+        for e in range(hb):
+            z = {a - 1 - e: 1.0}
+            for i in range(a, a + span):
+                z[i] = float(fwd[i, 1]) * sum(float(fwd[i, 4 + K + q]) * z.get(i - (hb - q), 0.0) for q in range(hb))
+            worst = max(worst, max(abs(z[a + span - 1 - q]) for q in range(hb)))
+            x = {a + span + e: 1.0}
+            for i in range(a + span - 1, a - 1, -1):
+                x[i] = -sum(float(bwd[i, q]) * x.get(i + (q + 1 if hb == 3 else hb - q), 0.0) for q in range(hb))
+            worst = max(worst, max(abs(x[a + q]) for q in range(hb)))
+    return worst
+
+
+@pytest.mark.parametrize("req", [
+    (300, 200, 200.0, 0.0, "spline64", 3, 0, 0.5, 1.1, "symmetric", 0),
+    (500, 470, 470.0, 0.0, "lanczos", 3, 0, 0.5, 1.0, "mirror", 0),
+])
+def test_two_pass_segment_margins(gb, req):
+    """The two-pass kernels' segment margin: the smallest of 1..4 chunks
+    leaving less than 2^-26, its transfer equal to a float64 restatement on
+    the packed records."""
+    p = gb.AxisPlan(product_request(gb, req), cached=False)
+    info = p.stream_info(records=True)
+    assert info["exact"]
+    chunks = -(-p.destination_size // info["chunk"])
+    want, t = 0, None
+    for margin in (1, 2, 3, 4):
+        t = exact_margin_transfer(info, p, margin)
+        if chunks >= 2 * margin + 1 and t <= 2.0 ** -26:
+            want = margin
+            break
+    assert info["exact_margin"] == want
+    assert info["exact_margin_transfer"] == pytest.approx(t, rel=1e-6, abs=1e-300)

@@ -262,6 +262,8 @@ int dsmvc_gb_plan_stream_info(const dsmvc_gb_plan *plan, dsmvc_gb_stream_info *i
         info->f64_eligible = pack64.eligible ? 1 : 0;
         info->f64_segmentable = pack64.segmentable ? 1 : 0;
         info->f64_margin = pack64.margin;
+        info->exact_margin = pack.exact_margin;
+        info->exact_margin_transfer = pack.exact_margin_transfer;
         info->f64_margin_transfer = pack64.margin_transfer;
         info->chunk = dsmvc_gb::kStreamChunk;
         info->ring = dsmvc_gb::kStreamRing;

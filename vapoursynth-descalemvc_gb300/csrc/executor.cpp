@@ -105,6 +105,8 @@ struct DevicePlan {
     // (stream_plan.hpp); the ring's first block of each chunk.
     bool stream_seg = false;
     std::vector<int> chunk_first_block;
+    // Two-pass transposing kernels in segments (StreamPack::exact_margin).
+    int exact_margin = 0;
     std::size_t bytes = 0;
 };
 
@@ -177,7 +179,8 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         dp->stream_u8 = pack.eligible && pack.ring_ok_u8;
         dp->stream_t = pack.eligible && pack.ring_ok_transposed;
         dp->stream_seg = dp->stream_t && pack.segmentable;
-        if (dp->stream_seg) dp->chunk_first_block = pack.chunk_first_block;
+        dp->exact_margin = pack.exact_margin;
+        if (dp->stream_seg || dp->exact_margin) dp->chunk_first_block = pack.chunk_first_block;
         dp->stream_x = pack.exact;
         dp->stream_xg = pack.exact && pack.ring_ok_transposed && pack.window == 8;
         auto &sv = dp->stream_view;
@@ -566,12 +569,13 @@ std::size_t segment64_chunks(int destinations, int segments, int margin) {
     return total;
 }
 
-// One Float64 two-pass job, or its segments: chunk ranges, each with its
-// forward-value region in `yseg` (rows of `pitch` doubles, starting at the
+// One two-pass job (Float64 or Float32), or its segments: chunk ranges with
+// `margin` chunks on either side, each with its forward-value region in
+// `yseg` (rows of `pitch` elements of `elem` bytes, starting at the
 // segment's first computed chunk) and its ring's first block.
 template <class Item>
-void push_segments64(std::vector<Item> &group, const Item &whole, const DevicePlan &dp, int destinations,
-                     int segments, char *yseg, std::int64_t pitch) {
+void push_segments(std::vector<Item> &group, const Item &whole, const std::vector<int> &first_blocks, int margin,
+                   int destinations, int segments, char *yseg, std::int64_t pitch, std::size_t elem) {
     if (segments <= 1) {
         group.push_back(whole);
         return;
@@ -581,14 +585,14 @@ void push_segments64(std::vector<Item> &group, const Item &whole, const DevicePl
     for (int k = 0; k < segments; ++k) {
         const int begin = static_cast<int>(static_cast<long>(k) * chunks / segments);
         const int end = static_cast<int>(static_cast<long>(k + 1) * chunks / segments);
-        const int first = std::max(begin - dp.margin64, 0);
-        const int last = std::min(end + dp.margin64, chunks);
+        const int first = std::max(begin - margin, 0);
+        const int last = std::min(end + margin, chunks);
         Item it = whole;
         it.stream.chunk_begin = begin;
         it.stream.chunk_end = end;
-        it.stream.first_sample = dp.chunk_first_block64[static_cast<std::size_t>(first)];
-        it.stream.margin = dp.margin64;
-        it.stream.y = reinterpret_cast<float *>(yseg + at * kStreamChunk * static_cast<std::size_t>(pitch) * 8);
+        it.stream.first_sample = first_blocks[static_cast<std::size_t>(first)];
+        it.stream.margin = margin;
+        it.stream.y = reinterpret_cast<float *>(yseg + at * kStreamChunk * static_cast<std::size_t>(pitch) * elem);
         it.stream.y_elem = pitch;
         at += static_cast<std::size_t>(last - first);
         group.push_back(it);
@@ -727,18 +731,48 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     // Float64 segments: each pass's kind-6 warps decide the split (as for the
     // chunk-delayed kernels); every segment writes its forward values, its
     // margins included, to a scratch region of its own.
+    // The two-pass Float32 kernels (kind 5) split alike, with their own
+    // margins and Float32 forward values.
     {
-        long warps64[2] = {0, 0};
+        long warps64[2] = {0, 0}, warps32[2] = {0, 0};
         for (std::size_t t = 0; t < tasks.size(); ++t) {
-            if (!routes[t].transposed64) continue;
-            warps64[0] += (tasks[t].vertical->source_size + 31) / 32;
-            warps64[1] += (tasks[t].horizontal->destination_size + 31) / 32;
+            const auto &r = routes[t];
+            if (r.transposed64) {
+                warps64[0] += (tasks[t].vertical->source_size + 31) / 32;
+                warps64[1] += (tasks[t].horizontal->destination_size + 31) / 32;
+            }
+            if (r.transposed && r.h_kind == 5) warps32[0] += (tasks[t].vertical->source_size + 31) / 32;
+            if (r.transposed && r.v_kind == 5) warps32[1] += (tasks[t].horizontal->destination_size + 31) / 32;
+        }
+        auto split32 = [&](const DevicePlan &dp, int destinations, long warps) {
+            if (!dp.exact_margin || segment_mode == 1) return 1;
+            const int chunks = (destinations + kStreamChunk - 1) / kStreamChunk;
+            int s = segment_mode >= 2 ? segment_mode
+                                      : (warps > 0 ? static_cast<int>(std::min<long>(warp_slots / (2 * warps), 64)) : 1);
+            return std::max(1, std::min(s, chunks / (2 * dp.exact_margin + 1)));
+        };
+        for (std::size_t t = 0; t < tasks.size(); ++t) {
+            auto &r = routes[t];
+            if (!r.transposed) continue;
+            const AxisPlan *h = tasks[t].horizontal, *v = tasks[t].vertical;
+            if (r.h_kind == 5 && (r.seg_h = split32(*r.h, h->destination_size, warps32[0])) > 1) {
+                r.yseg_h = bytes;
+                bytes += align_up(segment64_chunks(h->destination_size, r.seg_h, r.h->exact_margin) * kStreamChunk
+                                  * r.mid_stride * 4);
+            }
+            if (r.v_kind == 5 && (r.seg_v = split32(*r.v, v->destination_size, warps32[1])) > 1) {
+                r.yseg_v = bytes;
+                bytes += align_up(segment64_chunks(v->destination_size, r.seg_v, r.v->exact_margin) * kStreamChunk
+                                  * static_cast<std::size_t>(h->destination_size) * 4);
+            }
         }
         auto split = [&](const DevicePlan &dp, int destinations, long warps) {
             if (!dp.stream64_seg || segment_mode == 1) return 1;
             const int chunks = (destinations + kStreamChunk - 1) / kStreamChunk;
+            // Margins cost 2 x margin chunks a boundary: split only launches
+            // that fill less than half of the GPU's warp slots.
             int s = segment_mode >= 2 ? segment_mode
-                                      : (warps > 0 ? static_cast<int>(std::min<long>(warp_slots / warps, 64)) : 1);
+                                      : (warps > 0 ? static_cast<int>(std::min<long>(warp_slots / (2 * warps), 64)) : 1);
             return std::max(1, std::min(s, chunks / (2 * dp.margin64)));
         };
         for (std::size_t t = 0; t < tasks.size(); ++t) {
@@ -790,8 +824,9 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             a.y = static_cast<float *>(mid); a.y_elem = pitch;   // Float64 forward values in place
             a.vectors = v->source_size;
             a.conv = conv;
-            push_segments64(groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}], hi, *r.h,
-                            h->destination_size, r.seg_h, base + r.yseg_h, pitch);
+            push_segments(groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}], hi,
+                          r.h->chunk_first_block64, r.h->margin64, h->destination_size, r.seg_h, base + r.yseg_h, pitch,
+                          8);
             auto &b = vi.stream;
             b.plan = r.v->stream_view64;
             b.in = mid; b.in_elem = 1; b.in_vec = pitch;
@@ -799,8 +834,9 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             b.y = reinterpret_cast<float *>(base + r.fwd); b.y_elem = static_cast<std::int64_t>(r.fwd_stride);
             b.vectors = h->destination_size;
             b.conv = conv;
-            push_segments64(groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}], vi, *r.v,
-                            v->destination_size, r.seg_v, base + r.yseg_v, static_cast<std::int64_t>(r.fwd_stride));
+            push_segments(groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}], vi,
+                          r.v->chunk_first_block64, r.v->margin64, v->destination_size, r.seg_v, base + r.yseg_v,
+                          static_cast<std::int64_t>(r.fwd_stride), 8);
             continue;
         }
         if (r.transposed) {
@@ -820,8 +856,13 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.vectors = v->source_size;
                 j.conv = conv;
                 hi.plan = r.h;
-                groups[{0, r.h_kind, h->half_bandwidth, task.sample, dev::Sample::f32,
-                        compiled_window(*r.h, r.h_kind)}].push_back(hi);
+                auto &group = groups[{0, r.h_kind, h->half_bandwidth, task.sample, dev::Sample::f32,
+                                      compiled_window(*r.h, r.h_kind)}];
+                if (r.h_kind == 5)
+                    push_segments(group, hi, r.h->chunk_first_block, r.h->exact_margin, h->destination_size, r.seg_h,
+                                  base + r.yseg_h, pitch, 4);
+                else
+                    group.push_back(hi);
             } else {
                 auto &j = hi.axis;
                 j.plan = r.h->view;
@@ -848,8 +889,13 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.vectors = h->destination_size;
                 j.conv = conv;
                 vi.plan = r.v;
-                groups[{1, r.v_kind, v->half_bandwidth, dev::Sample::f32, task.sample,
-                        compiled_window(*r.v, r.v_kind)}].push_back(vi);
+                auto &group = groups[{1, r.v_kind, v->half_bandwidth, dev::Sample::f32, task.sample,
+                                      compiled_window(*r.v, r.v_kind)}];
+                if (r.v_kind == 5)
+                    push_segments(group, vi, r.v->chunk_first_block, r.v->exact_margin, v->destination_size, r.seg_v,
+                                  base + r.yseg_v, static_cast<std::int64_t>(h->destination_size), 4);
+                else
+                    group.push_back(vi);
             } else {
                 auto &j = vi.axis;
                 j.plan = r.v->view;
@@ -1609,9 +1655,9 @@ std::size_t PreparedBatch::table_bytes() const { return impl_->compiled.table.si
 std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
     // Per task: the intermediate plane (destinations of the first pass x
     // sources of the second, rows padded to 4) plus a forward plane of the
-    // output's size, in the route's sample width; Float64 2D planes also the
-    // forward values of their segments (margins included, at most twice a
-    // pass's whole chunks of forward values).
+    // output's size, in the route's sample width; 2D planes also the forward
+    // values of two-pass segments (margins included, at most twice a pass's
+    // whole chunks of forward values).
     std::size_t bytes = kAlign;
     for (const auto &t : tasks) {
         const AxisPlan *h = t.horizontal, *v = t.vertical;
@@ -1622,10 +1668,10 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
         const std::size_t vs = v ? (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4 : static_cast<std::size_t>(t.vectors);
         const std::size_t vd = v ? static_cast<std::size_t>(v->destination_size) : static_cast<std::size_t>(t.vectors);
         bytes += align_up(hd * vs * es) + align_up(hd * vd * es);
-        if (f64 && h && v) {
+        if (h && v) {
             const std::size_t hc = (hd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
             const std::size_t vc = (vd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
-            bytes += align_up(2 * hc * vs * 8) + align_up(2 * vc * hd * 8);
+            bytes += align_up(2 * hc * vs * es) + align_up(2 * vc * hd * es);
         }
     }
     return bytes;

@@ -228,6 +228,50 @@ StreamPack pack_stream_plan(const AxisPlan &p, int chunk, int ring, bool hb_supp
         }
     }
     out.segmentable = delayed && out.ring_ok_transposed && fworst <= std::ldexp(1.0, -26);
+    if (out.exact) {
+        const auto fs = static_cast<std::size_t>(out.forward_stride), bs = static_cast<std::size_t>(out.backward_stride);
+        auto transfer = [&](int margin) {
+            const int span = margin * chunk;
+            double t = 0.0;
+            std::vector<double> z(static_cast<std::size_t>(span + hb));
+            for (int k = 1; k < chunks; ++k) {
+                const int a = k * chunk;
+                if (a + span > n) break;
+                for (int e = 0; e < hb; ++e) {
+                    std::fill(z.begin(), z.end(), 0.0);
+                    z[static_cast<std::size_t>(hb - 1 - e)] = 1.0;           // z[i]: position a - hb + i
+                    for (int i = a; i < a + span; ++i) {
+                        const float *f = out.forward.data() + static_cast<std::size_t>(i) * fs;
+                        double s = 0.0;
+                        for (int q = 0; q < hb; ++q)
+                            s += static_cast<double>(f[4 + window + q]) * z[static_cast<std::size_t>(i - (hb - q) - a + hb)];
+                        z[static_cast<std::size_t>(i - a + hb)] = s * static_cast<double>(f[1]);
+                    }
+                    for (int q = 0; q < hb; ++q) t = std::max(t, std::abs(z[static_cast<std::size_t>(span + q)]));
+                    std::fill(z.begin(), z.end(), 0.0);
+                    z[static_cast<std::size_t>(span + e)] = 1.0;             // z[i]: position a + i
+                    for (int i = a + span - 1; i >= a; --i) {
+                        const float *b = out.backward.data() + static_cast<std::size_t>(i) * bs;
+                        double s = 0.0;
+                        for (int q = 0; q < hb; ++q) {
+                            const int d = hb == 3 ? q + 1 : hb - q;
+                            s += static_cast<double>(b[q]) * z[static_cast<std::size_t>(i + d - a)];
+                        }
+                        z[static_cast<std::size_t>(i - a)] = -s;
+                    }
+                    for (int q = 0; q < hb; ++q) t = std::max(t, std::abs(z[static_cast<std::size_t>(q)]));
+                }
+            }
+            return t;
+        };
+        for (int margin = 1; margin <= 4; ++margin) {
+            out.exact_margin_transfer = transfer(margin);
+            if (chunks >= 2 * margin + 1 && out.exact_margin_transfer <= std::ldexp(1.0, -26)) {
+                out.exact_margin = margin;
+                break;
+            }
+        }
+    }
     out.chunk_first_block.resize(static_cast<std::size_t>(chunks));
     for (int k = 0; k < chunks; ++k) out.chunk_first_block[static_cast<std::size_t>(k)] = s0[static_cast<std::size_t>(k) * chunk] / 16 * 16;
 

@@ -47,6 +47,13 @@ struct StreamPack {
     std::vector<float> backward_groups;
     bool segmentable = false;
     double forward_transfer = 0.0;  // max |history -> state| over one chunk
+    // Segments of the two-pass transposing kernels (exact plans): forward
+    // sweep from `exact_margin` chunks before a range (zero history),
+    // backward sweep from as many after it (zero carry), within the vector;
+    // the smallest margin of 1..4 chunks leaving below 2^-26 of a unit
+    // history or carry from every chunk boundary (in double), 0 when none.
+    int exact_margin = 0;
+    double exact_margin_transfer = 0.0;
     // Window start of each chunk's first destination, rounded down to the
     // 16-sample feeding block: where a segment's warm-up starts its ring.
     std::vector<int> chunk_first_block;

@@ -37,8 +37,21 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
     // Jobs are assigned warps; a CTA's warps share one plan.
     const int cta_warp = static_cast<int>(blockIdx.x) * (nthreads >> 5);
     const StreamJob &job = jobs[find_tjob(jobs, job_count, cta_warp + warp)];
-    const dev::StreamPlanView p = jobs[find_tjob(jobs, job_count, cta_warp)].plan;
+    const StreamJob &lead = jobs[find_tjob(jobs, job_count, cta_warp)];
+    const dev::StreamPlanView p = lead.plan;
     const int n = p.destination_size;
+    const int chunks = (n + LC - 1) / LC;
+    // Chunks stored: [ca, cb); a segment (chunk_end > 0) sweeps forward over
+    // [fc0, fce] from a zero history and backward from a zero carry after
+    // fce, `margin` chunks beyond its range on either side (within the
+    // vector), with its forward values in its own region from chunk fc0 on.
+    // Every warp of a CTA serves the same plan and range.
+    const bool segment = lead.chunk_end > 0;
+    const int ca = lead.chunk_begin;
+    const int cb = segment ? lead.chunk_end : chunks;
+    const int fc0 = segment ? max(ca - lead.margin, 0) : 0;
+    const int fce = segment ? min(cb + lead.margin, chunks) - 1 : chunks - 1;
+    const int ybase = fc0 * LC;
     const int per_buffer = kTChunk * record_floats;
     float *bufs = smem;
     float *ring = smem + 3 * per_buffer + warp * kTRingFloats;
@@ -65,23 +78,24 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
-    if (!idle) feed.start();
+    if (!idle) feed.start(fc0 > 0 ? lead.first_sample : 0);
 
-    float *yplane = job.y + v;
+    // Forward value of destination j at yplane[j * y_elem] (a segment's
+    // region starts at its first computed destination).
+    float *yplane = job.y + v - static_cast<std::int64_t>(ybase) * job.y_elem;
     Out *out = static_cast<Out *>(job.out) + v;
     const int fs = fwd_stride<HB, K>(p), bs = bwd_stride<HB, K>(p);
     const int kw = K > 0 ? K : p.window;
-    const int chunks = (n + LC - 1) / LC;
 
     // ---- forward sweep ---------------------------------------------------
-    tstage(bufs, p, 0, tid, nthreads);
+    tstage(bufs + (fc0 % 3) * per_buffer, p, fc0, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, 1, tid, nthreads);
+    if (fc0 + 1 <= fce) tstage(bufs + ((fc0 + 1) % 3) * per_buffer, p, fc0 + 1, tid, nthreads);
     tcp_commit();
     float hist[HB];
 #pragma unroll
     for (int d = 0; d < HB; ++d) hist[d] = 0.0f;
-    for (int c = 0; c < chunks; ++c) {
+    for (int c = fc0; c <= fce; ++c) {
         tcp_wait_one();
         __syncthreads();
         const float *fwd = bufs + (c % 3) * per_buffer;
@@ -142,22 +156,23 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
             for (int d = 0; d < HB; ++d) hist[d] = y[LC - HB + d];
         }
         __syncthreads();
-        if (c + 2 < chunks) tstage(bufs + ((c + 2) % 3) * per_buffer, p, c + 2, tid, nthreads);
+        if (c + 2 <= fce) tstage(bufs + ((c + 2) % 3) * per_buffer, p, c + 2, tid, nthreads);
         tcp_commit();
     }
 
     // ---- backward sweep --------------------------------------------------
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncthreads();
-    tstage(bufs, p, chunks - 1, tid, nthreads);
+    tstage(bufs, p, fce, tid, nthreads);
     tcp_commit();
-    if (chunks > 1) tstage(bufs + per_buffer, p, chunks - 2, tid, nthreads);
+    if (fce - 1 >= ca) tstage(bufs + per_buffer, p, fce - 1, tid, nthreads);
     tcp_commit();
     float carry[HB];
 #pragma unroll
     for (int d = 0; d < HB; ++d) carry[d] = 0.0f;
-    for (int c = chunks - 1, k = 0; c >= 0; --c, ++k) {
+    for (int c = fce, k = 0; c >= ca; --c, ++k) {
         const int j0 = c * LC;
+        const bool store = active && c < cb;
         float yv[LC];
         if (!idle) {
 #pragma unroll
@@ -189,13 +204,13 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
                 }
                 const float xt = yv[t] - sum;
                 x[t % HB] = xt;
-                if (active && j0 + t < n) out[static_cast<std::int64_t>(j0 + t) * job.out_elem] = tout<Out>(xt, job.conv);
+                if (store && j0 + t < n) out[static_cast<std::int64_t>(j0 + t) * job.out_elem] = tout<Out>(xt, job.conv);
             }
 #pragma unroll
             for (int d = 0; d < HB; ++d) carry[d] = x[d];
         }
         __syncthreads();
-        if (c - 2 >= 0) tstage(bufs + ((k + 2) % 3) * per_buffer, p, c - 2, tid, nthreads);
+        if (c - 2 >= ca) tstage(bufs + ((k + 2) % 3) * per_buffer, p, c - 2, tid, nthreads);
         tcp_commit();
     }
 }

@@ -92,7 +92,8 @@ class StreamInfoC(C.Structure):
                 ("segmentable", C.c_int32), ("forward_transfer", C.c_double),
                 ("group_union", C.c_int32), ("group_stride", C.c_int32),
                 ("f64_eligible", C.c_int32), ("f64_segmentable", C.c_int32),
-                ("f64_margin", C.c_int32), ("f64_margin_transfer", C.c_double)]
+                ("f64_margin", C.c_int32), ("f64_margin_transfer", C.c_double),
+                ("exact_margin", C.c_int32), ("exact_margin_transfer", C.c_double)]
 
 
 class SweepOptionsC(C.Structure):
@@ -320,7 +321,7 @@ class AxisPlan:
         _check(lib().dsmvc_gb_plan_stream_info(self._h, C.byref(info), None, 0, None, 0))
         out = {k: getattr(info, k) for k, _ in info._fields_}
         out["reason"] = info.reason.decode()
-        if records and info.eligible:
+        if records and (info.eligible or info.exact):
             # Records cover whole chunks: zero records past the last destination.
             n = -(-self.destination_size // info.chunk) * info.chunk
             fwd = np.zeros(n * info.forward_stride, np.float32)
