@@ -16,7 +16,6 @@
 #define ORC_PI 3.141592653589793238462643383279502884
 
 static int32_t imin(int32_t a, int32_t b) { return a < b ? a : b; }
-static int32_t imax(int32_t a, int32_t b) { return a > b ? a : b; }
 
 /* ---- Kernel weights: src/axis_plan.cpp:246-344 ------------------------- */
 
@@ -353,7 +352,7 @@ static void condition_bounds(const double *bands, int32_t n, int32_t hb,
             work[col + d] += v;
         }
     }
-    double norm = work[0];
+    double norm = n > 0 ? work[0] : 0.0;
     for (int32_t i = 1; i < n; ++i) if (norm < work[i]) norm = work[i];
     double margin = INFINITY;
     for (int32_t row = 0; row < n; ++row) {
