@@ -243,6 +243,9 @@ struct Workspace {
     DeviceBuffer jobs;
     std::uint32_t *status = nullptr;      // device
     std::uint32_t *status_host = nullptr; // pinned
+    // A Float64 kernel (the only kernels that set the status word) ran on
+    // this stream since the status was last read.
+    bool status_pending = false;
     std::vector<char> host_table;
     // Job tables travel through two pinned slots, each reused only after
     // its previous copy has finished; an unchanged table is not copied.
@@ -1110,6 +1113,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
     if (c.launches.empty()) return;
     ws.upload_table(c.table);
     launch(c, ws.jobs.data(), ws.stream, ws.status);
+    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind == 6;
     if (c.private_uploads > 0) {
         // Private plan uploads must outlive the kernels that read them.
         // (Cached plans evicted meanwhile are released by cudaFree, which
@@ -1119,6 +1123,12 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
 }
 
 void Executor::Impl::finish(Workspace &ws) {
+    if (!ws.status_pending) {
+        // Only the Float64 kernels set the status word: nothing to read.
+        cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
+        return;
+    }
+    ws.status_pending = false;
     cuda_check(cudaMemcpyAsync(ws.status_host, ws.status, sizeof(std::uint32_t),
                                cudaMemcpyDeviceToHost, ws.stream), "reading status");
     cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
