@@ -79,7 +79,9 @@ template <> __device__ __forceinline__ float tout<float>(float v, const Conversi
 __device__ __forceinline__ float4 tlds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
 // Predicated global stores of one output sample: no branch around the
-// store, and the address is known to be global.
+// store, and the address is known to be global.  No memory clobber: the
+// kernels never read what they store through these (outputs only), and the
+// compiler stays free to move shared-memory loads across the stores.
 __device__ __forceinline__ void tst(float *p, float v, bool pred) {
     asm volatile("{\n .reg .pred q;\n setp.ne.b32 q, %2, 0;\n @q st.global.f32 [%0], %1;\n}\n"
                  :: "l"(p), "f"(v), "r"(static_cast<int>(pred)));
