@@ -1,5 +1,6 @@
 // Candidate scoring kernels (score.cuh).
 #include "score.cuh"
+#include "smem_limit.cuh"
 
 #include <cuda_runtime.h>
 
@@ -248,13 +249,8 @@ int launch_score_tiles(const dev::ScoreJob *jobs, int count, int blocks, int max
     const int smem = max_span_rows * kScoreThreads * static_cast<int>(sizeof(float));
     // The kernel's static shared memory counts against the default 48 KiB
     // too, so the dynamic limit is raised for any size not configured yet.
-    static int configured = 0;
-    if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(score_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   smem);
-        if (e != cudaSuccess) return static_cast<int>(e);
-        configured = smem;
-    }
+    static SmemLimit limit;
+    if (const cudaError_t e = limit.ensure(score_tiles_kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     score_tiles_kernel<<<blocks, kScoreThreads, smem, static_cast<cudaStream_t>(stream)>>>(jobs, count);
     return static_cast<int>(cudaGetLastError());
 }

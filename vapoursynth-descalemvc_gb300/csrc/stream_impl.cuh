@@ -24,6 +24,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "smem_limit.cuh"
 #include "stream.cuh"
 
 #include <cuda_runtime.h>
@@ -361,12 +362,8 @@ int launch_typed(const StreamJob *jobs, int count, int blocks, int record_floats
     const int per_buffer = kChunk * record_floats;
     const int smem = kWarps * (kRingFloats + 3 * per_buffer) * static_cast<int>(sizeof(float));
     auto kernel = stream_kernel<HB, LC, In, Out, CONTIG>;
-    static int configured = 0;
-    if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return static_cast<int>(e);
-        configured = smem;
-    }
+    static SmemLimit limit;
+    if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     kernel<<<blocks, kThreads, smem, s>>>(jobs, count, per_buffer);
     return static_cast<int>(cudaGetLastError());
 }

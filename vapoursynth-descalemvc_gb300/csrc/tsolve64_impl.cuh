@@ -274,12 +274,8 @@ int x64launch_typed(const StreamJob *jobs, int count, int blocks, int threads, i
     const int smem = 3 * kTChunk * record_floats * static_cast<int>(sizeof(float))
         + threads / 32 * kXRingDoubles * static_cast<int>(sizeof(double));
     auto kernel = tsolve64_kernel<HB, In, Out>;
-    static int configured = 0;
-    if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return static_cast<int>(e);
-        configured = smem;
-    }
+    static SmemLimit limit;
+    if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     kernel<<<blocks, threads, smem, s>>>(jobs, count, record_floats, status);
     return static_cast<int>(cudaGetLastError());
 }

@@ -27,6 +27,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "smem_limit.cuh"
 #include "stream.cuh"
 
 #include <cuda_runtime.h>
@@ -414,12 +415,8 @@ int plaunch_typed(const StreamJob *jobs, int count, int blocks, int threads, int
     const int smem = (3 * kPChunk * record_floats + threads / 32 * (kPRingFloats + kPYFloats))
         * static_cast<int>(sizeof(float));
     auto kernel = tstream2_kernel<HB, K, In, Out>;
-    static int configured = 0;
-    if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return static_cast<int>(e);
-        configured = smem;
-    }
+    static SmemLimit limit;
+    if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     kernel<<<blocks, threads, smem, s>>>(jobs, count, record_floats);
     return static_cast<int>(cudaGetLastError());
 }

@@ -28,6 +28,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "smem_limit.cuh"
 #include "stream.cuh"
 
 #include <cuda_runtime.h>
@@ -507,12 +508,8 @@ int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int threads, int
     if (threads < 32 || threads > kTMaxThreads || threads % 32) return static_cast<int>(cudaErrorInvalidValue);
     const int smem = (3 * kTChunk * record_floats + threads / 32 * kTRingFloats) * static_cast<int>(sizeof(float));
     auto kernel = tstream_kernel<HB, LC, K, In, Out>;
-    static int configured = 0;
-    if (smem > configured) {
-        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return static_cast<int>(e);
-        configured = smem;
-    }
+    static SmemLimit limit;
+    if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     kernel<<<blocks, threads, smem, s>>>(jobs, count, record_floats);
     return static_cast<int>(cudaGetLastError());
 }
