@@ -225,7 +225,15 @@ def test_segment_admission_and_emulation(gb, name, req, eligible):
             assert np.max(np.abs(v - whole[:, j])) <= 2e-7 * scale
 
 
-@pytest.mark.parametrize("name,req,eligible", CASES[:6], ids=[c[0] for c in CASES[:6]])
+# 4K Debicubic(1/3, 1/3) with blur 1.1: seven taps 1.5 samples apart, so the
+# groups of four need the 16-sample union (the cases above take 12 or none).
+GROUPED_16 = [
+    ("bicubic-blur-3840-2560", (3840, 2560, 2560.0, 0.0, "bicubic", 3, 1 / 3, 1 / 3, 1.1, "symmetric", 0), True),
+    ("bicubic-blur-2160-1440", (2160, 1440, 1440.0, 0.0, "bicubic", 3, 1 / 3, 1 / 3, 1.1, "symmetric", 0), True),
+]
+
+
+@pytest.mark.parametrize("name,req,eligible", CASES[:6] + GROUPED_16, ids=[c[0] for c in CASES[:6] + GROUPED_16])
 def test_grouped_records(gb, name, req, eligible):
     """Grouped records of the 2D chunk-delayed kernels restate the
     per-destination records: each group of four destinations carries the
@@ -242,6 +250,8 @@ def test_grouped_records(gb, name, req, eligible):
     span = max(int(starts[g + 3]) + K - int(starts[g]) for g in range(0, len(starts), 4))
     want_u = 12 if span <= 12 else 16 if span <= 16 else 0
     assert info["group_union"] == want_u
+    if any(name == c[0] for c in GROUPED_16):
+        assert want_u == 16
     if not want_u:
         return
     U = want_u
