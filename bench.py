@@ -37,10 +37,13 @@ SRC_W, SRC_H, DST_W, DST_H = 1920, 1080, 1440, 810
 FRAMES = 64
 KERNEL = dict(kernel="lanczos", taps=3, b=0.0, c=0.5, blur=1.0, border="repeat", f64_mode=0)
 METRIC = "descale Mpix/s (source pixels, Delanczos YUV420P16 1920x1080->1440x810)"
-# DRAM bytes (read + write) per frame of both passes, from one ncu capture of
-# the 24-frame cut of this workload (profiles/tstream_c1_24frames_full.md:
-# 619.6 MB per 24 frames; traffic grows with the frame count).
+# DRAM bytes (read + write) per frame of both passes: dram__bytes_read.sum +
+# dram__bytes_write.sum of the rows and columns pass from one ncu capture of
+# a 24-frame cut of this workload, divided by 24 (traffic grows with the
+# frame count).
 DRAM_BYTES_PER_FRAME = 619.6e6 / 24
+TRAFFIC_SOURCE = ("ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, both passes) of a "
+                  "24-frame cut of this workload, scaled to the step's frames")
 
 
 def peaks():
@@ -115,19 +118,38 @@ def plane_requests(gb):
     }
 
 
-def _upscale_matrix(gb, src, dst):
+def _upscale_matrix(arrays, src, dst):
     """Forward bicubic (b=0, c=0.5) resampling dst -> src: the descale
-    matrix A of a plan, rebuilt from its A^T CSR."""
+    matrix A of a plan, rebuilt from its A^T CSR.  `arrays(src, dst)` returns
+    the plan's (transpose_weights, transpose_indices, transpose_offsets)."""
     import scipy.sparse as sp
-    p = gb.AxisPlan(gb.AxisRequest(src, dst, float(dst), 0.0, "bicubic", 3, 0.0, 0.5, 1.0,
-                                   "symmetric", 1), cached=False)
-    at = sp.csr_matrix((p.array("transpose_weights").astype(np.float64),
-                        p.array("transpose_indices"), p.array("transpose_offsets")),
-                       shape=(dst, src))
+    w, idx, off = arrays(src, dst)
+    at = sp.csr_matrix((np.asarray(w, np.float64), idx, off), shape=(dst, src))
     return at.T.tocsr()
 
 
-def make_frames(gb, frames, seed):
+def product_arrays(gb):
+    """Upscaler arrays from this executor's planner (the GPU arm)."""
+    def arrays(src, dst):
+        p = gb.AxisPlan(gb.AxisRequest(src, dst, float(dst), 0.0, "bicubic", 3, 0.0, 0.5, 1.0,
+                                       "symmetric", 1), cached=False)
+        return (p.array("transpose_weights"), p.array("transpose_indices"),
+                p.array("transpose_offsets"))
+    return arrays
+
+
+def checker_arrays(mod, O):
+    """Upscaler arrays from the reference engine's planner (or the oracle's,
+    which is bit-identical): the CPU arm synthesises its frames without
+    loading the executor library."""
+    def arrays(src, dst):
+        p = mod.Plan(O.make_request(src, dst, float(dst), 0.0, "bicubic", 3, 0.0, 0.5, 1.0,
+                                    "symmetric", 1))
+        return p.transpose_weights, p.transpose_indices, p.transpose_offsets
+    return arrays
+
+
+def make_frames(arrays, frames, seed):
     """Seeded synthetic YUV420P16 frames (see the module docstring)."""
     from scipy.ndimage import gaussian_filter
     rng = np.random.default_rng(seed)
@@ -140,7 +162,7 @@ def make_frames(gb, frames, seed):
                                                  (SRC_W >> 1, SRC_H >> 1, DST_W >> 1, DST_H >> 1)]):
             key = (sw, sh, dw, dh)
             if key not in mats:
-                mats[key] = (_upscale_matrix(gb, sw, dw), _upscale_matrix(gb, sh, dh))
+                mats[key] = (_upscale_matrix(arrays, sw, dw), _upscale_matrix(arrays, sh, dh))
             ah, av = mats[key]
             base = gaussian_filter(rng.random((dh, dw)), 1.5)
             up = av @ (ah @ base.T).T
@@ -215,15 +237,41 @@ def pixels_per_frame():
     return SRC_W * SRC_H + 2 * (SRC_W >> 1) * (SRC_H >> 1)
 
 
-def cpu_baseline(frames, threads, budget_s=12.0, kind="port"):
-    """The oracle port (or the reference engine built here) on the host
-    cores: whole frames through the scalar 2D route, one frame per thread."""
+def host_threads():
+    """Host threads this process may run on (os.sched_getaffinity), and how
+    that was found."""
+    try:
+        return len(os.sched_getaffinity(0)), "os.sched_getaffinity(0)"
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1, "os.cpu_count()"
+
+
+def checker_modules():
+    """The oracle and, where it was built on this machine, the reference
+    engine (oracle/_ref): (oracle, reference-or-None)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
-    mod = O
-    if kind == "reference":
+    try:
         import reference as R
-        mod = R
+        if not R.available():
+            R = None
+    except Exception:
+        R = None
+    return O, R
+
+
+def cpu_baseline(frames, threads, budget_s=12.0, route="automatic"):
+    """The reference's own CPU engine (oracle/_ref, built from its sources
+    on this machine) on the host cores, whole frames through its 2D integer
+    route, one frame per thread; the oracle port of its scalar route where
+    the engine is absent.  route: "automatic" (the engine's own pick: NEON
+    on aarch64, AVX-512/AVX2 on x86) or "scalar"."""
+    O, R = checker_modules()
+    mod = R if R is not None else O
+    kind = "reference" if R is not None else "port"
+    if R is None:
+        route = "scalar"
+    path = 1 if route == "automatic" else 0
     reqs = {
         "luma_h": (SRC_W, DST_W, float(DST_W), 0.0), "luma_v": (SRC_H, DST_H, float(DST_H), 0.0),
         "chroma_h": (SRC_W >> 1, DST_W >> 1, DST_W * (SRC_W >> 1) / SRC_W, 0.25 - 0.25 * DST_W / SRC_W),
@@ -239,7 +287,10 @@ def cpu_baseline(frames, threads, budget_s=12.0, kind="port"):
         for plane, (h, vv, conv) in zip((y, u, v), [("luma_h", "luma_v", luma),
                                                     ("chroma_h", "chroma_v", chroma),
                                                     ("chroma_h", "chroma_v", chroma)]):
-            out.append(mod.inverse_2d(plans[h], plans[vv], plane, conv))
+            if R is not None:
+                out.append(R.inverse_2d(plans[h], plans[vv], plane, conv, path=path))
+            else:
+                out.append(O.inverse_2d(plans[h], plans[vv], plane, conv))
         return out
 
     one(frames[0])  # warm-up
@@ -250,44 +301,45 @@ def cpu_baseline(frames, threads, budget_s=12.0, kind="port"):
             list(pool.map(one, batch))
             done += len(batch)
     elapsed = time.perf_counter() - t0
+    isa = os.uname().machine
+    what = (f"reference engine CpuPath::{route} ({'NEON' if isa == 'aarch64' else 'AVX-512/AVX2'} "
+            f"route on {isa})" if route == "automatic" else f"reference engine CpuPath::scalar on {isa}") \
+        if kind == "reference" else f"oracle port of the scalar route on {isa}"
     return {"value": done * pixels_per_frame() / elapsed / 1e6, "unit": "Mpix/s",
-            "cores": threads, "kind": kind,
+            "cores": threads, "kind": kind, "route": route,
             "sample": f"{done} frames (YUV420P16 1920x1080->1440x810, Delanczos taps=3), "
-                      f"{threads} threads x 1 frame, scalar 2D route, {elapsed:.1f} s"}
+                      f"{threads} threads x 1 frame, {what}, {elapsed:.1f} s"}
 
 
 def run_reference(args, rank, world):
-    """The reference arm: the reference's own CPU implementation of the path
-    on the host cores (built from its sources when that build is present on
-    this machine, else the oracle port), all host threads."""
+    """The reference arm: the reference's own CPU engine (built from its
+    sources on this machine into oracle/_ref) on every host thread, through
+    its optimized route (CpuPath::automatic), one frame per thread, with the
+    scalar route timed beside it; the oracle port of the scalar route where
+    the engine could not be built.  The frames are synthesised with the
+    reference planner's own upscaler: the executor library is not loaded."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    kind = "port"
-    try:
-        import reference as R
-        if R.available():
-            kind = "reference"
-    except Exception:
-        pass
-    sys.path.insert(0, os.path.join(REPO, "vapoursynth-descalemvc_gb300"))
-    import dsmvc_gb300 as gb
-    frames = make_frames(gb, 4, 1234)
-    threads = os.cpu_count() or 1
-    per_step = max(2.0, 30.0 / max(1, args.steps + args.warmup))
+    O, R = checker_modules()
+    frames = make_frames(checker_arrays(R if R is not None else O, O), 4, 1234)
+    threads, how = host_threads()
+    per_step = max(1.5, 30.0 / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
-        cpu_baseline(frames, threads, budget_s=0.1, kind=kind)
-    results = [cpu_baseline(frames, threads, budget_s=per_step, kind=kind)
-               for _ in range(args.steps)]
+        cpu_baseline(frames, threads, budget_s=0.1)
+    results = [cpu_baseline(frames, threads, budget_s=per_step) for _ in range(args.steps)]
     value = float(np.mean([r["value"] for r in results]))
+    scalar = cpu_baseline(frames, threads, budget_s=4.0, route="scalar") if R is not None else None
     ms = pixels_per_frame() * FRAMES / (value * 1e6) * 1e3
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": workload_config(),
-            "cpu_baseline": dict(results[-1], value=value),
+            "cpu_baseline": dict(results[-1], value=value, cores_source=how),
+            "scalar_route": scalar,
             "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    if R is None:
+        line["note"] = "reference engine not built on this machine: oracle port of the scalar route"
     print(json.dumps(line), flush=True)
 
 
@@ -837,7 +889,7 @@ def main():
     luma_conv = gb.integer_conversion(16, chroma=False, full_range=False)
     chroma_conv = gb.integer_conversion(16, chroma=True, full_range=False)
 
-    frames = make_frames(gb, 8, 20250 + rank)  # 8 distinct frames, reused cyclically
+    frames = make_frames(product_arrays(gb), 8, 20250 + rank)  # 8 distinct frames, reused cyclically
     stream = torch.cuda.Stream()
     dev_in, dev_out, tasks = [], [], []
     for f in range(FRAMES):
@@ -951,7 +1003,8 @@ def main():
         return
     cpu = None
     if not args.no_cpu_baseline and not args.kernels_only and world == 1:
-        cpu = cpu_baseline(frames, os.cpu_count() or 1, budget_s=args.cpu_seconds)
+        threads, how = host_threads()
+        cpu = dict(cpu_baseline(frames, threads, budget_s=args.cpu_seconds), cores_source=how)
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
@@ -968,6 +1021,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
                      "traffic": DRAM_BYTES_PER_FRAME * FRAMES,
+                     "traffic_source": TRAFFIC_SOURCE,
                      "algorithmic_bytes": total_bytes / max(1, args.steps),
                      "peak_source": peak_kind,
                      "kernel": "2D descale (horizontal + vertical passes per step)",

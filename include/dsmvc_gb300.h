@@ -319,17 +319,23 @@ void dsmvc_gb_batch_destroy(dsmvc_gb_batch *batch);
  * framework's memory pool, allocator-free real-time pipelines): the Float32
  * route of the 2D descale on device pointers, enqueued on `stream` (a
  * cudaStream_t; NULL = the legacy default stream), with no cudaMalloc,
- * cudaFree or other allocating call.  Its scratch -- job table, both plans'
- * coefficients, the Float32 intermediate plane (4 x vertical source size x
- * horizontal destination size bytes) and, for integer output, a forward
- * plane of the output's size -- lives in one file-scope device array of
- * DSMVC_GB_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
- * until the process exits.  Frames that need more, and plans that need
- * Float64, are rejected with DSMVC_GB_INVALID_ARGUMENT.  The first call on a
- * device looks the array up (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race, so order them on one stream.  `sample` is an
- * enum dsmvc_gb_sample; `conversion` is read for integer samples. */
+ * cudaFree or other allocating call.  Its scratch lives in one file-scope
+ * device array of DSMVC_GB_NOALLOC_SCRATCH_BYTES that every GPU loading this
+ * library holds until the process exits.  A frame needs, each part rounded
+ * up to 256 bytes: the job table; both plans' coefficients; the Float32
+ * intermediate plane, 4 x vertical source size x horizontal destination
+ * size bytes; and, for u8 or u16 output only, a forward plane of 4 x
+ * vertical destination size x horizontal destination size bytes.  Frames
+ * that need more, and plans that need Float64, are rejected with
+ * DSMVC_GB_INVALID_ARGUMENT.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and keeps the address for the life of the process:
+ * do not call this on a device after cudaDeviceReset.  Every call copies the
+ * job table and the plans' coefficients from pageable host memory, so it may
+ * block the host until those copies are done, and it returns
+ * DSMVC_GB_INVALID_ARGUMENT on a stream that is being captured.  All calls
+ * share the array: calls whose work overlaps on the GPU race, so order them
+ * on one stream.  `sample` is an enum dsmvc_gb_sample; `conversion` is read
+ * for integer samples. */
 #define DSMVC_GB_NOALLOC_SCRATCH_BYTES (32u << 20)
 int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal,
                                 const dsmvc_gb_plan *vertical, int32_t sample,

@@ -1,18 +1,53 @@
 """ctypes binding of the reference's own CPU engine built by oracle/ref
-(test infrastructure only; the library exists where the reference sources
-were present at build time, i.e. not on machines without them).
+(test infrastructure only: the checker and the timed CPU baseline).
+
+Where the reference tree is: $DSMVC_REFERENCE if set, else a staged copy of
+its engine sources under baseline/_ref/dsmvc (made by `stage()` on a machine
+that has the tree, kept out of version control, and carried along with the
+working copy so that a machine without the tree can build the engine for its
+own CPU), else /root/reference.  The library exists only where one of them
+was present at build time.
 """
 from __future__ import annotations
 
 import ctypes as C
 import os
+import shutil
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "_ref", "libdsmvc_ref.so")
-REFERENCE_ROOT = "/root/reference"
+STAGED_ROOT = os.path.join(REPO, "baseline", "_ref", "dsmvc")
+# The reference engine's CPU sources and headers (src/, include/dsmvc/); no
+# CUDA, Vulkan, Metal or VapourSynth file is needed for the CPU routes.
+ENGINE_FILES = (
+    ["include/dsmvc/engine.hpp", "include/dsmvc/host_blocks.hpp"]
+    + ["src/" + f for f in (
+        "axis_plan.cpp", "axis_plan_internal.hpp", "backend.cpp", "checked_size.hpp",
+        "cpu_executor.cpp", "cpu_executor_avx2.cpp", "cpu_executor_avx2_fixed.cpp",
+        "cpu_executor_avx512.cpp", "cpu_executor_neon.cpp", "cpu_float_workspace.hpp",
+        "cpu_horizontal_window.hpp", "cpu_packed.hpp", "cpu_rhs_span.hpp", "executor.cpp",
+        "host_blocks.cpp", "host_copy.cpp", "host_copy.hpp", "solve_partition.cpp",
+        "solve_partition.hpp")])
+
+
+def _tree_ok(root: str) -> bool:
+    return all(os.path.exists(os.path.join(root, f)) for f in ENGINE_FILES)
+
+
+def reference_root():
+    """The reference tree to build from, or None."""
+    env = os.environ.get("DSMVC_REFERENCE")
+    for root in ([env] if env else []) + [STAGED_ROOT, "/root/reference"]:
+        if root and _tree_ok(root):
+            return root
+    return None
+
+
+REFERENCE_ROOT = reference_root() or ""
 
 from oracle import Request, Conversion, ERRORS  # noqa: E402
 
@@ -29,12 +64,32 @@ def available() -> bool:
     return False
 
 
-def build() -> bool:
-    """Compile the reference engine when its sources are present."""
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
+def stage() -> bool:
+    """Copies the engine's CPU sources from the reference tree into the
+    ignored baseline/_ref/dsmvc, so that a machine without the tree (another
+    CPU architecture: the NEON route) can build the engine.  No-op when the
+    tree is absent or the staged copy is current."""
+    env = os.environ.get("DSMVC_REFERENCE")
+    src = next((r for r in ([env] if env else []) + ["/root/reference"] if r and _tree_ok(r)), None)
+    if src is None or os.path.realpath(src) == os.path.realpath(STAGED_ROOT):
         return False
-    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"),
-                    f"REF={REFERENCE_ROOT}"], check=True)
+    for f in ENGINE_FILES:
+        dst = os.path.join(STAGED_ROOT, f)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        a = os.path.join(src, f)
+        if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(a):
+            shutil.copy2(a, dst)
+    return True
+
+
+def build() -> bool:
+    """Compile the reference engine (scalar route plus this CPU's SIMD
+    route) when a reference tree is present."""
+    root = reference_root()
+    if root is None:
+        return False
+    subprocess.run(["make", "-s", f"-j{os.cpu_count() or 8}", "-C", os.path.join(HERE, "ref"),
+                    f"REF={root}"], check=True)
     return True
 
 

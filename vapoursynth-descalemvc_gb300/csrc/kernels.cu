@@ -1,8 +1,8 @@
 // Generic-stride axis kernels: one thread solves one vector (a row or a
 // column) through the gather, the forward and the backward substitution.
 // They serve every layout and every half-bandwidth, and are the
-// reference-order baseline the tiled kernels (tiled.cu) are checked
-// against.
+// reference-order baseline the streaming kernels (stream_impl.cuh,
+// tstream_impl.cuh) are checked against.
 //
 // Float32 arithmetic per element is that of the reference CUDA kernels
 // (src/cuda/dsmvc_cuda.cu:62-148, inverse_axis_ring): the A^T gather is one

@@ -8,13 +8,20 @@
 // plane (plus a forward scratch plane for integer output) -- lives in one
 // file-scope __device__ array of kNoAllocBytes.  Every GPU that loads this
 // library holds that array until the process exits.  The host reaches it
-// through cudaGetSymbolAddress, once per device on the device's first call
-// (which should therefore come before any stream capture); in host code the
-// array's name is only a stand-in, never a device address.  All calls share
-// the array, so calls whose work overlaps on the GPU (different streams, or
-// the same stream from several threads without ordering) race on it.  No
-// part of it needs to start at zero: every byte a call reads was written
-// earlier by the same call.
+// through cudaGetSymbolAddress, once per device on the device's first call;
+// in host code the array's name is only a stand-in, never a device address.
+// The looked-up address is kept for the life of the process, so the entry
+// point must not be used on a device after cudaDeviceReset.
+//
+// Each call copies the job table and both plans' coefficients into the
+// array from pageable host memory (the plans' own vectors and a job table on
+// the caller's stack) with cudaMemcpyAsync: the call may block the host
+// until those copies are done, and it refuses a stream that is being
+// captured, whose copies would point at host memory gone by the time the
+// work runs.  All calls share the array, so calls whose work overlaps on the
+// GPU (different streams, or the same stream from several threads without
+// ordering) race on it.  No part of it needs to start at zero: every byte a
+// call reads was written earlier by the same call.
 #include "noalloc.hpp"
 
 #include "kernels.cuh"
@@ -133,8 +140,13 @@ void inverse_2d_noalloc(const AxisPlan &h, const AxisPlan &v, dev::Sample sample
         throw std::invalid_argument("frame needs " + std::to_string(end) + " bytes of scratch; the "
                                     "allocation-free entry point holds " + std::to_string(kNoAllocBytes));
 
-    char *base = scratch_address();
     auto s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    check(cudaStreamIsCapturing(s, &capture), "querying the stream's capture status");
+    if (capture != cudaStreamCaptureStatusNone)
+        throw std::invalid_argument("the allocation-free entry point copies its plans from pageable "
+                                    "host memory and cannot run on a stream that is being captured");
+    char *base = scratch_address();
     copy_array(base, lh.offsets, h.transpose_offsets, s);
     copy_array(base, lh.indices, h.transpose_indices, s);
     copy_array(base, lh.weights, h.transpose_weights, s);

@@ -692,8 +692,11 @@ def inverse_2d_noalloc(h: AxisPlan, v: AxisPlan, sample: int, input_ptr: int, in
                        output_ptr: int, output_stride: int, conversion=None, stream: int = 0) -> None:
     """Allocation-free 2D descale on device pointers (see the C header):
     for callers that cannot allocate device memory.  Float32 route only;
-    frames whose scratch exceeds NOALLOC_SCRATCH_BYTES are rejected; calls
-    that overlap on the GPU race on the shared scratch array."""
+    frames whose scratch (plans, intermediate, and a forward plane for
+    integer output) exceeds NOALLOC_SCRATCH_BYTES are rejected; the plan
+    uploads come from pageable memory, so the call may block and is refused
+    on a capturing stream; calls that overlap on the GPU race on the shared
+    scratch array."""
     conv = _conv(conversion)
     _check(lib().dsmvc_gb_inverse_2d_noalloc(h.handle, v.handle, int(sample), C.c_void_p(input_ptr),
                                              int(input_stride), C.c_void_p(output_ptr),
