@@ -183,8 +183,9 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device):
+    def __init__(self, device, period_ms=25):
         self.device = device
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
 
@@ -192,7 +193,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "25"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -476,7 +477,7 @@ def run_sweep(args, rank, world):
                      "algorithmic_bytes": algo,
                      "kernel": "whole sweep graph (descale passes + scoring)"},
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 SERVE_SIZES = [(1280, 720), (1920, 1080), (2560, 1440), (3840, 2160)]
@@ -554,6 +555,7 @@ def run_serving(args, rank, world):
         return planes, sum(sw * sh for sw, sh, *_ in shapes)
 
     results = []
+    clocks = ClockSampler(local, period_ms=100)
     for rate in args.rates:
         # Requests are built (plans planned, output slots pinned) before the
         # clock starts; arrivals follow exponential gaps at `rate` per second.
@@ -565,6 +567,7 @@ def run_serving(args, rank, world):
             server.wait(server.submit(planes))
         server.reset_stats()
         pending = {}
+        clocks.__enter__()
         t0 = time.perf_counter()
         due = t0
         for i, ((planes, pix), gap) in enumerate(zip(reqs, gaps)):
@@ -581,6 +584,7 @@ def run_serving(args, rank, world):
         for t in pending.values():
             server.wait(t)
         elapsed = time.perf_counter() - t0
+        clocks.__exit__(None, None, None)
         st = server.stats()
         results.append({"offered_rate": rate, "requests": count, "seconds": elapsed,
                         "achieved_rate": st["completed"] / elapsed,
@@ -605,13 +609,14 @@ def run_serving(args, rank, world):
                    "memory_budget_mb": args.serve_budget, "streams": args.serve_streams,
                    "l2": "inputs larger than L2 per batch; no flush", "parallelism": "replicas"},
         "latency_p50_ms": head["latency_p50_ms"], "latency_p99_ms": head["latency_p99_ms"],
+        "clocks": clocks.summary(),
         "rates": results,
         "plan_cache": {k: cache[k] for k in ("plan_cache_hits", "plan_cache_misses",
                                              "plan_cache_evictions", "plan_cache_bytes")},
         "e2e": {"value": head["mpix_per_s"], "unit": "Mpix/s",
                 "note": "every request is a host frame: copies are inside the latency"},
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def _f64_solution(plan_h, plan_v, x):
@@ -668,13 +673,15 @@ def run_single_frame(args, rank, world):
     batch = ex.prepare_batch([gb.PlaneTask(h, v, dx.data_ptr(), sw, dy.data_ptr(), dw, 0, 0, None)])
     for _ in range(args.warmup):
         batch.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        start.record(stream)
-        for _ in range(args.steps):
-            batch.launch(stream.cuda_stream)
-        stop.record(stream)
-    stream.synchronize()
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                batch.launch(stream.cuda_stream)
+            stop.record(stream)
+        stream.synchronize()
     dev_ms = start.elapsed_time(stop) / args.steps
     gpu = dy.cpu().numpy()
     oh = O.Plan(O.make_request(sw, dw, float(dw), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 1))
@@ -696,6 +703,7 @@ def run_single_frame(args, rank, world):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "C0: Debicubic(b=0,c=0.5) GRAYS f32 1920x1080->1280x720, padding=3, "
                                "f64mode=1, single frame", "l2": "single 8.3 MB frame (L2-resident)"},
+        "clocks": clocks.summary(),
         "e2e": {"value": pix / (host_ms / 1e3) / 1e6, "unit": "Mpix/s", "ms_per_frame": host_ms,
                 "h2d_bytes_per_step": frame.nbytes, "d2h_bytes_per_step": out.nbytes},
         "cpu_baseline": {"value": pix / (cpu_ms / 1e3) / 1e6, "unit": "Mpix/s", "cores": 1, "kind": "port",
@@ -707,7 +715,7 @@ def run_single_frame(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": algo / (dev_ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": algo / (dev_ms / 1e3) / 1e9 / hbm, "traffic": None, "peak_source": peak_kind},
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 F64_CASES = {
@@ -719,34 +727,44 @@ F64_CASES = {
 def run_float64(args, rank, world):
     """C2: Despline64 and Debicubic(b=1/3, c=1/3) with blur=1.1, GRAYS
     float32 3840x2160 -> 2560x1440, 32 frames per step, f64mode=2 (forced
-    Float64) and f64mode=0 (auto), from HBM.  Float64 FLOP/s against the
-    measured FP64 peak; error against the CPU scalar route (float32 ULPs,
-    Float64 route) and a Float64 solve."""
+    Float64) and f64mode=0 (auto: Float32 for these well-conditioned plans),
+    from HBM.  Float64 cases: FLOP/s against the measured FP64 peak; Float32
+    cases: compulsory bytes against the HBM peak.  Error against the CPU
+    scalar route (float32 ULPs) and a Float64 solve."""
     import torch
     import dsmvc_gb300 as gb
     from dsmvc_gb300 import synthetic
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from common import max_ulp
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     sw, sh, dw, dh = 3840, 2160, 2560, 1440
     nframes = args.frames or 32
     base = synthetic.gray_frame(sw, sh, dw, dh, seed=args.seed)
     rng = np.random.default_rng(args.seed)
-    # One distinct frame per task, so that a step's inputs exceed L2.
-    frames = [torch.from_numpy(base + rng.normal(0, 1e-3, base.shape).astype(np.float32)).cuda()
-              for _ in range(nframes)]
+    # Eight distinct frames (266 MB, twice the L2) cycled over the step's
+    # tasks: a step reads 1.06 GB of inputs.
+    distinct = [torch.from_numpy(base + rng.normal(0, 1e-3, base.shape).astype(np.float32)).cuda()
+                for _ in range(min(8, nframes))]
+    frames = [distinct[i % len(distinct)] for i in range(nframes)]
     outs = [torch.empty((dh, dw), dtype=torch.float32, device="cuda") for _ in range(nframes)]
     fp64_peak = gb.measure_fp64_peak(local)
     hbm, peak_kind = peaks()
     ex = gb.Executor(local)
     stream = torch.cuda.Stream()
     sid = stream.cuda_stream
+    x0 = frames[0].cpu().numpy()
     results = {}
     for name, (k, taps, b, c) in F64_CASES.items():
+        req = lambda s_, d_, m_: gb.AxisRequest(s_, d_, float(d_), 0.0, k, taps, b, c, 1.1, "symmetric", m_)
+        oreq = lambda s_, d_, m_: O.make_request(s_, d_, float(d_), 0.0, k, taps, b, c, 1.1, "symmetric", m_)
+        # Float64 solve of the frame with the Float64-retaining plans.
+        ref = _f64_solution(gb.AxisPlan(req(sw, dw, 2), cached=False), gb.AxisPlan(req(sh, dh, 2), cached=False),
+                            x0)
         for mode in (2, 0):
-            req = lambda s, d: gb.AxisRequest(s, d, float(d), 0.0, k, taps, b, c, 1.1, "symmetric", mode)
-            h, v = gb.AxisPlan(req(sw, dw), cached=False), gb.AxisPlan(req(sh, dh), cached=False)
+            h, v = gb.AxisPlan(req(sw, dw, mode), cached=False), gb.AxisPlan(req(sh, dh, mode), cached=False)
             ex.prepare(h)
             ex.prepare(v)
             tasks = [gb.PlaneTask(h, v, frames[i].data_ptr(), sw, outs[i].data_ptr(), dw, 0, 0, None)
@@ -756,12 +774,13 @@ def run_float64(args, rank, world):
                 batch.launch(sid)
             torch.cuda.synchronize()
             start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                start.record(stream)
-                for _ in range(args.steps):
-                    batch.launch(sid)
-                stop.record(stream)
-            stream.synchronize()
+            with ClockSampler(local) as clocks:
+                with torch.cuda.stream(stream):
+                    start.record(stream)
+                    for _ in range(args.steps):
+                        batch.launch(sid)
+                    stop.record(stream)
+                stream.synchronize()
             batch.check(sid)
             ms = start.elapsed_time(stop) / args.steps
             f64 = h.requires_float64 or v.requires_float64
@@ -772,18 +791,7 @@ def run_float64(args, rank, world):
                 flops += vectors * (2 * int(p.nonzeros) + p.destination_size * (4 * p.half_bandwidth + 2))
             flops *= nframes
             gpu = outs[0].cpu().numpy()
-            x0 = frames[0].cpu().numpy()
-            oh = O.Plan(O.make_request(sw, dw, float(dw), 0.0, k, taps, b, c, 1.1, "symmetric", mode))
-            ov = O.Plan(O.make_request(sh, dh, float(dh), 0.0, k, taps, b, c, 1.1, "symmetric", mode))
-            cpu = O.inverse_2d(oh, ov, x0)
-            ref = _f64_solution(gb.AxisPlan(req(sw, dw), cached=False) if mode == 2 else
-                                gb.AxisPlan(gb.AxisRequest(sw, dw, float(dw), 0.0, k, taps, b, c, 1.1,
-                                                           "symmetric", 2), cached=False),
-                                gb.AxisPlan(req(sh, dh), cached=False) if mode == 2 else
-                                gb.AxisPlan(gb.AxisRequest(sh, dh, float(dh), 0.0, k, taps, b, c, 1.1,
-                                                           "symmetric", 2), cached=False), x0)
-            sys.path.insert(0, os.path.join(REPO, "tests"))
-            from common import max_ulp
+            cpu = O.inverse_2d(O.Plan(oreq(sw, dw, mode)), O.Plan(oreq(sh, dh, mode)), x0)
             algo = nframes * (sw * sh + dw * dh) * 4
             results[f"{name}/f64mode={mode}"] = {
                 "route": "float64" if f64 else "float32", "ms_per_step": ms,
@@ -794,11 +802,17 @@ def run_float64(args, rank, world):
                 "rcond": [h.normal_rcond, v.normal_rcond], "half_bandwidth": [h.half_bandwidth, v.half_bandwidth],
                 "max_ulp_vs_cpu_scalar": max_ulp(gpu, cpu),
                 "max_abs_vs_cpu_scalar": float(np.abs(gpu - cpu).max()),
+                "mean_abs_vs_cpu_scalar": float(np.abs(gpu - cpu).mean()),
                 "max_abs_vs_f64": float(np.abs(gpu - ref).max()),
+                "cpu_scalar_max_abs_vs_f64": float(np.abs(cpu - ref).max()),
+                "clocks": clocks.summary(),
+                "gpu_launches": batch.info()["kernel_launches"] * args.steps,
             }
+            del batch
     if rank != 0:
-        return
+        return None
     head = results["spline64-blur1.1/f64mode=2"]
+    f32 = results["bicubic(1/3,1/3)-blur1.1/f64mode=0"]
     line = {
         "metric": "descale Mpix/s, Float64 route (Despline64 blur 1.1, GRAYS 3840x2160->2560x1440)",
         "value": head["mpix_per_s"], "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
@@ -806,14 +820,78 @@ def run_float64(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"C2: GRAYS f32 3840x2160->2560x1440, {nframes} frames, blur 1.1, "
                                "f64mode 2 and 0", "frames_per_step": nframes,
-                   "l2": f"inputs ({nframes * sw * sh * 4 / 1e9:.2f} GB, one distinct frame per "
-                         "task) larger than L2; no flush"},
+                   "l2": f"inputs ({nframes * sw * sh * 4 / 1e9:.2f} GB per step from 8 distinct "
+                         "frames of 266 MB) larger than L2; no flush"},
+        "clocks": head["clocks"],
         "fp64_peak_tflops": fp64_peak, "cases": results,
         "roofline": {"bound": "fp64", "achieved": head["gflops"] / 1e3, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": head["fp64_frac"], "traffic": None,
                      "peak_source": "measured (dsmvc_gb_measure_fp64_peak)"},
+        "roofline_f32_debicubic": {"bound": "hbm", "achieved": f32["hbm_frac"] * hbm, "peak": hbm,
+                                   "unit": "GB/s", "frac": f32["hbm_frac"], "peak_source": peak_kind,
+                                   "case": "bicubic(1/3,1/3)-blur1.1/f64mode=0 (Float32 route)"},
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+SUB_WORKLOADS = {"c0": run_single_frame, "c2": run_float64, "c3": run_sweep, "c4": run_serving}
+
+
+def run_configs(args, rank, world):
+    """The other configurations, each measured as its own line (own timed
+    region, clocks and error figures) and nested in the headline line:
+    c0 single frame, c2 4K Float64/Float32, c3 candidate sweep, c4 request
+    loop.  Shorter runs than the standalone --workload lines."""
+    import torch
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = max(3, min(args.steps, 20))
+    sub.warmup = 3
+    sub.frames = None
+    sub.rates = [200.0, 800.0]
+    sub.serve_seconds = 2.0
+    out = {}
+    for key, fn in SUB_WORKLOADS.items():
+        t0 = time.perf_counter()
+        try:
+            out[key] = fn(sub, rank, world) or {}
+        except Exception as e:  # noqa: BLE001 - recorded in the line, the headline stands
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+        out[key]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
+
+
+def c1_error(frame, outputs, plans, convs):
+    """Error of the step's first frame, luma and one chroma plane (computed
+    outside the timed region): codes against the CPU scalar route (the
+    reference engine built on this machine, else the oracle port) and
+    against an unrounded Float64 solve of the same plane in code units."""
+    import dsmvc_gb300 as gb
+    O, R = checker_modules()
+    res = {}
+    for name, idx, (hk, vk), conv in (("luma", 0, ("luma_h", "luma_v"), convs[0]),
+                                      ("chroma_u", 1, ("chroma_h", "chroma_v"), convs[1])):
+        x = frame[idx]
+        got = outputs[idx].astype(np.int64)
+        hq, vq = plans[hk].request, plans[vk].request
+        oreq = lambda q: O.make_request(q.source_size, q.destination_size, q.active_length, q.shift,
+                                        q.kernel, q.taps, q.b, q.c, q.blur, q.border, q.f64_mode)
+        if R is not None:
+            cpu = R.inverse_2d(R.Plan(oreq(hq)), R.Plan(oreq(vq)), x, conv, path=0)
+        else:
+            cpu = O.inverse_2d(O.Plan(oreq(hq)), O.Plan(oreq(vq)), x, conv)
+        f64p = lambda q: gb.AxisPlan(gb.AxisRequest(q.source_size, q.destination_size, q.active_length,
+                                                    q.shift, q.kernel, q.taps, q.b, q.c, q.blur,
+                                                    q.border, 2), cached=False)
+        xf = (x.astype(np.float64) - conv[0]) * conv[1]
+        ref = _f64_solution(f64p(hq), f64p(vq), xf) * conv[2] + conv[3]
+        res[name] = {"max_codes_vs_cpu_scalar": int(np.max(np.abs(got - cpu.astype(np.int64)))),
+                     "mismatched_samples_vs_cpu_scalar": int(np.count_nonzero(got != cpu)),
+                     "max_abs_codes_vs_f64": float(np.max(np.abs(got - ref))),
+                     "cpu_scalar_max_abs_codes_vs_f64": float(np.max(np.abs(cpu.astype(np.int64) - ref)))}
+    res["checker"] = "reference engine (scalar route)" if R is not None else "oracle port (scalar route)"
+    return res
 
 
 def workload_config():
@@ -849,7 +927,9 @@ def main():
     ap.add_argument("--sweep-step", type=int, default=1,
                     help="c3: height step (1 = the full sweep; larger steps give small profiling cases)")
     ap.add_argument("--kernels-only", action="store_true",
-                    help="skip the end-to-end and CPU legs (profiling runs)")
+                    help="skip the end-to-end and CPU legs and the other configurations (profiling runs)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline line only (no c0/c2/c3/c4 blocks)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     FRAMES = args.frames or FRAMES
@@ -864,8 +944,9 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     if args.workload != "c1" and args.impl != "reference":
-        {"c0": run_single_frame, "c2": run_float64, "c3": run_sweep,
-         "c4": run_serving}[args.workload](args, rank, world)
+        line = SUB_WORKLOADS[args.workload](args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
         if dist is not None:
             dist.barrier()
             dist.destroy_process_group()
@@ -1005,6 +1086,10 @@ def main():
     if not args.no_cpu_baseline and not args.kernels_only and world == 1:
         threads, how = host_threads()
         cpu = dict(cpu_baseline(frames, threads, budget_s=args.cpu_seconds), cores_source=how)
+    err = None
+    if not args.kernels_only and world == 1:
+        err = c1_error(frames[0], [dev_out[i].cpu().numpy().view(np.uint16) for i in range(2)],
+                       plans, (luma_conv, chroma_conv))
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
@@ -1028,7 +1113,10 @@ def main():
                      "kernels": [dict(k, share=k["milliseconds"] / total_ms) for k in ktimes],
                      "dominant": dominant["name"] if dominant else None},
         "cpu_baseline": cpu,
+        "error": err,
     }
+    if not args.kernels_only and not args.no_configs and world == 1:
+        line["configs"] = run_configs(args, rank, world)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
