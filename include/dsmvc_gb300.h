@@ -170,6 +170,40 @@ int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out);
  * 7 normal_bands_f64, 8 ldlt_bands_f64, 9 inverse_diagonal_f64 (f64). */
 int dsmvc_gb_plan_get_array(const dsmvc_gb_plan *plan, int32_t which,
                             const void **data, uint64_t *count);
+/* The arrays and scalars of a plan built elsewhere -- a reference
+ * dsmvc::AxisPlan (include/dsmvc/engine.hpp:82-107) -- described by
+ * pointers and element counts (each vector's data() and size()).  A pointer
+ * may be NULL only when its count is 0; the four Float64 arrays are all
+ * present (a plan that needs Float64) or all empty. */
+typedef struct dsmvc_gb_plan_arrays {
+    int32_t source_size;
+    int32_t destination_size;
+    int32_t support;
+    int32_t half_bandwidth;
+    double active_length;
+    double shift;
+    double normal_rcond;
+    double normal_inf_norm;
+    const uint32_t *transpose_offsets;     uint64_t transpose_offsets_count;
+    const int32_t *transpose_indices;      uint64_t transpose_indices_count;
+    const float *transpose_weights;        uint64_t transpose_weights_count;
+    const float *lower_ld;                 uint64_t lower_ld_count;
+    const float *upper_l;                  uint64_t upper_l_count;
+    const float *inverse_diagonal;         uint64_t inverse_diagonal_count;
+    const double *transpose_weights_f64;   uint64_t transpose_weights_f64_count;
+    const double *normal_bands_f64;        uint64_t normal_bands_f64_count;
+    const double *ldlt_bands_f64;          uint64_t ldlt_bands_f64_count;
+    const double *inverse_diagonal_f64;    uint64_t inverse_diagonal_f64_count;
+} dsmvc_gb_plan_arrays;
+/* Imports a plan built by the reference planner, for the reference's
+ * CudaExecutor::prepare(std::shared_ptr<const AxisPlan>) and the executor
+ * calls that take `const AxisPlan &` (src/cuda/cuda_executor.hpp:26-52,
+ * include/dsmvc/engine.hpp:389): the arrays are copied, checked like
+ * AxisPlan::check_valid (src/axis_plan.cpp:1259-1341) and returned as a
+ * plan handle the executor treats like one it built.  An invalid plan is
+ * DSMVC_GB_INVALID_ARGUMENT.  An imported plan carries no request:
+ * dsmvc_gb_plan_hashes then needs one. */
+int dsmvc_gb_plan_import(const dsmvc_gb_plan_arrays *arrays, dsmvc_gb_plan **out);
 /* FNV-1a plan hashes of tests/numerical_conformance.hpp:193-248. */
 int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan,
                          const dsmvc_gb_axis_request *request,

@@ -26,6 +26,8 @@
 struct dsmvc_gb_plan {
     std::shared_ptr<const dsmvc_gb::AxisPlan> plan;
     dsmvc_gb::AxisRequest request;
+    // Imported plans (dsmvc_gb_plan_import) carry no request.
+    bool has_request = true;
 };
 
 struct dsmvc_gb_executor {
@@ -226,10 +228,62 @@ int dsmvc_gb_plan_get_array(const dsmvc_gb_plan *plan, int32_t which, const void
     });
 }
 
+int dsmvc_gb_plan_import(const dsmvc_gb_plan_arrays *a, dsmvc_gb_plan **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output handle is null");
+        *out = nullptr;
+        if (!a) throw std::invalid_argument("plan arrays are null");
+        auto copy = [](const auto *data, std::uint64_t count, auto &dst, const char *name) {
+            if (count > 0 && !data) throw std::invalid_argument(std::string("plan array ") + name + " is null");
+            if (count > (std::uint64_t{1} << 40)) throw std::length_error(std::string("plan array ") + name + " is too large");
+            dst.assign(data, data + count);
+        };
+        dsmvc_gb::AxisPlan p;
+        p.source_size = a->source_size;
+        p.destination_size = a->destination_size;
+        p.support = a->support;
+        p.half_bandwidth = a->half_bandwidth;
+        p.active_length = a->active_length;
+        p.shift = a->shift;
+        p.normal_rcond = a->normal_rcond;
+        p.normal_inf_norm = a->normal_inf_norm;
+        copy(a->transpose_offsets, a->transpose_offsets_count, p.transpose_offsets, "transpose_offsets");
+        copy(a->transpose_indices, a->transpose_indices_count, p.transpose_indices, "transpose_indices");
+        copy(a->transpose_weights, a->transpose_weights_count, p.transpose_weights, "transpose_weights");
+        copy(a->lower_ld, a->lower_ld_count, p.lower_ld, "lower_ld");
+        copy(a->upper_l, a->upper_l_count, p.upper_l, "upper_l");
+        copy(a->inverse_diagonal, a->inverse_diagonal_count, p.inverse_diagonal, "inverse_diagonal");
+        copy(a->transpose_weights_f64, a->transpose_weights_f64_count, p.transpose_weights_f64,
+             "transpose_weights_f64");
+        copy(a->normal_bands_f64, a->normal_bands_f64_count, p.normal_bands_f64, "normal_bands_f64");
+        copy(a->ldlt_bands_f64, a->ldlt_bands_f64_count, p.ldlt_bands_f64, "ldlt_bands_f64");
+        copy(a->inverse_diagonal_f64, a->inverse_diagonal_f64_count, p.inverse_diagonal_f64,
+             "inverse_diagonal_f64");
+        if (p.transpose_offsets.empty() || !p.valid())
+            throw std::invalid_argument("imported axis plan is invalid");
+        std::int32_t widest = 0;
+        for (std::size_t j = 0; j + 1 < p.transpose_offsets.size(); ++j)
+            widest = std::max<std::int32_t>(widest, static_cast<std::int32_t>(p.transpose_offsets[j + 1]
+                                                                              - p.transpose_offsets[j]));
+        p.max_row_entries = widest;
+        p.validated = true;
+        dsmvc_gb::AxisRequest q;
+        q.source_size = p.source_size;
+        q.destination_size = p.destination_size;
+        q.active_length = p.active_length;
+        q.shift = p.shift;
+        q.kernel.kind = dsmvc_gb::KernelKind::custom;
+        q.f64_mode = p.requires_float64() ? dsmvc_gb::F64Mode::float64_only : dsmvc_gb::F64Mode::automatic;
+        *out = new dsmvc_gb_plan{std::make_shared<const dsmvc_gb::AxisPlan>(std::move(p)), q, false};
+    });
+}
+
 int dsmvc_gb_plan_hashes(const dsmvc_gb_plan *plan, const dsmvc_gb_axis_request *request,
                          uint64_t *f32_hash, uint64_t *complete_hash) {
     return guarded([&] {
         const auto &p = plan_of(plan);
+        if (!request && !plan->has_request)
+            throw std::invalid_argument("an imported plan carries no request: pass one for its hashes");
         const auto q = request ? to_request(request) : plan->request;
         if (f32_hash) *f32_hash = dsmvc_gb::f32_plan_hash(q, p);
         if (complete_hash) *complete_hash = dsmvc_gb::complete_plan_hash(q, p);

@@ -52,6 +52,18 @@ class ConversionC(C.Structure):
                 ("output_maximum", C.c_uint32)]
 
 
+class PlanArraysC(C.Structure):
+    """dsmvc_gb_plan_arrays: a plan built elsewhere, by pointers and counts."""
+    _fields_ = [("source_size", C.c_int32), ("destination_size", C.c_int32),
+                ("support", C.c_int32), ("half_bandwidth", C.c_int32),
+                ("active_length", C.c_double), ("shift", C.c_double),
+                ("normal_rcond", C.c_double), ("normal_inf_norm", C.c_double)] + [
+        (f, t) for name in ("transpose_offsets", "transpose_indices", "transpose_weights", "lower_ld",
+                            "upper_l", "inverse_diagonal", "transpose_weights_f64", "normal_bands_f64",
+                            "ldlt_bands_f64", "inverse_diagonal_f64")
+        for f, t in ((name, C.c_void_p), (name + "_count", C.c_uint64))]
+
+
 class PlanInfoC(C.Structure):
     _fields_ = [("source_size", C.c_int32), ("destination_size", C.c_int32),
                 ("support", C.c_int32), ("half_bandwidth", C.c_int32),
@@ -182,6 +194,7 @@ SIGNATURES = {
     "dsmvc_gb_inverse_2d_noalloc": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
                                      C.c_void_p, C.c_int64, C.POINTER(ConversionC), C.c_void_p],
                                     C.c_int),
+    "dsmvc_gb_plan_import": ([C.POINTER(PlanArraysC), C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_plan_build_many": ([C.POINTER(AxisRequestC), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_sweep_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int32,
@@ -348,6 +361,29 @@ class AxisPlan:
         if h is not None and h.value and _lib is not None:
             _lib.dsmvc_gb_plan_release(h)
             self._h = None
+
+
+def import_plan(source) -> AxisPlan:
+    """A plan built elsewhere (any object with the reference AxisPlan's
+    scalars and arrays as attributes, e.g. the reference engine's own plan)
+    imported through dsmvc_gb_plan_import: copied and validated.  An
+    imported plan carries no request: the returned plan's `request` holds
+    only its sizes and shift (kernel "custom")."""
+    keep = []
+    a = PlanArraysC()
+    for name in ("source_size", "destination_size", "support", "half_bandwidth"):
+        setattr(a, name, int(getattr(source, name)))
+    for name in ("active_length", "shift", "normal_rcond", "normal_inf_norm"):
+        setattr(a, name, float(getattr(source, name, 0.0)))
+    for name, dt in AxisPlan._ARRAYS:
+        arr = np.ascontiguousarray(getattr(source, name, np.zeros(0, dt)), dt)
+        keep.append(arr)
+        setattr(a, name, arr.ctypes.data if arr.size else None)
+        setattr(a, name + "_count", int(arr.size))
+    h = C.c_void_p()
+    _check(lib().dsmvc_gb_plan_import(C.byref(a), C.byref(h)))
+    req = AxisRequest(a.source_size, a.destination_size, a.active_length, a.shift, "custom")
+    return AxisPlan(req, _handle=h.value)
 
 
 def measure_fp64_peak(device: int = 0) -> float:
