@@ -177,13 +177,14 @@ def make_frames(arrays, frames, seed):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region
+    (every 10 ms by default)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device, period_ms=25):
+    def __init__(self, device, period_ms=10):
         self.device = device
         self.period_ms = period_ms
         self.proc = None
@@ -675,14 +676,17 @@ def run_single_frame(args, rank, world):
         batch.launch(stream.cuda_stream)
     torch.cuda.synchronize()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # A single frame takes tens of microseconds: enough steps for a timed
+    # region of about 0.3 s, so that the clocks are sampled inside it.
+    steps = max(args.steps, 8000)
     with ClockSampler(local) as clocks:
         with torch.cuda.stream(stream):
             start.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 batch.launch(stream.cuda_stream)
             stop.record(stream)
         stream.synchronize()
-    dev_ms = start.elapsed_time(stop) / args.steps
+    dev_ms = start.elapsed_time(stop) / steps
     gpu = dy.cpu().numpy()
     oh = O.Plan(O.make_request(sw, dw, float(dw), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 1))
     ov = O.Plan(O.make_request(sh, dh, float(dh), 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 1))
@@ -700,7 +704,7 @@ def run_single_frame(args, rank, world):
         "metric": "descale Mpix/s, single frame (Debicubic GRAYS 1920x1080->1280x720)",
         "value": pix / (dev_ms / 1e3) / 1e6, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "device_steps": steps,
         "config": {"workload": "C0: Debicubic(b=0,c=0.5) GRAYS f32 1920x1080->1280x720, padding=3, "
                                "f64mode=1, single frame", "l2": "single 8.3 MB frame (L2-resident)"},
         "clocks": clocks.summary(),
@@ -808,6 +812,33 @@ def run_float64(args, rank, world):
                 "clocks": clocks.summary(),
                 "gpu_launches": batch.info()["kernel_launches"] * args.steps,
             }
+            if f64:
+                # The kernels in the CPU scalar route's operation order
+                # (unfused, true division), for comparison.
+                os.environ["DSMVC_GB_F64_EXACT"] = "1"
+                try:
+                    exact_ex = gb.Executor(local)
+                finally:
+                    del os.environ["DSMVC_GB_F64_EXACT"]
+                exact_ex.prepare(h)
+                exact_ex.prepare(v)
+                eb = exact_ex.prepare_batch(tasks)
+                for _ in range(2):
+                    eb.launch(sid)
+                torch.cuda.synchronize()
+                start.record(stream)
+                for _ in range(max(3, args.steps // 4)):
+                    eb.launch(sid)
+                stop.record(stream)
+                stream.synchronize()
+                ems = start.elapsed_time(stop) / max(3, args.steps // 4)
+                eb.check(sid)
+                egpu = outs[0].cpu().numpy()
+                results[f"{name}/f64mode={mode}"]["cpu_order"] = {
+                    "ms_per_step": ems, "fp64_frac": flops / (ems / 1e3) / 1e12 / fp64_peak,
+                    "max_ulp_vs_cpu_scalar": max_ulp(egpu, cpu), "speedup_of_fused": ems / ms}
+                del eb
+                exact_ex.close()
             del batch
     if rank != 0:
         return None

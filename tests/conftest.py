@@ -75,6 +75,16 @@ def exact_executor(gb):
 
 
 @pytest.fixture(scope="session")
+def f64_exact_executor(gb):
+    """An executor whose Float64 two-pass kernels run the CPU scalar route's
+    operation order (DSMVC_GB_F64_EXACT=1): bit for bit its results; the
+    default fused kernels stay within 1 float32 ULP / 1 code of them."""
+    ex = _executor_with(gb, "DSMVC_GB_F64_EXACT", "1")
+    yield ex
+    ex.close()
+
+
+@pytest.fixture(scope="session")
 def paired_executor(gb):
     """An executor whose admitted 2D planes use the paired transposing
     kernels (DSMVC_GB_PAIRED=1)."""

@@ -6,8 +6,8 @@ solve.
     Despline64 and Debicubic(b=1/3, c=1/3), f64mode 2 (forced Float64) and
     0 (auto: these plans are well conditioned, so the Float32 route), one
     frame alone and two frames in one prepared batch.  Float64 route:
-    <= 1 float32 ULP against the CPU scalar Float64 route (the kernels meet
-    it bit for bit on whole vectors).  Float32 route: max-abs <= 2e-5 and
+    <= 1 float32 ULP against the CPU scalar Float64 route with the default
+    fused kernels, bit for bit with the kernels in the CPU's operation order.  Float32 route: max-abs <= 2e-5 and
     mean-abs <= 1e-6 against the CPU scalar route (tests/vs_gpu_concurrency.py:57).
     Both: within the CPU scalar route's own distance from the Float64 solve
     plus the Float32 tolerance.
@@ -61,7 +61,7 @@ def frame_4k(gb):
 
 @pytest.mark.parametrize("mode", [2, 0])
 @pytest.mark.parametrize("name", list(C2_KERNELS))
-def test_4k_blur_against_cpu_scalar_and_f64(gb, executor, frame_4k, name, mode):
+def test_4k_blur_against_cpu_scalar_and_f64(gb, executor, f64_exact_executor, frame_4k, name, mode):
     torch = pytest.importorskip("torch")
     k, taps, b, c = C2_KERNELS[name]
     t = lambda s, d, m: (s, d, float(d), 0.0, k, taps, b, c, 1.1, "symmetric", m)
@@ -86,6 +86,10 @@ def test_4k_blur_against_cpu_scalar_and_f64(gb, executor, frame_4k, name, mode):
     batch.check(stream.cuda_stream)
     batched = [y.cpu().numpy() for y in dy]
 
+    if f64_route:
+        # The Float64 kernels in the CPU's operation order: bit for bit.
+        exact = f64_exact_executor.inverse_2d(h, v, frame_4k[0])
+        assert max_ulp(exact, O.inverse_2d(oh, ov, frame_4k[0])) == 0
     for i, got in enumerate([alone, batched[0], batched[1]]):
         x = frame_4k[0 if i < 2 else 1]
         want = O.inverse_2d(oh, ov, x) if i != 1 else want

@@ -385,6 +385,11 @@ struct Executor::Impl {
     // transposing kernels; otherwise they serve the plans the chunk-delayed
     // kernels do not admit (slowly decaying factors, half-bandwidths 9, 11).
     bool prefer_exact = false;
+    // The Float64 two-pass kernels fuse multiply-adds and multiply by the
+    // reciprocal pivot (within the <= 1 float32 ULP contract, about half the
+    // FP64 operations); DSMVC_GB_F64_EXACT=1 (or DSMVC_GB_EXACT=1) runs the
+    // CPU scalar route's operation order, equal to it bit for bit.
+    bool f64_fused = true;
     // Default CTA size of the transposing kernels (DSMVC_GB_TSTREAM_THREADS,
     // 32..256 in multiples of 32); batches may tune it per launch group.
     int tstream_threads = kTStreamThreads;
@@ -1069,7 +1074,7 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         int rc = 0;
         if (l.kind == 6) {
             rc = launch_tsolve64(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
-                                 l.hb, l.in, l.out, l.record_floats, status, stream);
+                                 l.hb, l.in, l.out, l.record_floats, f64_fused, status, stream);
         } else if (l.kind == 5) {
             rc = launch_tsolve(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
                                l.hb, l.variant ? 8 : 0, l.in, l.out, l.record_floats, stream);
@@ -1155,6 +1160,9 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         impl_->allow_paired = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_EXACT"))
         impl_->prefer_exact = std::string(env) == "1";
+    if (impl_->prefer_exact) impl_->f64_fused = false;
+    if (const char *env = std::getenv("DSMVC_GB_F64_EXACT"))
+        impl_->f64_fused = std::string(env) != "1" && !impl_->prefer_exact;
     if (const char *env = std::getenv("DSMVC_GB_HOST_DIRECT")) impl_->host_direct = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
         char *end = nullptr;

@@ -73,22 +73,23 @@ int launch_tsolve_hb7(const dev::StreamJob *, int, int, int, int, dev::Sample, d
 int launch_tsolve_hb9(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
 int launch_tsolve_hb11(const dev::StreamJob *, int, int, int, int, dev::Sample, dev::Sample, int, void *);
 
-int launch_tsolve64_hb1(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
-int launch_tsolve64_hb3(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
-int launch_tsolve64_hb5(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
-int launch_tsolve64_hb7(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
-int launch_tsolve64_hb9(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
-int launch_tsolve64_hb11(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, std::uint32_t *, void *);
+int launch_tsolve64_hb1(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
+int launch_tsolve64_hb3(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
+int launch_tsolve64_hb5(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
+int launch_tsolve64_hb7(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
+int launch_tsolve64_hb9(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
+int launch_tsolve64_hb11(const dev::StreamJob *, int, int, int, dev::Sample, dev::Sample, int, bool, std::uint32_t *, void *);
 
 int launch_tsolve64(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
-                    dev::Sample in, dev::Sample out, int record_floats, std::uint32_t *status, void *stream) {
+                    dev::Sample in, dev::Sample out, int record_floats, bool fused, std::uint32_t *status,
+                    void *stream) {
     switch (half_bandwidth) {
-    case 1: return launch_tsolve64_hb1(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
-    case 3: return launch_tsolve64_hb3(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
-    case 5: return launch_tsolve64_hb5(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
-    case 7: return launch_tsolve64_hb7(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
-    case 9: return launch_tsolve64_hb9(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
-    case 11: return launch_tsolve64_hb11(jobs, job_count, total_blocks, threads, in, out, record_floats, status, stream);
+    case 1: return launch_tsolve64_hb1(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
+    case 3: return launch_tsolve64_hb3(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
+    case 5: return launch_tsolve64_hb5(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
+    case 7: return launch_tsolve64_hb7(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
+    case 9: return launch_tsolve64_hb9(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
+    case 11: return launch_tsolve64_hb11(jobs, job_count, total_blocks, threads, in, out, record_floats, fused, status, stream);
     default: return static_cast<int>(cudaErrorInvalidValue);
     }
 }

@@ -109,8 +109,11 @@ int launch_tsolve(const dev::StreamJob *jobs, int job_count, int total_blocks, i
 // retain Float64: the first pass reads u8/u16/f32 and writes the Float64
 // intermediate, the second reads it and writes f32/u8/u16; the forward-value
 // plane is Float64 (job.y as double); non-finite data sets `status` bits.
+// `fused`: fused multiply-adds and the reciprocal pivot (<= 1 float32 ULP of
+// the CPU route); otherwise the CPU scalar route's order, bit for bit.
 int launch_tsolve64(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads, int half_bandwidth,
-                    dev::Sample in, dev::Sample out, int record_floats, std::uint32_t *status, void *stream);
+                    dev::Sample in, dev::Sample out, int record_floats, bool fused, std::uint32_t *status,
+                    void *stream);
 
 // `record_floats`: the largest forward_stride + backward_stride of the jobs.
 int launch_stream(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth,

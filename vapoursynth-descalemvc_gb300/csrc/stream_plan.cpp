@@ -329,7 +329,7 @@ StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_
         previous = first;
     }
     if (!ring_fits(s0, window, m, 16, ring)) return out;
-    const int fs = (2 + window + hb + 1) / 2 * 2;          // doubles, even
+    const int fs = (3 + window + hb + 1) / 2 * 2;          // doubles, even
     const int bs = std::max(2, (hb + 1) / 2 * 2);
     const auto padded = static_cast<std::size_t>((n + chunk - 1) / chunk) * static_cast<std::size_t>(chunk);
     out.forward.assign(padded * static_cast<std::size_t>(fs), 0.0);
@@ -343,14 +343,15 @@ StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_
         if (real) {
             for (auto k = p.transpose_offsets[j]; k < p.transpose_offsets[j + 1]; ++k) {
                 const int at = p.transpose_indices[k] - start;
-                f[2 + at] = p.transpose_weights_f64[k];
+                f[3 + at] = p.transpose_weights_f64[k];
                 count = std::max(count, at + 1);
             }
             f[1] = p.ldlt_bands_f64[j] + DBL_EPSILON;      // band 0 holds D
+            f[2] = 1.0 / f[1];
             for (int q = 0; q < hb; ++q) {
                 const int d = hb - q;                          // d = hb..1
                 if (static_cast<std::size_t>(d) <= j)
-                    f[2 + window + q] = p.ldlt_bands_f64[static_cast<std::size_t>(d) * w + j - static_cast<std::size_t>(d)];
+                    f[3 + window + q] = p.ldlt_bands_f64[static_cast<std::size_t>(d) * w + j - static_cast<std::size_t>(d)];
             }
             double *b = out.backward.data() + j * static_cast<std::size_t>(bs);
             const auto avail = std::min<std::size_t>(static_cast<std::size_t>(hb), w - j - 1);
@@ -361,6 +362,7 @@ StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_
             }
         } else {
             f[1] = 1.0;
+            f[2] = 1.0;
         }
         const long long head = static_cast<long long>(static_cast<std::uint32_t>(start))
             | (static_cast<long long>(count) << 32);
@@ -390,7 +392,7 @@ StreamPack64 pack_stream_plan64(const AxisPlan &p, int chunk, int ring, bool hb_
                 for (int i = a; i < hi; ++i) {
                     const double *f = out.forward.data() + static_cast<std::size_t>(i) * static_cast<std::size_t>(fs);
                     double s = 0.0;
-                    for (int q = 0; q < hb; ++q) s += f[2 + window + q] * z[static_cast<std::size_t>(i - (hb - q) - a + hb)];
+                    for (int q = 0; q < hb; ++q) s += f[3 + window + q] * z[static_cast<std::size_t>(i - (hb - q) - a + hb)];
                     z[static_cast<std::size_t>(i - a + hb)] = -s;
                 }
                 if (hi == a + span64)

@@ -86,10 +86,10 @@ StreamPack pack_stream_plan(const AxisPlan &plan, int chunk, int ring,
 // Records of the Float64 two-pass transposing kernels (tsolve64_impl.cuh)
 // for plans that retain Float64: window up to 16 samples, monotone window
 // starts, the per-destination ring replay in blocks of 16.  Forward record
-// (doubles): [s0 | count << 32 (bits), D + DBL_EPSILON, window weights
-// (count from s0), L(i, i - d) for d = hb..1]; backward record: L(i + d, i)
-// for d = hb..1; both padded to an even number of doubles.  Strides are in
-// floats (the staging copies floats).
+// (doubles): [s0 | count << 32 (bits), D + DBL_EPSILON, 1 / (D + DBL_EPSILON),
+// window weights (count from s0), L(i, i - d) for d = hb..1]; backward
+// record: L(i + d, i) for d = hb..1; both padded to an even number of
+// doubles.  Strides are in floats (the staging copies floats).
 struct StreamPack64 {
     bool eligible = false;
     int window = 0;

@@ -5,8 +5,8 @@
 namespace dsmvc_gb {
 
 int launch_tsolve64_hb3(const dev::StreamJob *jobs, int count, int blocks, int threads, dev::Sample in,
-                         dev::Sample out, int record_floats, std::uint32_t *status, void *stream) {
-    return x64launch_hb<3>(jobs, count, blocks, threads, in, out, record_floats, status,
+                         dev::Sample out, int record_floats, bool fused, std::uint32_t *status, void *stream) {
+    return x64launch_hb<3>(jobs, count, blocks, threads, in, out, record_floats, fused, status,
                             static_cast<cudaStream_t>(stream));
 }
 

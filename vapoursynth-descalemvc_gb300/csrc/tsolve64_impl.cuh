@@ -13,6 +13,13 @@
 // term.  Two sweeps: the forward values go to a Float64 plane laid out like
 // the output (the intermediate itself in the first pass), the backward sweep
 // reads them back.  Results equal the CPU's bit for bit.
+//
+// FUSED variant (the default route): the same sweeps with every multiply-add
+// fused (fma, one rounding instead of two) and the division by D + DBL_EPSILON
+// replaced by a product with its reciprocal (rounded once on the host): less
+// than half the FP64 pipe operations of the CPU order.  The Float64 results
+// differ from the CPU's by a few double ULPs, far below a float32 ULP, so
+// outputs stay within the <= 1 float32 ULP / <= 1 code contract.
 #pragma once
 
 #include "tstream_impl.cuh"
@@ -122,9 +129,10 @@ struct WarpFeeder64 {
 };
 
 // Record words (doubles): forward [s0 | count << 32 (bits), D + DBL_EPSILON,
-// window weights, L factors for d = HB..1, padding to even]; backward [L
-// factors of the following destinations for d = HB..1, padding to even].
-template <int HB, class In, class Out>
+// 1 / (D + DBL_EPSILON), window weights, L factors for d = HB..1, padding to
+// even]; backward [L factors of the following destinations for d = HB..1,
+// padding to even].
+template <int HB, bool FUSED, class In, class Out>
 __global__ void __launch_bounds__(kTMaxThreads)
 tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floats, std::uint32_t *status) {
     constexpr int LC = kTChunk;
@@ -206,16 +214,24 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
                 feed.ensure(min(s0 + kw, p.source_size));
                 const double *win = ring + (s0 & (kTRing - 1)) * kXPitch + lane;
                 double sum = 0.0;
-                for (int k = 0; k < count; ++k) sum = __dadd_rn(sum, __dmul_rn(rec[2 + k], win[k * kXPitch]));
+                if constexpr (FUSED) {
+                    for (int k = 0; k < count; ++k) sum = fma(rec[3 + k], win[k * kXPitch], sum);
 #pragma unroll
-                for (int q = 0; q < HB; ++q) {                 // d = HB - q, descending
-                    const int d = HB - q;
-                    sum = __dsub_rn(sum, __dmul_rn(rec[2 + kw + q], z[d - 1]));
+                    for (int q = 0; q < HB; ++q) sum = fma(-rec[3 + kw + q], z[HB - q - 1], sum);
+                } else {
+                    for (int k = 0; k < count; ++k) sum = __dadd_rn(sum, __dmul_rn(rec[3 + k], win[k * kXPitch]));
+#pragma unroll
+                    for (int q = 0; q < HB; ++q) {             // d = HB - q, descending
+                        const int d = HB - q;
+                        sum = __dsub_rn(sum, __dmul_rn(rec[3 + kw + q], z[d - 1]));
+                    }
                 }
 #pragma unroll
                 for (int d = HB - 1; d > 0; --d) z[d] = z[d - 1];
                 z[0] = sum;
-                if (active) yplane[static_cast<std::int64_t>(j - ybase) * job.y_elem] = __ddiv_rn(sum, rec[1]);
+                if (active)
+                    yplane[static_cast<std::int64_t>(j - ybase) * job.y_elem] =
+                        FUSED ? sum * rec[2] : __ddiv_rn(sum, rec[1]);
             }
         }
         __syncthreads();
@@ -252,7 +268,7 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
 #pragma unroll
                 for (int q = 0; q < HB; ++q) {                 // d = HB - q, descending
                     const int d = HB - q;
-                    xt = __dsub_rn(xt, __dmul_rn(rec[q], x[d - 1]));
+                    xt = FUSED ? fma(-rec[q], x[d - 1], xt) : __dsub_rn(xt, __dmul_rn(rec[q], x[d - 1]));
                 }
 #pragma unroll
                 for (int d = HB - 1; d > 0; --d) x[d] = x[d - 1];
@@ -267,34 +283,41 @@ tsolve64_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_fl
     if (flags && active) atomicOr(status, flags);
 }
 
-template <int HB, class In, class Out>
+template <int HB, bool FUSED, class In, class Out>
 int x64launch_typed(const StreamJob *jobs, int count, int blocks, int threads, int record_floats,
                     std::uint32_t *status, cudaStream_t s) {
     if (threads < 32 || threads > kTMaxThreads || threads % 32) return static_cast<int>(cudaErrorInvalidValue);
     const int smem = 3 * kTChunk * record_floats * static_cast<int>(sizeof(float))
         + threads / 32 * kXRingDoubles * static_cast<int>(sizeof(double));
-    auto kernel = tsolve64_kernel<HB, In, Out>;
+    auto kernel = tsolve64_kernel<HB, FUSED, In, Out>;
     static SmemLimit limit;
     if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
     kernel<<<blocks, threads, smem, s>>>(jobs, count, record_floats, status);
     return static_cast<int>(cudaGetLastError());
 }
 
-template <int HB>
-int x64launch_hb(const StreamJob *jobs, int count, int blocks, int threads, dev::Sample in, dev::Sample out,
-                 int record_floats, std::uint32_t *status, cudaStream_t s) {
+template <int HB, bool FUSED>
+int x64launch_fused(const StreamJob *jobs, int count, int blocks, int threads, dev::Sample in, dev::Sample out,
+                    int record_floats, std::uint32_t *status, cudaStream_t s) {
     using dev::Sample;
     if (out == Sample::f64) {
-        if (in == Sample::f32) return x64launch_typed<HB, float, double>(jobs, count, blocks, threads, record_floats, status, s);
-        if (in == Sample::u16) return x64launch_typed<HB, std::uint16_t, double>(jobs, count, blocks, threads, record_floats, status, s);
-        if (in == Sample::u8) return x64launch_typed<HB, std::uint8_t, double>(jobs, count, blocks, threads, record_floats, status, s);
+        if (in == Sample::f32) return x64launch_typed<HB, FUSED, float, double>(jobs, count, blocks, threads, record_floats, status, s);
+        if (in == Sample::u16) return x64launch_typed<HB, FUSED, std::uint16_t, double>(jobs, count, blocks, threads, record_floats, status, s);
+        if (in == Sample::u8) return x64launch_typed<HB, FUSED, std::uint8_t, double>(jobs, count, blocks, threads, record_floats, status, s);
     }
     if (in == Sample::f64) {
-        if (out == Sample::f32) return x64launch_typed<HB, double, float>(jobs, count, blocks, threads, record_floats, status, s);
-        if (out == Sample::u16) return x64launch_typed<HB, double, std::uint16_t>(jobs, count, blocks, threads, record_floats, status, s);
-        if (out == Sample::u8) return x64launch_typed<HB, double, std::uint8_t>(jobs, count, blocks, threads, record_floats, status, s);
+        if (out == Sample::f32) return x64launch_typed<HB, FUSED, double, float>(jobs, count, blocks, threads, record_floats, status, s);
+        if (out == Sample::u16) return x64launch_typed<HB, FUSED, double, std::uint16_t>(jobs, count, blocks, threads, record_floats, status, s);
+        if (out == Sample::u8) return x64launch_typed<HB, FUSED, double, std::uint8_t>(jobs, count, blocks, threads, record_floats, status, s);
     }
     return static_cast<int>(cudaErrorInvalidValue);
+}
+
+template <int HB>
+int x64launch_hb(const StreamJob *jobs, int count, int blocks, int threads, dev::Sample in, dev::Sample out,
+                 int record_floats, bool fused, std::uint32_t *status, cudaStream_t s) {
+    return fused ? x64launch_fused<HB, true>(jobs, count, blocks, threads, in, out, record_floats, status, s)
+                 : x64launch_fused<HB, false>(jobs, count, blocks, threads, in, out, record_floats, status, s);
 }
 
 } // namespace
