@@ -163,6 +163,16 @@ void dsmvc_gb_plan_release(dsmvc_gb_plan *plan);
 int dsmvc_gb_plan_build_many(const dsmvc_gb_axis_request *requests,
                              int32_t count, int32_t threads,
                              dsmvc_gb_plan **out);
+/* The same plans with their numerical part computed on GPU `device` (-1:
+ * the current device): the normal-matrix band, its banded LDL^T factor, the
+ * three-stage condition estimate and Float64 routing, and the Float32 solve
+ * arrays, for all plans at once (src/axis_plan.cpp:628-967 run per plan on
+ * the host by the reference); the geometry, kernel weights and A^T CSR stay
+ * on up to `threads` host threads.  The plans equal dsmvc_gb_plan_build's
+ * bit for bit (same plan hashes).  Custom kernels are refused. */
+int dsmvc_gb_plan_build_many_device(const dsmvc_gb_axis_request *requests,
+                                    int32_t count, int32_t device, int32_t threads,
+                                    dsmvc_gb_plan **out);
 int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out);
 /* Read-only view of one plan array: 0 transpose_offsets (u32),
  * 1 transpose_indices (i32), 2 transpose_weights (f32), 3 lower_ld (f32),

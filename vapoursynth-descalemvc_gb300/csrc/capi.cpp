@@ -188,6 +188,22 @@ int dsmvc_gb_plan_build_many(const dsmvc_gb_axis_request *requests, int32_t coun
     });
 }
 
+int dsmvc_gb_plan_build_many_device(const dsmvc_gb_axis_request *requests, int32_t count, int32_t device,
+                                    int32_t threads, dsmvc_gb_plan **out) {
+    return guarded([&] {
+        if (count < 0 || (count > 0 && (!requests || !out))) throw std::invalid_argument("invalid plan list");
+        std::vector<dsmvc_gb::AxisRequest> qs;
+        qs.reserve(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) qs.push_back(to_request(&requests[i]));
+        for (int32_t i = 0; i < count; ++i) out[i] = nullptr;
+        auto plans = dsmvc_gb::build_axis_plans_on_device(qs, device, threads);
+        for (int32_t i = 0; i < count; ++i)
+            out[i] = new dsmvc_gb_plan{std::make_shared<const dsmvc_gb::AxisPlan>(
+                                           std::move(plans[static_cast<std::size_t>(i)])),
+                                       qs[static_cast<std::size_t>(i)]};
+    });
+}
+
 int dsmvc_gb_plan_get_info(const dsmvc_gb_plan *plan, dsmvc_gb_plan_info *out) {
     return guarded([&] {
         const auto &p = plan_of(plan);

@@ -3,6 +3,10 @@
 // order of the reference planner, src/axis_plan.cpp:246-970.
 #include "planner.hpp"
 
+#include "gpu_planner.cuh"
+
+#include <cuda_runtime.h>
+
 #include <algorithm>
 #include <bit>
 #include <cfloat>
@@ -17,6 +21,7 @@
 #include <numbers>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <unordered_map>
 
 namespace dsmvc_gb {
@@ -700,6 +705,209 @@ std::uint64_t complete_plan_hash(const AxisRequest &r, const AxisPlan &p) {
     h.span(p.ldlt_bands_f64);
     h.span(p.inverse_diagonal_f64);
     return h.v;
+}
+
+// ---- device planning batch ------------------------------------------------
+
+namespace {
+
+void device_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA ") + what + ": " + cudaGetErrorString(e));
+}
+
+struct HostHalf {
+    std::int32_t support = 0;
+    std::int32_t hb = 0;
+    Csr t;
+};
+
+// One batch of at most 65535 plans.
+void plan_batch_on_device(const AxisRequest *requests, HostHalf *halves, std::size_t count, AxisPlan *out) {
+    std::vector<PlannerJob> jobs(count);
+    std::int64_t offsets = 0, entries = 0, bands = 0, factors = 0, diagonal = 0, work = 0;
+    int max_n = 1;
+    for (std::size_t k = 0; k < count; ++k) {
+        const auto &h = halves[k];
+        auto &j = jobs[k];
+        j.n = requests[k].destination_size;
+        j.hb = h.hb;
+        j.mode = static_cast<std::int32_t>(requests[k].f64_mode);
+        j.offsets_at = offsets;
+        j.entries_at = entries;
+        j.bands_at = bands;
+        j.factors_at = factors;
+        j.diagonal_at = diagonal;
+        j.work_at = work;
+        offsets += j.n + 1;
+        entries += static_cast<std::int64_t>(h.t.indices.size());
+        bands += static_cast<std::int64_t>(h.hb + 1) * j.n;
+        factors += static_cast<std::int64_t>(h.hb) * j.n;
+        diagonal += j.n;
+        work += 4 * static_cast<std::int64_t>(j.n);
+        max_n = std::max(max_n, j.n);
+    }
+    // One device allocation: inputs first (one upload), then the outputs.
+    auto al = [](std::size_t v) { return (v + 255) / 256 * 256; };
+    const std::size_t b_jobs = al(count * sizeof(PlannerJob)), b_off = al(static_cast<std::size_t>(offsets) * 4),
+                      b_idx = al(static_cast<std::size_t>(entries) * 4), b_w = al(static_cast<std::size_t>(entries) * 8);
+    const std::size_t in_bytes = b_jobs + b_off + b_idx + b_w;
+    const std::size_t b_bands = al(static_cast<std::size_t>(bands) * 8), b_fac = al(static_cast<std::size_t>(factors) * 4),
+                      b_diag = al(static_cast<std::size_t>(diagonal) * 4), b_diag64 = al(static_cast<std::size_t>(diagonal) * 8),
+                      b_work = al(static_cast<std::size_t>(work) * 8), b_res = al(count * sizeof(PlannerResult));
+    const std::size_t total = in_bytes + 2 * b_bands + 2 * b_fac + b_diag + b_diag64 + b_work + b_res;
+    std::vector<char> host(in_bytes, 0);
+    std::memcpy(host.data(), jobs.data(), count * sizeof(PlannerJob));
+    {
+        char *o = host.data() + b_jobs;
+        char *ix = o + b_off;
+        char *w = ix + b_idx;
+        for (std::size_t k = 0; k < count; ++k) {
+            const auto &t = halves[k].t;
+            std::memcpy(o + jobs[k].offsets_at * 4, t.offsets.data(), t.offsets.size() * 4);
+            std::memcpy(ix + jobs[k].entries_at * 4, t.indices.data(), t.indices.size() * 4);
+            std::memcpy(w + jobs[k].entries_at * 8, t.weights.data(), t.weights.size() * 8);
+        }
+    }
+    char *dev = nullptr;
+    device_check(cudaMalloc(&dev, total), "allocating the planning batch");
+    struct Free {
+        char *p;
+        ~Free() { cudaFree(p); }
+    } release{dev};
+    cudaStream_t stream = nullptr;
+    device_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "creating a stream");
+    struct Destroy {
+        cudaStream_t s;
+        ~Destroy() { cudaStreamDestroy(s); }
+    } destroy{stream};
+    device_check(cudaMemcpyAsync(dev, host.data(), in_bytes, cudaMemcpyHostToDevice, stream), "uploading plans");
+    PlannerBatch b;
+    b.jobs = reinterpret_cast<const PlannerJob *>(dev);
+    b.count = static_cast<int>(count);
+    b.max_n = max_n;
+    b.offsets = reinterpret_cast<const std::uint32_t *>(dev + b_jobs);
+    b.indices = reinterpret_cast<const std::int32_t *>(dev + b_jobs + b_off);
+    b.weights = reinterpret_cast<const double *>(dev + b_jobs + b_off + b_idx);
+    char *o = dev + in_bytes;
+    b.bands = reinterpret_cast<double *>(o);
+    b.factor = reinterpret_cast<double *>(o + b_bands);
+    b.lower = reinterpret_cast<float *>(o + 2 * b_bands);
+    b.upper = reinterpret_cast<float *>(o + 2 * b_bands + b_fac);
+    b.inv_diag = reinterpret_cast<float *>(o + 2 * b_bands + 2 * b_fac);
+    b.inv_diag64 = reinterpret_cast<double *>(o + 2 * b_bands + 2 * b_fac + b_diag);
+    b.work = reinterpret_cast<double *>(o + 2 * b_bands + 2 * b_fac + b_diag + b_diag64);
+    b.results = reinterpret_cast<PlannerResult *>(o + 2 * b_bands + 2 * b_fac + b_diag + b_diag64 + b_work);
+    device_check(static_cast<cudaError_t>(launch_device_planner(b, stream)), "launching the device planner");
+    // Float32 arrays and results of every plan in three copies.
+    std::vector<float> lower(static_cast<std::size_t>(factors)), upper(static_cast<std::size_t>(factors)),
+        inv(static_cast<std::size_t>(diagonal));
+    std::vector<PlannerResult> results(count);
+    device_check(cudaMemcpyAsync(lower.data(), b.lower, lower.size() * 4, cudaMemcpyDeviceToHost, stream), "reading plans");
+    device_check(cudaMemcpyAsync(upper.data(), b.upper, upper.size() * 4, cudaMemcpyDeviceToHost, stream), "reading plans");
+    device_check(cudaMemcpyAsync(inv.data(), b.inv_diag, inv.size() * 4, cudaMemcpyDeviceToHost, stream), "reading plans");
+    device_check(cudaMemcpyAsync(results.data(), b.results, count * sizeof(PlannerResult), cudaMemcpyDeviceToHost, stream),
+                 "reading plans");
+    device_check(cudaStreamSynchronize(stream), "planning on the device");
+    for (std::size_t k = 0; k < count; ++k) {
+        const auto &r = requests[k];
+        auto &h = halves[k];
+        const auto &res = results[k];
+        const auto n = r.destination_size;
+        const auto w = static_cast<std::size_t>(n);
+        AxisPlan &p = out[k];
+        p.source_size = r.source_size;
+        p.destination_size = n;
+        p.support = h.support;
+        p.half_bandwidth = h.hb;
+        p.active_length = r.active_length;
+        p.shift = r.shift;
+        p.normal_rcond = res.rcond;
+        p.transpose_weights.resize(h.t.weights.size());
+        std::transform(h.t.weights.begin(), h.t.weights.end(), p.transpose_weights.begin(),
+                       [](double x) { return static_cast<float>(x); });
+        for (std::int32_t i = 0; i < n; ++i)
+            p.max_row_entries = std::max<std::int32_t>(
+                p.max_row_entries, static_cast<std::int32_t>(h.t.offsets[i + 1] - h.t.offsets[i]));
+        if (res.f64) {
+            const std::size_t nb = (static_cast<std::size_t>(h.hb) + 1U) * w;
+            p.normal_inf_norm = res.one_norm;
+            p.normal_bands_f64.resize(nb);
+            p.ldlt_bands_f64.resize(nb);
+            p.inverse_diagonal_f64.resize(w);
+            device_check(cudaMemcpyAsync(p.normal_bands_f64.data(), b.bands + jobs[k].bands_at, nb * 8,
+                                         cudaMemcpyDeviceToHost, stream), "reading plans");
+            device_check(cudaMemcpyAsync(p.ldlt_bands_f64.data(), b.factor + jobs[k].bands_at, nb * 8,
+                                         cudaMemcpyDeviceToHost, stream), "reading plans");
+            device_check(cudaMemcpyAsync(p.inverse_diagonal_f64.data(), b.inv_diag64 + jobs[k].diagonal_at, w * 8,
+                                         cudaMemcpyDeviceToHost, stream), "reading plans");
+            p.transpose_weights_f64 = h.t.weights;
+        }
+        p.transpose_offsets = std::move(h.t.offsets);
+        p.transpose_indices = std::move(h.t.indices);
+        const auto f_at = static_cast<std::size_t>(jobs[k].factors_at);
+        const auto d_at = static_cast<std::size_t>(jobs[k].diagonal_at);
+        p.lower_ld.assign(lower.begin() + static_cast<std::ptrdiff_t>(f_at),
+                          lower.begin() + static_cast<std::ptrdiff_t>(f_at + static_cast<std::size_t>(h.hb) * w));
+        p.upper_l.assign(upper.begin() + static_cast<std::ptrdiff_t>(f_at),
+                         upper.begin() + static_cast<std::ptrdiff_t>(f_at + static_cast<std::size_t>(h.hb) * w));
+        p.inverse_diagonal.assign(inv.begin() + static_cast<std::ptrdiff_t>(d_at),
+                                  inv.begin() + static_cast<std::ptrdiff_t>(d_at + w));
+    }
+    device_check(cudaStreamSynchronize(stream), "reading Float64 plans");
+    for (std::size_t k = 0; k < count; ++k) {
+        if (!out[k].valid()) throw std::runtime_error("failed to build inverse axis plan");
+        out[k].validated = true;
+    }
+}
+
+} // namespace
+
+std::vector<AxisPlan> build_axis_plans_on_device(const std::vector<AxisRequest> &requests, int device,
+                                                 int threads) {
+    const std::size_t count = requests.size();
+    std::vector<AxisPlan> out(count);
+    if (count == 0) return out;
+    for (const auto &r : requests)
+        if (r.kernel.kind == KernelKind::custom)
+            throw std::invalid_argument("custom kernels are planned on the host (build_axis_plan)");
+    g_builds.fetch_add(count, std::memory_order_relaxed);
+    // The host half (geometry, kernel weights, the A^T CSR) on host threads.
+    std::vector<HostHalf> halves(count);
+    std::vector<std::string> errors(count);
+    std::atomic<std::size_t> next{0};
+    auto worker = [&] {
+        for (std::size_t i = next++; i < count; i = next++) {
+            try {
+                const auto &r = requests[i];
+                auto &h = halves[i];
+                h.support = effective_support(r);
+                h.t = transpose(descale_matrix(r, h.support, {}), r.source_size, r.destination_size);
+                h.hb = std::min(2 * h.support - 1, r.destination_size - 1);
+            } catch (const std::exception &e) {
+                errors[i] = e.what();
+            }
+        }
+    };
+    unsigned n = threads > 0 ? static_cast<unsigned>(threads) : std::thread::hardware_concurrency();
+    n = std::max(1U, std::min<unsigned>(n, static_cast<unsigned>(count)));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < n; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+    for (std::size_t i = 0; i < count; ++i)
+        if (!errors[i].empty()) throw std::invalid_argument("plan " + std::to_string(i) + ": " + errors[i]);
+
+    int previous = -1;
+    device_check(cudaGetDevice(&previous), "querying the device");
+    if (device >= 0) device_check(cudaSetDevice(device), "selecting the device");
+    struct Restore {
+        int d;
+        ~Restore() { if (d >= 0) cudaSetDevice(d); }
+    } restore{previous};
+    constexpr std::size_t kBatch = 65535;
+    for (std::size_t at = 0; at < count; at += kBatch)
+        plan_batch_on_device(requests.data() + at, halves.data() + at, std::min(kBatch, count - at), out.data() + at);
+    return out;
 }
 
 } // namespace dsmvc_gb

@@ -109,6 +109,15 @@ struct PlannerCacheStats {
 [[nodiscard]] std::shared_ptr<const AxisPlan> get_or_build_axis_plan(
     const AxisRequest &request, const CustomKernel &custom = {});
 
+// Many plans at once with their normal band, banded LDL^T, condition
+// estimate and Float32 arrays computed on the GPU `device` (-1: the current
+// one), the geometry, kernel weights and A^T CSR on up to `threads` host
+// threads (0: one per hardware thread).  Plans equal build_axis_plan's bit
+// for bit (same plan hashes).  Custom kernels are refused (they plan on the
+// host); the plan cache is not consulted.
+[[nodiscard]] std::vector<AxisPlan> build_axis_plans_on_device(
+    const std::vector<AxisRequest> &requests, int device, int threads);
+
 [[nodiscard]] PlannerCacheStats planner_cache_stats();
 void clear_planner_caches();
 

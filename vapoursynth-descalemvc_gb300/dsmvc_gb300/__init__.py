@@ -195,6 +195,8 @@ SIGNATURES = {
                                      C.c_void_p, C.c_int64, C.POINTER(ConversionC), C.c_void_p],
                                     C.c_int),
     "dsmvc_gb_plan_import": ([C.POINTER(PlanArraysC), C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_plan_build_many_device": ([C.POINTER(AxisRequestC), C.c_int32, C.c_int32, C.c_int32,
+                                         C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_plan_build_many": ([C.POINTER(AxisRequestC), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_sweep_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.c_int32,
@@ -393,12 +395,18 @@ def measure_fp64_peak(device: int = 0) -> float:
     return t.value
 
 
-def build_plans(requests: Sequence[AxisRequest], threads: int = 0) -> list:
-    """dsmvc_gb_plan_build_many: uncached plans built on `threads` host
-    threads (0 = all hardware threads)."""
+def build_plans(requests: Sequence[AxisRequest], threads: int = 0, device: Optional[int] = None) -> list:
+    """Uncached plans: dsmvc_gb_plan_build_many on `threads` host threads
+    (0 = all hardware threads), or with `device` (a CUDA device index, -1 =
+    the current one) dsmvc_gb_plan_build_many_device: the normal band, LDL^T,
+    condition estimate and Float32 arrays of every plan on that GPU, bit
+    for bit the same plans."""
     reqs = (AxisRequestC * len(requests))(*[r.to_c() for r in requests])
     out = (C.c_void_p * len(requests))()
-    _check(lib().dsmvc_gb_plan_build_many(reqs, len(requests), int(threads), out))
+    if device is None:
+        _check(lib().dsmvc_gb_plan_build_many(reqs, len(requests), int(threads), out))
+    else:
+        _check(lib().dsmvc_gb_plan_build_many_device(reqs, len(requests), int(device), int(threads), out))
     return [AxisPlan(r, _handle=out[i]) for i, r in enumerate(requests)]
 
 
