@@ -36,7 +36,7 @@ CUDA_SOURCES = TSTREAM2_SOURCES + TSOLVE_SOURCES + ["kernels.cu", "stream.cu", "
                 "stream_hb7.cu", "tstream_hb1.cu", "tstream_hb3.cu",
                 "tstream_hb5.cu", "tstream_hb7.cu", "tstream_hb1_g.cu", "tstream_hb3_g.cu",
                 "tstream_hb5_g.cu", "tstream_hb7_g.cu", "noalloc.cu", "score.cu",
-                "peak.cu", "gpu_planner.cu"]
+                "peak.cu", "gpu_planner.cu", "refine64.cu"]
 
 
 def cuda_home() -> str:

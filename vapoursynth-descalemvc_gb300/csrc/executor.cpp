@@ -122,6 +122,7 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         {p.inverse_diagonal.data(), p.inverse_diagonal.size() * 4},
         {f64 ? p.transpose_weights_f64.data() : nullptr, f64 ? p.transpose_weights_f64.size() * 8 : 0},
         {f64 ? p.ldlt_bands_f64.data() : nullptr, f64 ? p.ldlt_bands_f64.size() * 8 : 0},
+        {f64 ? p.normal_bands_f64.data() : nullptr, f64 ? p.normal_bands_f64.size() * 8 : 0},
     };
     const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
                                              tsolve_supports(p.half_bandwidth));
@@ -173,6 +174,7 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
     v.inv_diag = reinterpret_cast<const float *>(base + offsets[5]);
     v.weights64 = f64 ? reinterpret_cast<const double *>(base + offsets[6]) : nullptr;
     v.bands64 = f64 ? reinterpret_cast<const double *>(base + offsets[7]) : nullptr;
+    v.normal64 = f64 ? reinterpret_cast<const double *>(base + offsets[8]) : nullptr;
     if (pack.eligible || pack.exact) {
         dp->stream = pack.eligible;
         dp->stream_u16 = pack.eligible && pack.ring_ok_u16;
@@ -390,6 +392,10 @@ struct Executor::Impl {
     // FP64 operations); DSMVC_GB_F64_EXACT=1 (or DSMVC_GB_EXACT=1) runs the
     // CPU scalar route's operation order, equal to it bit for bit.
     bool f64_fused = true;
+    // DSMVC_GB_F64_REFINE=1: Float64 2D planes on the two-pass Float64
+    // kernels add one residual refinement step per pass (refine64.cu): the
+    // columns pass then writes a Float64 plane, refined and converted last.
+    bool f64_refine = false;
     // Default CTA size of the transposing kernels (DSMVC_GB_TSTREAM_THREADS,
     // 32..256 in multiples of 32); batches may tune it per launch group.
     int tstream_threads = kTStreamThreads;
@@ -556,7 +562,7 @@ int compiled_window(const DevicePlan &dp, int kind) {
 
 std::string kernel_name(const GroupKey &k) {
     static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32",
-                                  "tsolve_f32", "tsolve_f64"};
+                                  "tsolve_f32", "tsolve_f64", "refine_f64", "convert_f64"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -674,6 +680,10 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         // scratch (each segment's own, margins included).
         int seg_h = 1, seg_v = 1;
         std::size_t yseg_h = 0, yseg_v = 0;
+        // Refinement (f64_refine): per-vector correction scratch of each
+        // pass and the Float64 result plane of the columns pass.
+        bool refine = false;
+        std::size_t ref_h = 0, ref_v = 0, x64 = 0;
     };
     std::vector<Route> routes(tasks.size());
     std::size_t bytes = 0;
@@ -698,6 +708,15 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             r.fwd_stride = static_cast<std::size_t>(h->destination_size);
             r.fwd = bytes;
             bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 8);
+            if (f64_refine) {
+                r.refine = true;
+                r.ref_h = bytes;
+                bytes += align_up(r.mid_stride * static_cast<std::size_t>(h->destination_size) * 8);
+                r.x64 = bytes;
+                bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 8);
+                r.ref_v = bytes;
+                bytes += align_up(r.fwd_stride * static_cast<std::size_t>(v->destination_size) * 8);
+            }
         } else if (h && v && !r.f64) {
             r.transposed = true;
             auto pass_kind = [&](const DevicePlan &dp) {
@@ -835,16 +854,53 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             push_segments(groups[{0, 6, h->half_bandwidth, task.sample, dev::Sample::f64, 0}], hi,
                           r.h->chunk_first_block64, r.h->margin64, h->destination_size, r.seg_h, base + r.yseg_h, pitch,
                           8);
+            const auto xs = static_cast<std::int64_t>(r.fwd_stride);
+            if (r.refine) {
+                // Rows: x is the intermediate (destination-major), b the input.
+                Item ri;
+                auto &q = ri.axis;
+                q.plan = r.h->view;
+                q.in = task.input; q.in_elem = 1; q.in_vec = task.input_stride;
+                q.out = mid; q.out_elem = pitch; q.out_vec = 1;
+                q.fwd = base + r.ref_h; q.fwd_elem = pitch; q.fwd_vec = 1;
+                q.vectors = v->source_size;
+                q.conv = conv;
+                groups[{0, 7, h->half_bandwidth, task.sample, dev::Sample::f64, 0}].push_back(ri);
+            }
             auto &b = vi.stream;
             b.plan = r.v->stream_view64;
             b.in = mid; b.in_elem = 1; b.in_vec = pitch;
-            b.out = task.output; b.out_elem = task.output_stride; b.out_vec = 1;
-            b.y = reinterpret_cast<float *>(base + r.fwd); b.y_elem = static_cast<std::int64_t>(r.fwd_stride);
+            if (r.refine) {
+                b.out = base + r.x64; b.out_elem = xs; b.out_vec = 1;
+            } else {
+                b.out = task.output; b.out_elem = task.output_stride; b.out_vec = 1;
+            }
+            b.y = reinterpret_cast<float *>(base + r.fwd); b.y_elem = xs;
             b.vectors = h->destination_size;
             b.conv = conv;
-            push_segments(groups[{1, 6, v->half_bandwidth, dev::Sample::f64, task.sample, 0}], vi,
-                          r.v->chunk_first_block64, r.v->margin64, v->destination_size, r.seg_v, base + r.yseg_v,
-                          static_cast<std::int64_t>(r.fwd_stride), 8);
+            push_segments(groups[{1, 6, v->half_bandwidth, dev::Sample::f64, r.refine ? dev::Sample::f64 : task.sample,
+                                  0}], vi,
+                          r.v->chunk_first_block64, r.v->margin64, v->destination_size, r.seg_v, base + r.yseg_v, xs, 8);
+            if (r.refine) {
+                // Columns: x is the Float64 result plane, b the intermediate;
+                // then the conversion into the output.
+                Item ci, oi;
+                auto &q = ci.axis;
+                q.plan = r.v->view;
+                q.in = mid; q.in_elem = 1; q.in_vec = pitch;
+                q.out = base + r.x64; q.out_elem = xs; q.out_vec = 1;
+                q.fwd = base + r.ref_v; q.fwd_elem = xs; q.fwd_vec = 1;
+                q.vectors = h->destination_size;
+                q.conv = conv;
+                groups[{1, 7, v->half_bandwidth, dev::Sample::f64, dev::Sample::f64, 0}].push_back(ci);
+                auto &o = oi.axis;
+                o.plan = r.h->view;                 // destination_size: the row length
+                o.in = base + r.x64; o.in_elem = 1; o.in_vec = xs;
+                o.out = task.output; o.out_elem = 1; o.out_vec = task.output_stride;
+                o.vectors = v->destination_size;
+                o.conv = conv;
+                groups[{1, 8, 0, dev::Sample::f64, task.sample, 0}].push_back(oi);
+            }
             continue;
         }
         if (r.transposed) {
@@ -998,9 +1054,9 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     table.clear();
     launches.clear();
     for (auto &[key, items] : groups) {
-        const bool is_stream = key.kind >= 2;
-        int per_block = key.kind == 2 ? stream_block : key.kind >= 3 ? tstream_threads : kSeqThreads;
-        if (tuning && key.kind != 2) {
+        const bool is_stream = key.kind >= 2 && key.kind <= 6;
+        int per_block = key.kind == 2 ? stream_block : is_stream ? tstream_threads : kSeqThreads;
+        if (tuning && key.kind != 2 && key.kind <= 6) {
             const GroupTuple g{key.pass, key.kind, key.hb, static_cast<int>(key.in), static_cast<int>(key.out),
                                key.variant};
             if (auto it = tuning->find(g); it != tuning->end()) per_block = it->second;
@@ -1013,7 +1069,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         // Transposing kernels are assigned warps, not CTAs: a CTA's warps
         // may serve consecutive jobs of one plan (they share the CTA's record
         // copies), so only plan changes round up to a whole CTA.
-        const bool by_warp = key.kind >= 3;
+        const bool by_warp = key.kind >= 3 && key.kind <= 6;
         const int warps_per_cta = per_block / 32;
         const int vectors_per_warp = key.kind == 4 ? 64 : 32;
         if (by_warp)
@@ -1072,7 +1128,13 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         }
         const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.kind == 6) {
+        if (l.kind == 7) {
+            rc = launch_refine64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks, l.threads,
+                                 l.hb, l.in, status, stream);
+        } else if (l.kind == 8) {
+            rc = launch_convert64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks, l.threads,
+                                  l.out, status, stream);
+        } else if (l.kind == 6) {
             rc = launch_tsolve64(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.threads,
                                  l.hb, l.in, l.out, l.record_floats, f64_fused, status, stream);
         } else if (l.kind == 5) {
@@ -1118,7 +1180,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
     if (c.launches.empty()) return;
     ws.upload_table(c.table);
     launch(c, ws.jobs.data(), ws.stream, ws.status);
-    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind == 6;
+    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind >= 6;
     if (c.private_uploads > 0) {
         // Private plan uploads must outlive the kernels that read them.
         // (Cached plans evicted meanwhile are released by cudaFree, which
@@ -1163,6 +1225,7 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
     if (impl_->prefer_exact) impl_->f64_fused = false;
     if (const char *env = std::getenv("DSMVC_GB_F64_EXACT"))
         impl_->f64_fused = std::string(env) != "1" && !impl_->prefer_exact;
+    if (const char *env = std::getenv("DSMVC_GB_F64_REFINE")) impl_->f64_refine = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_HOST_DIRECT")) impl_->host_direct = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
         char *end = nullptr;
@@ -1702,8 +1765,8 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
     validate_tasks(tasks);
     for (const auto &[key, threads] : tuning ? *tuning : BatchTuning{}) {
         const int kind = key[1];
-        const int most = kind >= 3 ? 256 : 128;
-        if (kind == 2 || threads < 32 || threads > most || threads % 32)
+        const int most = kind >= 3 && kind <= 6 ? 256 : 128;
+        if (kind == 2 || kind > 6 || threads < 32 || threads > most || threads % 32)
             throw std::invalid_argument("invalid CTA size in batch tuning");
     }
     Executor::Impl::Tuning t;

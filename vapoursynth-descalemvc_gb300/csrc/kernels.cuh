@@ -24,6 +24,7 @@ struct PlanView {
     const float *inv_diag;
     const double *weights64;
     const double *bands64;
+    const double *normal64;     // unfactored normal band G (Float64 plans), band d at d*n+i
 };
 
 // IntegerConversion (include/dsmvc/engine.hpp:167-173).
@@ -73,5 +74,13 @@ int launch_axis_f32(const dev::AxisJob *jobs, int job_count, int total_blocks,
 int launch_axis_f64(const dev::AxisJob *jobs, int job_count, int total_blocks,
                     int threads, int half_bandwidth, dev::Sample in,
                     dev::Sample out, std::uint32_t *status, void *stream);
+// Float64 residual refinement of solved vectors and the conversion of a
+// Float64 result (refine64.cu); 32..128 threads a block, one vector (or
+// output row) per thread.
+int launch_refine64(const dev::AxisJob *jobs, int job_count, int total_blocks,
+                    int threads, int half_bandwidth, dev::Sample in,
+                    std::uint32_t *status, void *stream);
+int launch_convert64(const dev::AxisJob *jobs, int job_count, int total_blocks,
+                     int threads, dev::Sample out, std::uint32_t *status, void *stream);
 
 } // namespace dsmvc_gb

@@ -306,6 +306,7 @@ int x64launch_fused(const StreamJob *jobs, int count, int blocks, int threads, d
         if (in == Sample::u8) return x64launch_typed<HB, FUSED, std::uint8_t, double>(jobs, count, blocks, threads, record_floats, status, s);
     }
     if (in == Sample::f64) {
+        if (out == Sample::f64) return x64launch_typed<HB, FUSED, double, double>(jobs, count, blocks, threads, record_floats, status, s);
         if (out == Sample::f32) return x64launch_typed<HB, FUSED, double, float>(jobs, count, blocks, threads, record_floats, status, s);
         if (out == Sample::u16) return x64launch_typed<HB, FUSED, double, std::uint16_t>(jobs, count, blocks, threads, record_floats, status, s);
         if (out == Sample::u8) return x64launch_typed<HB, FUSED, double, std::uint8_t>(jobs, count, blocks, threads, record_floats, status, s);
