@@ -266,6 +266,11 @@ int dsmvc_gb_executor_create(int32_t device, dsmvc_gb_executor **out);
 void dsmvc_gb_executor_destroy(dsmvc_gb_executor *executor);
 /* Executor::prepare / seal (engine.hpp:383-385). */
 int dsmvc_gb_prepare(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan);
+/* Many Executor::prepare calls at once (a sweep's thousands of plans): the
+ * plans' device images are packed on host threads and uploaded in one
+ * allocation with one copy. */
+int dsmvc_gb_prepare_many(dsmvc_gb_executor *executor, const dsmvc_gb_plan *const *plans,
+                          int32_t count);
 int dsmvc_gb_seal(dsmvc_gb_executor *executor);
 int dsmvc_gb_executor_get_stats(dsmvc_gb_executor *executor,
                                 dsmvc_gb_executor_stats *out);

@@ -70,3 +70,26 @@ def test_device_planner_refuses_custom_kernels(gb, executor):
     req = gb.AxisRequest(64, 48, 48.0, 0.0, "custom", 3)
     with pytest.raises(ValueError, match="custom"):
         gb.build_plans([req], device=0)
+
+
+def test_prepare_many_matches_single_prepares(gb, executor):
+    """dsmvc_gb_prepare_many (one upload for many plans, device-planned
+    here) serves calls exactly like plans prepared one at a time."""
+    from common import make_input
+    reqs = [gb.AxisRequest(480, 320, 320.0, 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 0),
+            gb.AxisRequest(270, 180, 180.0, 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 0),
+            gb.AxisRequest(300, 200, 200.0, 0.0, "spline36", 3, 0.0, 0.5, 1.0, "reflect101", 2),
+            gb.AxisRequest(170, 113, 113.0, 0.0, "bicubic", 3, 0.0, 0.5, 1.0, "symmetric", 2)]
+    plans = gb.build_plans(reqs, device=0)
+    single = gb.Executor(0)
+    many = gb.Executor(0)
+    for p in plans:
+        single.prepare(p)
+    many.prepare_many(plans + plans[:1])          # repeats are prepared once
+    for h, v, sample in ((plans[0], plans[1], "f32"), (plans[0], plans[1], "u16"), (plans[2], plans[3], "f32")):
+        x = make_input(v.source_size, h.source_size, sample, 5)
+        conv = gb.integer_conversion(16, False, False) if sample == "u16" else None
+        assert np.array_equal(single.inverse_2d(h, v, x, conv), many.inverse_2d(h, v, x, conv))
+    assert many.stats()["plan_uploads"] == 4
+    single.close()
+    many.close()

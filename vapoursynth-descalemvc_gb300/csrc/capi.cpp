@@ -390,6 +390,19 @@ int dsmvc_gb_prepare(dsmvc_gb_executor *executor, const dsmvc_gb_plan *plan) {
     });
 }
 
+int dsmvc_gb_prepare_many(dsmvc_gb_executor *executor, const dsmvc_gb_plan *const *plans, int32_t count) {
+    return guarded([&] {
+        if (count < 0 || (count > 0 && !plans)) throw std::invalid_argument("invalid plan list");
+        std::vector<std::shared_ptr<const dsmvc_gb::AxisPlan>> list;
+        list.reserve(static_cast<std::size_t>(count));
+        for (int32_t i = 0; i < count; ++i) {
+            plan_of(plans[i]);
+            list.push_back(plans[i]->plan);
+        }
+        exec_of(executor).prepare_many(list);
+    });
+}
+
 int dsmvc_gb_seal(dsmvc_gb_executor *executor) {
     return guarded([&] { exec_of(executor).seal(); });
 }

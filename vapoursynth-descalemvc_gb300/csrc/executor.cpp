@@ -31,6 +31,9 @@
 #include <cstdlib>
 #include <functional>
 #include <unordered_map>
+#include <atomic>
+#include <thread>
+#include <vector>
 
 namespace dsmvc_gb {
 namespace {
@@ -82,6 +85,8 @@ private:
 struct DevicePlan {
     std::shared_ptr<const AxisPlan> keep;
     DeviceBuffer memory;
+    // Plans prepared together share one allocation (upload_plans).
+    std::shared_ptr<DeviceBuffer> arena;
     dev::PlanView view{};
     // Streaming-kernel records (when the plan qualifies, stream_plan.hpp).
     bool stream = false;
@@ -110,7 +115,17 @@ struct DevicePlan {
     std::size_t bytes = 0;
 };
 
-std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const AxisPlan> keep) {
+// Host image of a device plan: every array the kernels read, packed at
+// 256-byte offsets, with the stream-kernel admission of the plan.
+struct PlanImage {
+    std::vector<char> bytes;
+    std::vector<std::size_t> offsets;
+    StreamPack pack;
+    StreamPack64 pack64;
+    std::size_t at_records = 0, at_paired = 0, at_records64 = 0, at_groups = 0;
+};
+
+PlanImage plan_image(const AxisPlan &p) {
     if (!p.valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
     const bool f64 = p.requires_float64();
     std::vector<std::pair<const void *, std::size_t>> parts = {
@@ -124,10 +139,14 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         {f64 ? p.ldlt_bands_f64.data() : nullptr, f64 ? p.ldlt_bands_f64.size() * 8 : 0},
         {f64 ? p.normal_bands_f64.data() : nullptr, f64 ? p.normal_bands_f64.size() * 8 : 0},
     };
-    const StreamPack pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
-                                             tsolve_supports(p.half_bandwidth));
-    const StreamPack64 pack64 = pack_stream_plan64(p, kStreamChunk, kStreamRing, tsolve_supports(p.half_bandwidth));
-    std::size_t at_records = 0, at_paired = 0, at_records64 = 0, at_groups = 0;
+    PlanImage img;
+    img.pack = pack_stream_plan(p, kStreamChunk, kStreamRing, stream_supports(p.half_bandwidth),
+                                tsolve_supports(p.half_bandwidth));
+    img.pack64 = pack_stream_plan64(p, kStreamChunk, kStreamRing, tsolve_supports(p.half_bandwidth));
+    const StreamPack &pack = img.pack;
+    const StreamPack64 &pack64 = img.pack64;
+    std::size_t &at_records = img.at_records, &at_paired = img.at_paired, &at_records64 = img.at_records64,
+                &at_groups = img.at_groups;
     if (pack.eligible || pack.exact) {
         at_records = parts.size();
         parts.push_back({pack.forward.data(), pack.forward.size() * 4});
@@ -149,18 +168,25 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         parts.push_back({pack64.backward.data(), pack64.backward.size() * 8});
     }
     std::size_t total = 0;
-    std::vector<std::size_t> offsets;
     for (auto &part : parts) {
-        offsets.push_back(total);
+        img.offsets.push_back(total);
         total += align_up(std::max<std::size_t>(part.second, 1));
     }
-    std::vector<char> host(total, 0);
+    img.bytes.assign(total, 0);
     for (std::size_t i = 0; i < parts.size(); ++i)
-        if (parts[i].second) std::memcpy(host.data() + offsets[i], parts[i].first, parts[i].second);
-    auto dp = std::make_shared<DevicePlan>();
-    dp->memory.reserve(total);
-    cuda_check(cudaMemcpy(dp->memory.data(), host.data(), total, cudaMemcpyHostToDevice), "uploading plan");
-    char *base = dp->memory.data();
+        if (parts[i].second) std::memcpy(img.bytes.data() + img.offsets[i], parts[i].first, parts[i].second);
+    return img;
+}
+
+// Fills a device plan's views for its image uploaded at `base`.
+void finish_plan(DevicePlan *dp, const AxisPlan &p, const PlanImage &img, char *base) {
+    const bool f64 = p.requires_float64();
+    const StreamPack &pack = img.pack;
+    const StreamPack64 &pack64 = img.pack64;
+    const std::vector<std::size_t> &offsets = img.offsets;
+    const std::size_t at_records = img.at_records, at_paired = img.at_paired, at_records64 = img.at_records64,
+                      at_groups = img.at_groups;
+    const std::size_t total = img.bytes.size();
     auto &v = dp->view;
     v.source_size = p.source_size;
     v.destination_size = p.destination_size;
@@ -231,8 +257,70 @@ std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const
         xv.backward = reinterpret_cast<const float *>(base + offsets[at_records64 + 1]);
     }
     dp->bytes = total;
+}
+
+std::shared_ptr<DevicePlan> upload_plan(const AxisPlan &p, std::shared_ptr<const AxisPlan> keep) {
+    if (!p.valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
+    const PlanImage img = plan_image(p);
+    auto dp = std::make_shared<DevicePlan>();
+    dp->memory.reserve(img.bytes.size());
+    cuda_check(cudaMemcpy(dp->memory.data(), img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice),
+               "uploading plan");
+    finish_plan(dp.get(), p, img, dp->memory.data());
     dp->keep = std::move(keep);
     return dp;
+}
+
+// Many plans: images packed on host threads, one device allocation shared by
+// the plans (held until the last of them is released) and one copy.
+std::vector<std::shared_ptr<DevicePlan>> upload_plans(const std::vector<std::shared_ptr<const AxisPlan>> &plans) {
+    const std::size_t count = plans.size();
+    std::vector<PlanImage> images(count);
+    std::vector<std::string> errors(count);
+    std::atomic<std::size_t> next{0};
+    auto worker = [&] {
+        for (std::size_t i = next++; i < count; i = next++) {
+            try {
+                if (!plans[i] || !plans[i]->valid()) throw std::invalid_argument("cannot prepare an invalid axis plan");
+                images[i] = plan_image(*plans[i]);
+            } catch (const std::exception &e) {
+                errors[i] = e.what();
+            }
+        }
+    };
+    const unsigned n = std::max(1U, std::min<unsigned>(std::thread::hardware_concurrency(),
+                                                       static_cast<unsigned>(std::max<std::size_t>(count, 1))));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < n; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto &t : pool) t.join();
+    for (const auto &e : errors)
+        if (!e.empty()) throw std::invalid_argument(e);
+    std::vector<std::size_t> at(count);
+    std::size_t total = 0;
+    for (std::size_t i = 0; i < count; ++i) {
+        at[i] = total;
+        total += align_up(std::max<std::size_t>(images[i].bytes.size(), 1));
+    }
+    std::vector<std::shared_ptr<DevicePlan>> out;
+    if (count == 0) return out;
+    auto arena = std::make_shared<DeviceBuffer>();
+    arena->reserve(total);
+    {
+        std::vector<char> host(total, 0);
+        for (std::size_t i = 0; i < count; ++i)
+            std::memcpy(host.data() + at[i], images[i].bytes.data(), images[i].bytes.size());
+        cuda_check(cudaMemcpy(arena->data(), host.data(), total, cudaMemcpyHostToDevice), "uploading plans");
+    }
+    out.reserve(count);
+    for (std::size_t i = 0; i < count; ++i) {
+        auto dp = std::make_shared<DevicePlan>();
+        finish_plan(dp.get(), *plans[i], images[i], arena->data() + at[i]);
+        dp->arena = arena;
+        dp->keep = plans[i];
+        out.push_back(std::move(dp));
+    }
+    return out;
 }
 
 // Per-stream scratch: intermediate, forward scratch, staged host frames, job
@@ -1286,6 +1374,32 @@ void Executor::prepare(std::shared_ptr<const AxisPlan> plan) {
     impl_->stats.plan_uploads += 1;
     impl_->stats.device_plan_bytes += dp->bytes;
     impl_->plans.emplace(plan.get(), std::move(dp));
+}
+
+void Executor::prepare_many(const std::vector<std::shared_ptr<const AxisPlan>> &plans) {
+    std::vector<std::shared_ptr<const AxisPlan>> fresh;
+    {
+        std::scoped_lock lock(impl_->mutex);
+        for (const auto &p : plans) {
+            if (!p) throw std::invalid_argument("cannot prepare a null plan");
+            if (impl_->plans.count(p.get())) continue;
+            if (impl_->sealed) throw std::logic_error("executor is sealed; prepare plans before seal()");
+            fresh.push_back(p);
+        }
+    }
+    std::sort(fresh.begin(), fresh.end());
+    fresh.erase(std::unique(fresh.begin(), fresh.end()), fresh.end());
+    if (fresh.empty()) return;
+    DeviceGuard guard(impl_->device);
+    auto uploaded = upload_plans(fresh);
+    std::scoped_lock lock(impl_->mutex);
+    for (auto &dp : uploaded) {
+        if (impl_->plans.count(dp->keep.get())) continue;
+        impl_->stats.plan_uploads += 1;
+        impl_->stats.device_plan_bytes += dp->bytes;
+        const AxisPlan *key = dp->keep.get();
+        impl_->plans.emplace(key, std::move(dp));
+    }
 }
 
 void Executor::seal() {

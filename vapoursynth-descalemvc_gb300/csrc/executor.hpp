@@ -150,6 +150,9 @@ public:
     // Uploads the plan's coefficients once; later calls with the same plan
     // object reuse them (keyed by identity, kept alive by the executor).
     void prepare(std::shared_ptr<const AxisPlan> plan);
+    // Prepares many plans at once: their device images are packed on host
+    // threads and uploaded in one allocation with one copy.
+    void prepare_many(const std::vector<std::shared_ptr<const AxisPlan>> &plans);
     void seal();
 
     // Synchronous host-frame calls (reference Executor contract).

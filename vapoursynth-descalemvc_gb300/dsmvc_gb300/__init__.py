@@ -167,6 +167,7 @@ SIGNATURES = {
     "dsmvc_gb_executor_create": ([C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_executor_destroy": ([C.c_void_p], None),
     "dsmvc_gb_prepare": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_prepare_many": ([C.c_void_p, C.POINTER(C.c_void_p), C.c_int32], C.c_int),
     "dsmvc_gb_seal": ([C.c_void_p], C.c_int),
     "dsmvc_gb_executor_get_stats": ([C.c_void_p, C.POINTER(ExecutorStatsC)], C.c_int),
     "dsmvc_gb_inverse_rows": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
@@ -466,6 +467,13 @@ class Executor:
     def prepare(self, plan: AxisPlan) -> None:
         _check(lib().dsmvc_gb_prepare(self._h, plan.handle))
         self._keep.append(plan)
+
+    def prepare_many(self, plans: Sequence[AxisPlan]) -> None:
+        """dsmvc_gb_prepare_many: many plans packed on host threads and
+        uploaded in one allocation."""
+        arr = (C.c_void_p * len(plans))(*[p.handle.value for p in plans])
+        _check(lib().dsmvc_gb_prepare_many(self._h, arr, len(plans)))
+        self._keep.extend(plans)
 
     def seal(self) -> None:
         _check(lib().dsmvc_gb_seal(self._h))
