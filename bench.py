@@ -41,7 +41,7 @@ METRIC = "descale Mpix/s (source pixels, Delanczos YUV420P16 1920x1080->1440x810
 # dram__bytes_write.sum of the rows and columns pass from one ncu capture of
 # a 24-frame cut of this workload, divided by 24 (traffic grows with the
 # frame count).
-DRAM_BYTES_PER_FRAME = 619.6e6 / 24
+DRAM_BYTES_PER_FRAME = 619.8e6 / 24
 TRAFFIC_SOURCE = ("ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, both passes) of a "
                   "24-frame cut of this workload, scaled to the step's frames")
 
