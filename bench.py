@@ -476,6 +476,7 @@ def run_sweep(args, rank, world):
                  "sweep_setup_s": t_prepare, "seconds": t_cold},
         "sweep": {"waves": info["waves"], "device_bytes": info["device_bytes"],
                   "tune_ms": info["tune_milliseconds"], "segment_rows": info["segment_rows"],
+                  "vectors_per_warp": info["vectors_per_warp"],
                   "detected": {"kernel": cands[best][0], "width": cands[best][1],
                                "height": cands[best][2], "score": float(scores[best]),
                                "dip": dips[best]},

@@ -421,6 +421,7 @@ typedef struct dsmvc_gb_sweep_info {
     double tune_milliseconds;
     int32_t segment_rows;
     int32_t tuned_groups;
+    int32_t vectors_per_warp;     /* right-hand sides per warp the tuning chose: 32 or 64 */
 } dsmvc_gb_sweep_info;
 int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor,
                           const dsmvc_gb_plan *const *horizontal,

@@ -97,6 +97,7 @@ def test_sweep_is_independent_of_launch_shape(gb, whole_executor, setup):
     tuned, info = _scores(gb, executor, dframe, pairs, autotune=True, graph=True)
     assert np.array_equal(base, tuned)
     assert info["tuned_groups"] >= 1 and info["segment_rows"] in (16, 32, 64, 128, 256)
+    assert info["vectors_per_warp"] in (32, 64)
     waved, winfo = _scores(gb, executor, dframe, pairs, memory_budget=1 << 20, autotune=False)
     assert winfo["waves"] > 1
     assert np.array_equal(base, waved)

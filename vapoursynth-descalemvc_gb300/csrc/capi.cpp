@@ -689,6 +689,7 @@ int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *ou
         out->tune_milliseconds = i.tune_milliseconds;
         out->segment_rows = i.segment_rows;
         out->tuned_groups = static_cast<int32_t>(i.tuning.size());
+        out->vectors_per_warp = i.vectors_per_warp;
     });
 }
 

@@ -603,7 +603,8 @@ struct Executor::Impl {
         std::size_t tasks = 0;
     };
     void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                 const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr);
+                 const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr,
+                 int vectors_per_warp = 0);
     void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
     void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch = nullptr,
                  std::size_t scratch_capacity = 0);
@@ -747,7 +748,9 @@ std::vector<Item> segment_items(const std::vector<Item> &items, int vectors_per_
 } // namespace
 
 void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                             const std::function<char *(std::size_t)> &scratch, const Tuning *tuning) {
+                             const std::function<char *(std::size_t)> &scratch, const Tuning *tuning,
+                             int vectors_per_warp) {
+    const bool paired = vectors_per_warp ? vectors_per_warp == 64 : allow_paired;
     auto &temporaries = out.temporaries;
     // Per task: which kernels run each pass, and the scratch they need.
     struct Route {
@@ -811,7 +814,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 if (!allow_stream) return 0;
                 const bool delayed = dp.stream && dp.stream_t;
                 if (dp.stream_x && (prefer_exact || !delayed)) return 5;
-                if (delayed) return allow_paired && dp.stream_p ? 4 : 3;
+                if (delayed) return paired && dp.stream_p ? 4 : 3;
                 return 0;
             };
             r.h_kind = pass_kind(*r.h);
@@ -1160,8 +1163,14 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         const bool by_warp = key.kind >= 3 && key.kind <= 6;
         const int warps_per_cta = per_block / 32;
         const int vectors_per_warp = key.kind == 4 ? 64 : 32;
+        // Jobs of one plan stay together (they share record copies); plans
+        // with the longest vectors come first, so that the CTAs that take
+        // longest start in the first wave and the launch's tail is short
+        // (longest-first list scheduling).
         if (by_warp)
             std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) {
+                const int na = a.stream.plan.destination_size, nb = b.stream.plan.destination_size;
+                if (na != nb) return na > nb;
                 return a.stream.plan.forward < b.stream.plan.forward;
             });
         if (key.kind == 3) items = segment_items(items, vectors_per_warp, segment_mode, warp_slots);
@@ -1874,9 +1883,11 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
 
 std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks,
                                                        const BatchTuning *tuning, void *scratch,
-                                                       std::size_t scratch_capacity) {
+                                                       std::size_t scratch_capacity, int vectors_per_warp) {
     DeviceGuard guard(impl_->device);
     validate_tasks(tasks);
+    if (vectors_per_warp != 0 && vectors_per_warp != 32 && vectors_per_warp != 64)
+        throw std::invalid_argument("vectors per warp must be 0, 32 or 64");
     for (const auto &[key, threads] : tuning ? *tuning : BatchTuning{}) {
         const int kind = key[1];
         const int most = kind >= 3 && kind <= 6 ? 256 : 128;
@@ -1895,7 +1906,7 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
         }
         b->scratch.reserve(bytes);
         return b->scratch.data();
-    }, &t);
+    }, &t, vectors_per_warp);
     const auto &table = b->compiled.table;
     b->table.reserve(std::max<std::size_t>(table.size(), 1));
     if (!table.empty())

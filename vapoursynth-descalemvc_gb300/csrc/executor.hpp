@@ -192,10 +192,15 @@ public:
     // `scratch` the batch's intermediate planes live in that caller-owned
     // device buffer of `scratch_capacity` bytes (batches launched one after
     // another may share it); otherwise the batch allocates its own.
+    // `vectors_per_warp` picks the transposing Float32 kernels' right-hand
+    // sides per warp: 32 (one vector a lane), 64 (two a lane, the paired
+    // kernels, where a plan admits them; same results bit for bit), or 0
+    // for the executor's default (DSMVC_GB_PAIRED).
     [[nodiscard]] std::unique_ptr<PreparedBatch> prepare_batch(const std::vector<PlaneTask> &tasks,
                                                              const BatchTuning *tuning = nullptr,
                                                              void *scratch = nullptr,
-                                                             std::size_t scratch_capacity = 0);
+                                                             std::size_t scratch_capacity = 0,
+                                                             int vectors_per_warp = 0);
     // Upper bound of the scratch bytes prepare_batch needs for `tasks`.
     [[nodiscard]] static std::size_t batch_scratch_bound(const std::vector<PlaneTask> &tasks);
 

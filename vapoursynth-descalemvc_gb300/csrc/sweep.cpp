@@ -106,6 +106,7 @@ struct Sweep::Impl {
     std::map<const AxisPlan *, dev::ForwardCsr> forward;
     int segment_rows = 32;
     int best_segment = 32;
+    int vectors_per_warp = 0;   // 0: the executor's default; 32 / 64 once tuned
     BatchTuning tuning;
     double tune_ms = 0.0;
     cudaGraph_t graph = nullptr;
@@ -308,13 +309,29 @@ struct Sweep::Impl {
         return ms / static_cast<float>(reps);
     }
 
-    // Times every launch group of the first wave at each candidate CTA size
-    // and the scoring column pass at each row segment; keeps the fastest.
+    // Times the first wave's descale with one and with two right-hand sides
+    // a lane (32 or 64 vectors a warp), then every launch group of it at
+    // each candidate CTA size, and the scoring column pass at each row
+    // segment; keeps the fastest of each.  Scores do not depend on the
+    // choices: every kernel variant gives each output bit for bit.
     void autotune() {
         const auto t0 = std::chrono::steady_clock::now();
         Wave &w = waves.front();
+        {
+            float best_ms = 0.0F;
+            for (const int vpw : {32, 64}) {
+                auto batch = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity, vpw);
+                const float ms = time_ms([&] { batch->launch(stream); }, 3);
+                check(cudaStreamSynchronize(stream), "synchronizing");
+                if (vpw == 32 || ms < best_ms) {
+                    best_ms = ms;
+                    vectors_per_warp = vpw;
+                }
+            }
+        }
         std::map<std::array<int, 6>, std::pair<float, int>> best;
-        const auto keys = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity)->groups();
+        const auto keys = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity,
+                                                  vectors_per_warp)->groups();
         // 32-thread CTAs never win on these kernels (one warp per record copy).
         for (const int threads : {64, 128, 256}) {
             BatchTuning all;
@@ -323,7 +340,8 @@ struct Sweep::Impl {
                 if (g.kind != 2 && threads <= most) all[g.key] = threads;
             }
             if (all.empty()) continue;
-            auto batch = executor->prepare_batch(w.tasks, &all, scratch_mem.data(), scratch_capacity);
+            auto batch = executor->prepare_batch(w.tasks, &all, scratch_mem.data(), scratch_capacity,
+                                                 vectors_per_warp);
             const auto groups = batch->groups();
             for (std::size_t gi = 0; gi < groups.size(); ++gi) {
                 if (!all.count(groups[gi].key)) continue;
@@ -367,7 +385,8 @@ struct Sweep::Impl {
             if (span_rows(w) > kMaxSpanRows) throw std::length_error("candidate too far from its source size to score");
         }
         for (auto &w : waves)
-            w.batch = executor->prepare_batch(w.tasks, &tuning, scratch_mem.data(), scratch_capacity);
+            w.batch = executor->prepare_batch(w.tasks, &tuning, scratch_mem.data(), scratch_capacity,
+                                              vectors_per_warp);
         upload_jobs(plain_job_mem, score_jobs(segment_rows, true));
         upload_jobs(job_mem, score_jobs(segment_rows, false));
         if (options.graph) {
@@ -501,6 +520,7 @@ SweepInfo Sweep::info() const {
     for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 2;
     i.tune_milliseconds = m.tune_ms;
     i.segment_rows = m.segment_rows;
+    i.vectors_per_warp = m.vectors_per_warp ? m.vectors_per_warp : 32;
     i.tuning = m.tuning;
     return i;
 }

@@ -40,6 +40,7 @@ struct SweepInfo {
     std::size_t kernel_launches = 0;  // per run()
     double tune_milliseconds = 0.0;
     int segment_rows = 0;
+    int vectors_per_warp = 32;        // chosen right-hand sides per warp (32 or 64)
     BatchTuning tuning;               // chosen CTA sizes per launch group
 };
 

@@ -115,7 +115,8 @@ class SweepOptionsC(C.Structure):
 class SweepInfoC(C.Structure):
     _fields_ = [("candidates", C.c_int32), ("waves", C.c_int32), ("device_bytes", C.c_int64),
                 ("kernel_launches", C.c_int64), ("tune_milliseconds", C.c_double),
-                ("segment_rows", C.c_int32), ("tuned_groups", C.c_int32)]
+                ("segment_rows", C.c_int32), ("tuned_groups", C.c_int32),
+                ("vectors_per_warp", C.c_int32)]
 
 
 class ServerOptionsC(C.Structure):
