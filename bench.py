@@ -14,8 +14,11 @@ so no flush is needed between steps.
 Prints one JSON line (rank 0).  `value` is Mpix/s of source pixels summed
 over planes with inputs resident in HBM; `e2e` is the same metric through
 the synchronous host-frame C-ABI calls (pinned host planes, copies inside
-the timed region); `roofline` is measured with CUDA events around every
-kernel launch of the timed steps.
+the timed region); `roofline` divides the algorithmic bytes of a step (the
+sum over its kernel launches, each counted by the executor) by the step's
+CUDA-event time: the prepared batch runs as two parts on two streams whose
+kernels overlap, so the per-kernel event times (also reported, as shares)
+add up to more than the step.
 """
 from __future__ import annotations
 
@@ -1038,7 +1041,6 @@ def main():
     torch.cuda.synchronize()
     batch.check(sid)
     launches0 = ex.stats()["launches"]
-    ex.profile(True)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -1053,9 +1055,17 @@ def main():
     torch.cuda.synchronize()
     batch.check(sid)
     elapsed_ms = start.elapsed_time(stop)
+    launches = ex.stats()["launches"] - launches0
+    # Per-kernel event times and algorithmic bytes, from the same steps run
+    # again outside the timed region (events between kernels stay out of the
+    # timed number).
+    ex.profile(True)
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            batch.launch(sid)
+    torch.cuda.synchronize()
     ktimes = ex.kernel_times()
     ex.profile(False)
-    launches = ex.stats()["launches"] - launches0
     elapsed_ms = max_over_ranks(elapsed_ms, dist, "cuda")
     pix_step = pixels_per_frame() * FRAMES
     value = whole_job_rate(pix_step, world, args.steps, elapsed_ms)
@@ -1118,7 +1128,8 @@ def main():
     total_ms = sum(k["milliseconds"] for k in ktimes)
     total_bytes = sum(k["bytes"] for k in ktimes)
     dominant = max(ktimes, key=lambda k: k["milliseconds"]) if ktimes else None
-    achieved = total_bytes / (total_ms / 1e3) / 1e9 if total_ms else 0.0
+    step_bytes = total_bytes / max(1, args.steps)
+    achieved = step_bytes / (elapsed_ms / args.steps / 1e3) / 1e9 if elapsed_ms else 0.0
 
     if rank != 0:
         if dist is not None:
@@ -1150,9 +1161,12 @@ def main():
                      "frac": achieved / hbm,
                      "traffic": DRAM_BYTES_PER_FRAME * FRAMES,
                      "traffic_source": TRAFFIC_SOURCE,
-                     "algorithmic_bytes": total_bytes / max(1, args.steps),
+                     "algorithmic_bytes": step_bytes,
                      "peak_source": peak_kind,
-                     "kernel": "2D descale (horizontal + vertical passes per step)",
+                     "kernel": "2D descale step (horizontal + vertical passes of 192 planes, "
+                               "two overlapping parts); achieved = algorithmic bytes / step time",
+                     "batch_parts": batch.info()["parts"],
+                     "kernel_ms_sum_per_step": total_ms / max(1, args.steps),
                      "kernels": [dict(k, share=k["milliseconds"] / total_ms) for k in ktimes],
                      "dominant": dominant["name"] if dominant else None},
         "cpu_baseline": cpu,

@@ -361,6 +361,16 @@ int dsmvc_gb_batch_launch(dsmvc_gb_batch *batch, void *stream);
 int dsmvc_gb_batch_check(dsmvc_gb_batch *batch, void *stream);
 int dsmvc_gb_batch_info(const dsmvc_gb_batch *batch, int64_t *kernel_launches,
                         int64_t *scratch_bytes, int64_t *table_bytes);
+/* A batch whose tasks run in `parts` parts: 1 as one sequence of kernels;
+ * 2 split where the source pixels are halved, the halves launched on
+ * `stream` and on a stream of the batch forked from it and joined back to it
+ * (stream-ordered, capturable), so that one half's second pass overlaps the
+ * other's first; 0 (what dsmvc_gb_batch_create does) chooses 2 for 8 tasks
+ * or more.  dsmvc_gb_batch_parts reports the count. */
+int dsmvc_gb_batch_create_parts(dsmvc_gb_executor *executor,
+                                const dsmvc_gb_plane_task *tasks, int32_t count,
+                                int32_t parts, dsmvc_gb_batch **out);
+int dsmvc_gb_batch_parts(const dsmvc_gb_batch *batch, int32_t *parts);
 void dsmvc_gb_batch_destroy(dsmvc_gb_batch *batch);
 
 /* Allocation-free 2D descale.  No counterpart in the reference.  For callers

@@ -241,3 +241,45 @@ def test_pipelined_planes_direct_host_access(gb, whole_executor):
     for (_h, _v, _x, out, _c), w in zip(planes, want):
         assert np.array_equal(out, w)
     direct.close()
+
+
+def test_two_part_batch_matches_one_part(gb, whole_executor):
+    """A batch of eight or more tasks that owns its scratch is split into two
+    parts launched on a forked stream; on whole vectors (results independent
+    of launch composition) both splits write the same bytes, directly and
+    replayed from a CUDA graph."""
+    torch = pytest.importorskip("torch")
+    tasks, _inputs, outputs, _meta = _tasks(gb, whole_executor, torch, copies=3)
+    assert len(tasks) >= 8
+    sid = torch.cuda.current_stream().cuda_stream
+    one = whole_executor.prepare_batch(tasks, parts=1)
+    assert one.info()["parts"] == 1
+    one.launch(sid)
+    one.check(sid)
+    want = _snapshot(outputs)
+    auto = whole_executor.prepare_batch(tasks)
+    two = whole_executor.prepare_batch(tasks, parts=2)
+    assert auto.info()["parts"] == 2 and two.info()["parts"] == 2
+    assert two.info()["kernel_launches"] >= one.info()["kernel_launches"]
+    for batch in (auto, two):
+        for y in outputs:
+            y.zero_()
+        batch.launch(sid)
+        batch.check(sid)
+        for got, exp in zip(_snapshot(outputs), want):
+            assert np.array_equal(got, exp)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        two.launch(side.cuda_stream)
+    for _ in range(2):
+        for y in outputs:
+            y.zero_()
+        torch.cuda.synchronize()
+        graph.replay()
+        torch.cuda.synchronize()
+        for got, exp in zip(_snapshot(outputs), want):
+            assert np.array_equal(got, exp)
+    two.check(sid)

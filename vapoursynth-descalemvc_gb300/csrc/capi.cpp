@@ -545,6 +545,24 @@ int dsmvc_gb_batch_create(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task
     });
 }
 
+int dsmvc_gb_batch_create_parts(dsmvc_gb_executor *executor, const dsmvc_gb_plane_task *tasks, int32_t count,
+                                int32_t parts, dsmvc_gb_batch **out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output pointer is null");
+        *out = nullptr;
+        auto b = std::make_unique<dsmvc_gb_batch>();
+        b->batch = exec_of(executor).prepare_batch(task_list(tasks, count), nullptr, nullptr, 0, 0, parts);
+        *out = b.release();
+    });
+}
+
+int dsmvc_gb_batch_parts(const dsmvc_gb_batch *batch, int32_t *parts) {
+    return guarded([&] {
+        if (!batch || !parts) throw std::invalid_argument("batch or output is null");
+        *parts = static_cast<int32_t>(batch->batch->parts());
+    });
+}
+
 int dsmvc_gb_batch_launch(dsmvc_gb_batch *batch, void *stream) {
     return guarded([&] {
         if (!batch) throw std::invalid_argument("batch is null");

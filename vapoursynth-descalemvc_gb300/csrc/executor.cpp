@@ -46,6 +46,9 @@ void cuda_check(int e, const char *what) { cuda_check(static_cast<cudaError_t>(e
 
 constexpr std::size_t kAlign = 256;
 constexpr int kSeqThreads = 128;   // threads per block of the sequential kernels
+// Prepared batches of at least this many tasks (and their own scratch) run
+// as two parts on two streams.
+constexpr std::size_t kSplitBatchTasks = 8;
 std::size_t align_up(std::size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 std::size_t sample_bytes(dev::Sample s) {
@@ -1787,14 +1790,32 @@ void Executor::run_batch(const std::vector<PlaneTask> &tasks, void *stream, bool
 
 struct PreparedBatch::Impl {
     Executor::Impl *owner = nullptr;
-    Executor::Impl::Compiled compiled;
-    DeviceBuffer scratch;                 // unused with caller-owned scratch
-    DeviceBuffer table;
+    // The tasks in one part, or two (each half of the work) whose launches
+    // run on two streams forked from the caller's and joined back to it.
+    struct Part {
+        Executor::Impl::Compiled compiled;
+        DeviceBuffer scratch;             // unused with caller-owned scratch
+        DeviceBuffer table;
+    };
+    std::vector<std::unique_ptr<Part>> parts;
+    cudaStream_t side = nullptr;           // the second part's stream
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::uint32_t *status = nullptr;       // device
     std::uint32_t *status_host = nullptr;  // pinned
     ~Impl() {
+        if (join) cudaEventDestroy(join);
+        if (fork) cudaEventDestroy(fork);
+        if (side) cudaStreamDestroy(side);
         if (status) cudaFree(status);
         if (status_host) cudaFreeHost(status_host);
+    }
+    // Launch group `index` counted across the parts.
+    std::pair<const Part *, std::size_t> group(std::size_t index) const {
+        for (const auto &pt : parts) {
+            if (index < pt->compiled.launches.size()) return {pt.get(), index};
+            index -= pt->compiled.launches.size();
+        }
+        throw std::out_of_range("launch group index");
     }
 };
 
@@ -1810,21 +1831,34 @@ PreparedBatch::~PreparedBatch() {
 
 void PreparedBatch::launch(void *stream) {
     DeviceGuard guard(impl_->owner->device);
-    impl_->owner->launch(impl_->compiled, impl_->table.data(), static_cast<cudaStream_t>(stream),
-                         impl_->status);
+    auto s = static_cast<cudaStream_t>(stream);
+    auto &m = *impl_;
+    if (m.parts.size() == 1) {
+        m.owner->launch(m.parts[0]->compiled, m.parts[0]->table.data(), s, m.status);
+        return;
+    }
+    // Fork: the second part's stream waits for the caller's; join: the
+    // caller's waits for it.  Both are stream-ordered (capturable).
+    cuda_check(cudaEventRecord(m.fork, s), "recording fork");
+    cuda_check(cudaStreamWaitEvent(m.side, m.fork, 0), "forking");
+    m.owner->launch(m.parts[0]->compiled, m.parts[0]->table.data(), s, m.status);
+    m.owner->launch(m.parts[1]->compiled, m.parts[1]->table.data(), m.side, m.status);
+    cuda_check(cudaEventRecord(m.join, m.side), "recording join");
+    cuda_check(cudaStreamWaitEvent(s, m.join, 0), "joining");
 }
 
 void PreparedBatch::launch_group(std::size_t index, void *stream) {
     DeviceGuard guard(impl_->owner->device);
-    if (index >= impl_->compiled.launches.size()) throw std::out_of_range("launch group index");
+    const auto [part, i] = impl_->group(index);
     Executor::Impl::Compiled one;
-    one.launches.push_back(impl_->compiled.launches[index]);
-    impl_->owner->launch(one, impl_->table.data(), static_cast<cudaStream_t>(stream), impl_->status);
+    one.launches.push_back(part->compiled.launches[i]);
+    impl_->owner->launch(one, part->table.data(), static_cast<cudaStream_t>(stream), impl_->status);
 }
 
 std::vector<BatchGroup> PreparedBatch::groups() const {
     std::vector<BatchGroup> out;
-    for (const auto &l : impl_->compiled.launches) {
+    for (const auto &pt : impl_->parts)
+    for (const auto &l : pt->compiled.launches) {
         BatchGroup g;
         g.key = {l.pass, l.kind, l.hb, static_cast<int>(l.in), static_cast<int>(l.out), l.variant};
         g.kind = l.kind;
@@ -1852,9 +1886,22 @@ void PreparedBatch::check_status(void *stream) {
     }
 }
 
-std::size_t PreparedBatch::kernel_launches() const { return impl_->compiled.launches.size(); }
-std::size_t PreparedBatch::scratch_bytes() const { return impl_->compiled.scratch_bytes; }
-std::size_t PreparedBatch::table_bytes() const { return impl_->compiled.table.size(); }
+std::size_t PreparedBatch::kernel_launches() const {
+    std::size_t n = 0;
+    for (const auto &pt : impl_->parts) n += pt->compiled.launches.size();
+    return n;
+}
+std::size_t PreparedBatch::scratch_bytes() const {
+    std::size_t n = 0;
+    for (const auto &pt : impl_->parts) n += pt->compiled.scratch_bytes;
+    return n;
+}
+std::size_t PreparedBatch::table_bytes() const {
+    std::size_t n = 0;
+    for (const auto &pt : impl_->parts) n += pt->compiled.table.size();
+    return n;
+}
+std::size_t PreparedBatch::parts() const { return impl_->parts.size(); }
 
 std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
     // Per task: the intermediate plane (destinations of the first pass x
@@ -1883,7 +1930,8 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
 
 std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks,
                                                        const BatchTuning *tuning, void *scratch,
-                                                       std::size_t scratch_capacity, int vectors_per_warp) {
+                                                       std::size_t scratch_capacity, int vectors_per_warp,
+                                                       int parts) {
     DeviceGuard guard(impl_->device);
     validate_tasks(tasks);
     if (vectors_per_warp != 0 && vectors_per_warp != 32 && vectors_per_warp != 64)
@@ -1899,19 +1947,55 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
         for (const auto &[k, v] : *tuning) t[{k[0], k[1], k[2], k[3], k[4], k[5]}] = v;
     auto b = std::make_unique<PreparedBatch::Impl>();
     b->owner = impl_.get();
-    impl_->compile(tasks, b->compiled, [&](std::size_t bytes) {
-        if (scratch) {
-            if (bytes > scratch_capacity) throw std::length_error("batch scratch exceeds the caller's buffer");
-            return static_cast<char *>(scratch);
+    // Two parts (launches overlapping on two streams: one part's second pass
+    // runs beside the other's first) for batches of many tasks that own
+    // their scratch; split where the source pixels are halved.
+    int n_parts = parts;
+    if (n_parts == 0) n_parts = !scratch && tasks.size() >= kSplitBatchTasks ? 2 : 1;
+    if (n_parts != 1 && n_parts != 2) throw std::invalid_argument("a prepared batch has 1 or 2 parts");
+    if (n_parts == 2 && (scratch || tasks.size() < 2))
+        throw std::invalid_argument("two batch parts need two tasks and batch-owned scratch");
+    std::size_t cut = tasks.size();
+    if (n_parts == 2) {
+        auto work = [](const PlaneTask &t) {
+            const auto rows = t.vertical ? t.vertical->source_size : t.vectors;
+            const auto cols = t.horizontal ? t.horizontal->source_size : t.vectors;
+            return static_cast<double>(rows) * static_cast<double>(cols);
+        };
+        double total = 0.0, acc = 0.0;
+        for (const auto &t : tasks) total += work(t);
+        cut = 1;
+        for (std::size_t i = 0; i + 1 < tasks.size(); ++i) {
+            acc += work(tasks[i]);
+            cut = i + 1;
+            if (acc >= total / 2) break;
         }
-        b->scratch.reserve(bytes);
-        return b->scratch.data();
-    }, &t, vectors_per_warp);
-    const auto &table = b->compiled.table;
-    b->table.reserve(std::max<std::size_t>(table.size(), 1));
-    if (!table.empty())
-        cuda_check(cudaMemcpy(b->table.data(), table.data(), table.size(), cudaMemcpyHostToDevice),
-                   "uploading job table");
+    }
+    for (int k = 0; k < n_parts; ++k) {
+        b->parts.push_back(std::make_unique<PreparedBatch::Impl::Part>());
+        auto &pt = *b->parts.back();
+        const std::vector<PlaneTask> part_tasks = n_parts == 1 ? tasks
+            : k == 0 ? std::vector<PlaneTask>(tasks.begin(), tasks.begin() + static_cast<std::ptrdiff_t>(cut))
+                     : std::vector<PlaneTask>(tasks.begin() + static_cast<std::ptrdiff_t>(cut), tasks.end());
+        impl_->compile(part_tasks, pt.compiled, [&](std::size_t bytes) {
+            if (scratch) {
+                if (bytes > scratch_capacity) throw std::length_error("batch scratch exceeds the caller's buffer");
+                return static_cast<char *>(scratch);
+            }
+            pt.scratch.reserve(bytes);
+            return pt.scratch.data();
+        }, &t, vectors_per_warp);
+        const auto &table = pt.compiled.table;
+        pt.table.reserve(std::max<std::size_t>(table.size(), 1));
+        if (!table.empty())
+            cuda_check(cudaMemcpy(pt.table.data(), table.data(), table.size(), cudaMemcpyHostToDevice),
+                       "uploading job table");
+    }
+    if (n_parts == 2) {
+        cuda_check(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "creating stream");
+        cuda_check(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "creating event");
+        cuda_check(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "creating event");
+    }
     cuda_check(cudaMalloc(&b->status, sizeof(std::uint32_t)), "allocating status");
     cuda_check(cudaMallocHost(&b->status_host, sizeof(std::uint32_t)), "allocating status");
     cuda_check(cudaMemset(b->status, 0, sizeof(std::uint32_t)), "clearing status");

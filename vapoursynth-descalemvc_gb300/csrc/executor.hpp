@@ -133,6 +133,8 @@ public:
     [[nodiscard]] std::size_t kernel_launches() const;
     [[nodiscard]] std::size_t scratch_bytes() const;
     [[nodiscard]] std::size_t table_bytes() const;
+    // 1, or 2 when the tasks run as two overlapping parts.
+    [[nodiscard]] std::size_t parts() const;
 
 private:
     std::unique_ptr<Impl> impl_;
@@ -195,12 +197,19 @@ public:
     // `vectors_per_warp` picks the transposing Float32 kernels' right-hand
     // sides per warp: 32 (one vector a lane), 64 (two a lane, the paired
     // kernels, where a plan admits them; same results bit for bit), or 0
-    // for the executor's default (DSMVC_GB_PAIRED).
+    // for the executor's default (DSMVC_GB_PAIRED).  `parts`: 1 launches
+    // every task in one sequence of kernels; 2 splits the tasks where the
+    // source pixels are halved and launches the halves on the caller's
+    // stream and a second one forked from it and joined back, so that one
+    // half's second pass overlaps the other's first (measured 14 % faster on
+    // 32 4K planes); 0 chooses 2 for batches of 8 tasks or more that own
+    // their scratch.  Results do not depend on the parts beyond what
+    // segment splits already allow (DSMVC_GB_SEGMENTS=1: none).
     [[nodiscard]] std::unique_ptr<PreparedBatch> prepare_batch(const std::vector<PlaneTask> &tasks,
                                                              const BatchTuning *tuning = nullptr,
                                                              void *scratch = nullptr,
                                                              std::size_t scratch_capacity = 0,
-                                                             int vectors_per_warp = 0);
+                                                             int vectors_per_warp = 0, int parts = 0);
     // Upper bound of the scratch bytes prepare_batch needs for `tasks`.
     [[nodiscard]] static std::size_t batch_scratch_bound(const std::vector<PlaneTask> &tasks);
 

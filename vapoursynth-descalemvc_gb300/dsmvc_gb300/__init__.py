@@ -190,6 +190,9 @@ SIGNATURES = {
                                C.POINTER(C.c_void_p)], C.c_int),
     "dsmvc_gb_batch_launch": ([C.c_void_p, C.c_void_p], C.c_int),
     "dsmvc_gb_batch_check": ([C.c_void_p, C.c_void_p], C.c_int),
+    "dsmvc_gb_batch_create_parts": ([C.c_void_p, C.POINTER(PlaneTaskC), C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_void_p)], C.c_int),
+    "dsmvc_gb_batch_parts": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
     "dsmvc_gb_batch_info": ([C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                              C.POINTER(C.c_int64)], C.c_int),
     "dsmvc_gb_batch_destroy": ([C.c_void_p], None),
@@ -541,10 +544,11 @@ class Executor:
         _check(lib().dsmvc_gb_run_batch(self._h, arr, len(tasks), C.c_void_p(stream or None),
                                         1 if synchronize else 0))
 
-    def prepare_batch(self, tasks: Sequence[PlaneTask]) -> "PreparedBatch":
+    def prepare_batch(self, tasks: Sequence[PlaneTask], parts: int = 0) -> "PreparedBatch":
         """Routes and uploads `tasks` once; PreparedBatch.launch() then
-        issues only the kernels (capturable into a CUDA graph)."""
-        return PreparedBatch(self, tasks)
+        issues only the kernels (capturable into a CUDA graph).  `parts`: 1
+        or 2 (overlapping halves on two streams), 0 = 2 for 8 tasks or more."""
+        return PreparedBatch(self, tasks, parts)
 
     def stream_check(self, stream: int = 0) -> None:
         _check(lib().dsmvc_gb_stream_check(self._h, C.c_void_p(stream or None)))
@@ -601,9 +605,10 @@ class PreparedBatch:
     """A task list packed once (dsmvc_gb_batch_create); keeps its executor
     and plans alive.  The task buffers must outlive it."""
 
-    def __init__(self, executor: Executor, tasks: Sequence[PlaneTask]):
+    def __init__(self, executor: Executor, tasks: Sequence[PlaneTask], parts: int = 0):
         h = C.c_void_p()
-        _check(lib().dsmvc_gb_batch_create(executor._h, _task_array(tasks), len(tasks), C.byref(h)))
+        _check(lib().dsmvc_gb_batch_create_parts(executor._h, _task_array(tasks), len(tasks), int(parts),
+                                                 C.byref(h)))
         self._h = h
         self._executor = executor
         executor._dependents.add(self)
@@ -618,7 +623,10 @@ class PreparedBatch:
     def info(self) -> dict:
         k, s, t = C.c_int64(), C.c_int64(), C.c_int64()
         _check(lib().dsmvc_gb_batch_info(self._h, C.byref(k), C.byref(s), C.byref(t)))
-        return {"kernel_launches": k.value, "scratch_bytes": s.value, "table_bytes": t.value}
+        parts = C.c_int32()
+        _check(lib().dsmvc_gb_batch_parts(self._h, C.byref(parts)))
+        return {"kernel_launches": k.value, "scratch_bytes": s.value, "table_bytes": t.value,
+                "parts": parts.value}
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value and _lib is not None:
