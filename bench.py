@@ -434,6 +434,25 @@ def run_sweep(args, rank, world):
     sweep.run_plain(sid)
     plain_scores = sweep.scores(sid)
     plain = len(cands) / (time.perf_counter() - t3)
+
+    # The same sweep with the scoring fused into the columns passes (the
+    # descaled planes stay on chip), timed alike.
+    sep = gb.Sweep(ex, pairs, dframe.data_ptr(), SWEEP_W, autotune=True, graph=True, fused_scoring=True)
+    for _ in range(args.warmup):
+        sep.run(sid)
+    torch.cuda.synchronize()
+    sep_steps = max(1, min(args.steps, 5))
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for _ in range(sep_steps):
+            sep.run(sid)
+        stop.record(stream)
+    stream.synchronize()
+    sep_ms = start.elapsed_time(stop) / sep_steps
+    sep_scores = sep.scores(sid)
+    sep_info = sep.info()
+    sep_stages = sep.profile(sid)
+    sep.close()
     # The native resolution shows as the sharpest dip of a kernel's score
     # against its neighbouring heights.  Heights at an exact integer ratio of
     # the source (1080 / 540 here) are left out: there a descale and its
@@ -451,9 +470,14 @@ def run_sweep(args, rank, world):
     base_idx = base_hits[0] if base_hits else None
 
     hbm, peak_kind = peaks()
-    out_bytes = sum(c[1] * c[2] * 4 for c in cands)
+    # Algorithmic bytes of a step: each candidate's Float32 intermediate
+    # (SWEEP_H x its width) written by the rows pass and read by the columns
+    # pass, its descaled plane written and read by the scoring, the plans'
+    # records and the frame.
+    mid_bytes = sum(2 * SWEEP_H * c[1] * 4 for c in cands)
+    out_bytes = sum(2 * c[1] * c[2] * 4 for c in cands)
     plan_bytes = sum(int(p.storage_bytes) for p in plans)
-    algo = out_bytes + plan_bytes + frame.nbytes
+    algo = mid_bytes + out_bytes + plan_bytes + frame.nbytes
     achieved = algo / (ms / 1e3) / 1e9
     if rank != 0:
         return
@@ -464,7 +488,7 @@ def run_sweep(args, rank, world):
         "config": {"workload": "C3 sweep: 1920x1080 GRAYS f32, heights 500..1000, "
                                "bicubic(0,0.5)/bilinear/lanczos3, mean-L1 score",
                    "candidates": len(cands), "hidden_base_height": base_h,
-                   "l2": "per-step outputs (6.2 GB) larger than L2; no flush",
+                   "l2": "per-step intermediates (17 GB) larger than L2; no flush",
                    "parallelism": "replicas"},
         "clocks": clocks.summary(),
         "e2e": {"value": e2e, "unit": "candidates/s", "h2d_bytes_per_step": frame.nbytes,
@@ -472,7 +496,12 @@ def run_sweep(args, rank, world):
         "gpu_launches": info["kernel_launches"] * args.steps,
         "plain_per_candidate": {"value": plain, "unit": "candidates/s",
                                 "speedup_batched": warm / plain,
-                                "scores_identical": bool(np.array_equal(plain_scores, scores))},
+                                "scores_identical": bool(np.array_equal(plain_scores, scores)),
+                                "max_rel_diff": float(np.max(np.abs(plain_scores - scores) / np.abs(scores)))},
+        "fused_scoring": {"value": len(cands) / (sep_ms / 1e3), "unit": "candidates/s", "ms_per_step": sep_ms,
+                          "fused_candidates": sep_info["fused_candidates"], "waves": sep_info["waves"],
+                          "device_bytes": sep_info["device_bytes"], "stages_ms": sep_stages,
+                          "max_rel_diff_vs_separate": float(np.max(np.abs(sep_scores - scores) / np.abs(scores)))},
         "cold": {"value": len(cands) / t_cold, "unit": "candidates/s", "planning_s": t_plan,
                  "planning": "host planner on all host threads",
                  "planning_device_s": t_plan_device, "plan_upload_s": t_upload,
@@ -480,6 +509,7 @@ def run_sweep(args, rank, world):
         "sweep": {"waves": info["waves"], "device_bytes": info["device_bytes"],
                   "tune_ms": info["tune_milliseconds"], "segment_rows": info["segment_rows"],
                   "vectors_per_warp": info["vectors_per_warp"],
+                  "fused_candidates": info["fused_candidates"],
                   "detected": {"kernel": cands[best][0], "width": cands[best][1],
                                "height": cands[best][2], "score": float(scores[best]),
                                "dip": dips[best]},
@@ -491,7 +521,7 @@ def run_sweep(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind,
                      "algorithmic_bytes": algo,
-                     "kernel": "whole sweep graph (descale passes + scoring)"},
+                     "kernel": "whole sweep graph (descale passes, scoring, score reductions)"},
     }
     return line
 

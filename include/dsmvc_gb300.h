@@ -409,6 +409,10 @@ int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal,
  * candidate (a horizontal and a vertical plan over the same source size) is
  * descaled from one device frame, re-upscaled with its plans' forward
  * operators and scored by the mean absolute error against the frame.  The
+ * scoring runs in a kernel of its own over each descaled plane or, with
+ * `fused_scoring`, inside each candidate's columns pass where the pass and
+ * the operators allow it (the descaled plane never reaches HBM, the sweep
+ * needs a fraction of the memory; `fused_candidates` counts them).  The
  * candidates run in waves within `memory_budget` bytes (0 = 32 GiB), one
  * prepared batch per wave, the whole sweep captured into one CUDA graph
  * (`graph`), with CTA sizes and the scoring row segment chosen by timing the
@@ -422,6 +426,8 @@ typedef struct dsmvc_gb_sweep_options {
     int64_t memory_budget;
     int32_t autotune;
     int32_t graph;
+    int32_t fused_scoring;        /* 1: score inside the columns pass where possible */
+    int32_t reserved;             /* 0 */
 } dsmvc_gb_sweep_options;
 typedef struct dsmvc_gb_sweep_info {
     int32_t candidates;
@@ -432,6 +438,7 @@ typedef struct dsmvc_gb_sweep_info {
     int32_t segment_rows;
     int32_t tuned_groups;
     int32_t vectors_per_warp;     /* right-hand sides per warp the tuning chose: 32 or 64 */
+    int32_t fused_candidates;     /* scored inside their columns pass */
 } dsmvc_gb_sweep_info;
 int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor,
                           const dsmvc_gb_plan *const *horizontal,

@@ -133,15 +133,25 @@ def test_sweep_full_frame_against_oracle(gb, executor):
     plans = gb.build_plans(reqs, threads=0)
     pairs = [(plans[2 * i], plans[2 * i + 1]) for i in range(len(cands))]
     dframe = torch.from_numpy(frame).cuda()
-    sweep = gb.Sweep(executor, pairs, dframe.data_ptr(), SWEEP_W, autotune=True, graph=True)
     sid = torch.cuda.current_stream().cuda_stream
-    sweep.run(sid)
-    got = sweep.scores(sid)
-    sweep.close()
-    assert len(got) == len(cands) == 63
+    results = {}
+    for fused in (False, True):
+        sweep = gb.Sweep(executor, pairs, dframe.data_ptr(), SWEEP_W, autotune=True, graph=True,
+                         fused_scoring=fused)
+        sweep.run(sid)
+        results[fused] = (sweep.scores(sid), sweep.info()["fused_candidates"])
+        sweep.close()
+    got, fused_count = results[False]
+    assert len(got) == len(cands) == 63 and fused_count == 0
+    # Fused scoring runs inside the columns pass of every candidate whose
+    # pass is chunk-delayed (all but the few whose windows the transposing
+    # ring cannot hold: 56 of the 63).
+    fgot, fused_count = results[True]
+    assert fused_count >= 56
     for i, cand in enumerate(cands):
         want = _oracle_score(frame, cand[3], cand[4])
         assert abs(got[i] - want) <= 2e-5 + 1e-3 * abs(want), (cand[:3], got[i], want)
+        assert abs(fgot[i] - want) <= 2e-5 + 1e-3 * abs(want), (cand[:3], fgot[i], want)
     # The hidden base height shows as the sharpest Debicubic dip.
     idx = [i for i, cand in enumerate(cands) if cand[0] == "bicubic"]
     dips = {cands[b][2]: got[b] / min(got[a], got[c]) for a, b, c in zip(idx, idx[1:], idx[2:])}

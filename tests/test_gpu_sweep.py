@@ -12,7 +12,10 @@ Bars:
     budget), and between the batched run and the one-candidate-at-a-time
     run; with segments the last two agree within 1e-6 relative;
   * the frame's hidden base height and kernel (bicubic) show the sharpest
-    dip of the score against the neighbouring heights of the same kernel.
+    dip of the score against the neighbouring heights of the same kernel;
+  * scoring fused into the columns pass (where a candidate allows it) and
+    the separate scoring kernel over the descaled plane agree within 1e-5
+    relative (the same descaled values, sums in another order).
 """
 import numpy as np
 import pytest
@@ -130,3 +133,28 @@ def test_sweep_rejects_mismatched_sources(gb, executor, setup):
                                        "mirror", 0), cached=False)
     with pytest.raises(ValueError):
         gb.Sweep(executor, [pairs[0], (other, pairs[0][1])], dframe.data_ptr(), dframe.shape[1])
+
+
+def test_fused_scoring_matches_separate_kernel(gb, whole_executor, setup):
+    frame, dframe, cands, pairs = setup
+    fused, finfo = _scores(gb, whole_executor, dframe, pairs, autotune=False, fused_scoring=True)
+    separate, sinfo = _scores(gb, whole_executor, dframe, pairs, autotune=False)
+    assert sinfo["fused_candidates"] == 0
+    assert finfo["fused_candidates"] >= len(pairs) // 2, finfo
+    assert np.max(np.abs(fused - separate) / np.abs(separate)) <= 1e-5
+    # Fused candidates need no descaled planes.
+    assert finfo["device_bytes"] < sinfo["device_bytes"]
+    for i in range(1, len(cands), 5):
+        want = _oracle_score(frame, cands[i][3], cands[i][4])
+        assert abs(fused[i] - want) <= 2e-5 + 1e-3 * abs(want), (cands[i][:3], fused[i], want)
+
+
+def test_fused_scoring_in_a_prepared_batch(gb, whole_executor, setup):
+    """Mixed waves: with a memory budget of one candidate per wave the
+    fused and unfused candidates of each wave still score as in one wave."""
+    _frame, dframe, _cands, pairs = setup
+    one, _ = _scores(gb, whole_executor, dframe, pairs, autotune=False, fused_scoring=True)
+    waved, info = _scores(gb, whole_executor, dframe, pairs, autotune=False, memory_budget=1 << 16,
+                          fused_scoring=True)
+    assert info["waves"] == len(pairs)
+    assert np.array_equal(one, waved)

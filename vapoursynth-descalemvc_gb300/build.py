@@ -35,7 +35,8 @@ TSOLVE_SOURCES = ([f"tsolve_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)]
 CUDA_SOURCES = TSTREAM2_SOURCES + TSOLVE_SOURCES + ["kernels.cu", "stream.cu", "stream_hb1.cu", "stream_hb3.cu", "stream_hb5.cu",
                 "stream_hb7.cu", "tstream_hb1.cu", "tstream_hb3.cu",
                 "tstream_hb5.cu", "tstream_hb7.cu", "tstream_hb1_g.cu", "tstream_hb3_g.cu",
-                "tstream_hb5_g.cu", "tstream_hb7_g.cu", "noalloc.cu", "score.cu",
+                "tstream_hb5_g.cu", "tstream_hb7_g.cu", "tscore_hb1.cu", "tscore_hb3.cu",
+                "tscore_hb5.cu", "tscore_hb7.cu", "noalloc.cu", "score.cu",
                 "peak.cu", "gpu_planner.cu", "refine64.cu"]
 
 

@@ -669,6 +669,7 @@ int dsmvc_gb_sweep_create(dsmvc_gb_executor *executor, const dsmvc_gb_plan *cons
             o.memory_budget = static_cast<std::size_t>(options->memory_budget);
             o.autotune = options->autotune != 0;
             o.graph = options->graph != 0;
+            o.fused_scoring = options->fused_scoring != 0;
         }
         s->sweep = std::make_unique<dsmvc_gb::Sweep>(exec_of(executor), list, frame, frame_stride, o);
         *out = s.release();
@@ -708,6 +709,7 @@ int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *ou
         out->segment_rows = i.segment_rows;
         out->tuned_groups = static_cast<int32_t>(i.tuning.size());
         out->vectors_per_warp = i.vectors_per_warp;
+        out->fused_candidates = i.fused_candidates;
     });
 }
 

@@ -12,6 +12,7 @@
 // the load of the first pass and the store of the second.
 #include "executor.hpp"
 #include "copy.hpp"
+#include "score.cuh"
 #include "stream.cuh"
 #include "stream_plan.hpp"
 
@@ -605,6 +606,8 @@ struct Executor::Impl {
         std::size_t scratch_bytes = 0;
         std::size_t tasks = 0;
     };
+    // Window of the fused scoring columns pass for this vertical plan, or -1.
+    [[nodiscard]] int fused_window(const DevicePlan &dp) const;
     void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                  const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr,
                  int vectors_per_warp = 0);
@@ -621,7 +624,8 @@ namespace {
 struct GroupKey {
     int pass;        // 0 first pass (rows), 1 second pass (columns)
     int kind;        // 0 sequential Float32, 1 sequential Float64, 2 streaming,
-                     // 3 transposing streaming (2D)
+                     // 3 transposing streaming (2D), ... 9 columns pass with
+                     // fused sweep scoring
     int hb;
     dev::Sample in, out;
     int variant = 0; // kind 3: the kernels' window (8, or 12 / 16 for grouped records), else 0
@@ -652,9 +656,23 @@ int compiled_window(const DevicePlan &dp, int kind) {
     return dp.stream_view.window == 8 ? (kind == 3 ? 8 : 1) : 0;
 }
 
+std::string kernel_name(const GroupKey &k);
+
+} // namespace
+
+int Executor::Impl::fused_window(const DevicePlan &dp) const {
+    if (!allow_stream || prefer_exact || !dp.stream || !dp.stream_t) return -1;
+    const int hb = dp.stream_view.half_bandwidth;
+    if (hb < 1 || hb > 7) return -1;
+    const int w = compiled_window(dp, 3);
+    return w == 0 || w == 8 || w == 12 || w == 16 ? w : -1;
+}
+
+namespace {
+
 std::string kernel_name(const GroupKey &k) {
     static const char *kinds[] = {"axis_f32", "axis_f64", "stream_f32", "tstream_f32", "tstream2_f32",
-                                  "tsolve_f32", "tsolve_f64", "refine_f64", "convert_f64"};
+                                  "tsolve_f32", "tsolve_f64", "refine_f64", "convert_f64", "tscore_f32"};
     return std::string(kinds[k.kind]) + (k.pass ? "/columns" : "/rows") + "/hb" + std::to_string(k.hb);
 }
 
@@ -789,6 +807,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         r.h = h ? &device_plan(*h, task.horizontal_keep, temporaries, out.private_uploads) : nullptr;
         r.v = v ? &device_plan(*v, task.vertical_keep, temporaries, out.private_uploads) : nullptr;
         r.f64 = (h && h->requires_float64()) || (v && v->requires_float64());
+        if (task.score && r.f64) throw std::invalid_argument("fused scoring needs Float32 plans");
         if (!r.f64 && allow_stream) {
             r.h_stream = r.h && stream_row_ok(*r.h, h && v ? task.sample : dev::Sample::f32);
             r.v_stream = r.v && r.v->stream;
@@ -822,6 +841,12 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
             };
             r.h_kind = pass_kind(*r.h);
             r.v_kind = pass_kind(*r.v);
+            if (task.score) {
+                // The fused scoring pass replaces the chunk-delayed one.
+                if (fused_window(*r.v) < 0 || task.sample != dev::Sample::f32)
+                    throw std::invalid_argument("fused scoring needs a chunk-delayed Float32 columns pass");
+                r.v_kind = 9;
+            }
             r.mid_stride = (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4;
             r.mid = bytes;
             bytes += align_up(r.mid_stride * static_cast<std::size_t>(h->destination_size) * 4);
@@ -922,6 +947,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         dev::StreamJob stream{};
         std::uint64_t bytes = 0;
         const DevicePlan *plan = nullptr;   // chunk-delayed transposing passes
+        int tiles = 0;                      // fused scoring: CTAs of the job
     };
     std::map<GroupKey, std::vector<Item>> groups;
     for (std::size_t t = 0; t < tasks.size(); ++t) {
@@ -1031,7 +1057,18 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 j.conv = conv;
                 groups[{0, 0, h->half_bandwidth, task.sample, dev::Sample::f32}].push_back(hi);
             }
-            if (r.v_kind) {
+            if (r.v_kind == 9) {
+                auto &j = vi.stream;
+                j.plan = r.v->stream_union ? r.v->stream_view_g : r.v->stream_view;
+                j.in = mid; j.in_elem = 1; j.in_vec = pitch;
+                j.vectors = h->destination_size;
+                j.conv = conv;
+                j.score = task.score;
+                vi.plan = r.v;
+                vi.tiles = task.score_tiles;
+                vi.bytes = static_cast<std::uint64_t>(h->destination_size) * v->source_size * 4;
+                groups[{1, 9, v->half_bandwidth, dev::Sample::f32, dev::Sample::f32, fused_window(*r.v)}].push_back(vi);
+            } else if (r.v_kind) {
                 auto &j = vi.stream;
                 j.plan = r.v_kind == 4 ? r.v->stream_view2
                        : r.v_kind == 3 && r.v->stream_union ? r.v->stream_view_g : r.v->stream_view;
@@ -1148,8 +1185,10 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
     table.clear();
     launches.clear();
     for (auto &[key, items] : groups) {
-        const bool is_stream = key.kind >= 2 && key.kind <= 6;
-        int per_block = key.kind == 2 ? stream_block : is_stream ? tstream_threads : kSeqThreads;
+        const bool fused = key.kind == 9;
+        const bool is_stream = (key.kind >= 2 && key.kind <= 6) || fused;
+        int per_block = key.kind == 2 ? stream_block : fused ? kScoreCtaThreads
+                      : is_stream ? tstream_threads : kSeqThreads;
         if (tuning && key.kind != 2 && key.kind <= 6) {
             const GroupTuple g{key.pass, key.kind, key.hb, static_cast<int>(key.in), static_cast<int>(key.out),
                                key.variant};
@@ -1163,7 +1202,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         // Transposing kernels are assigned warps, not CTAs: a CTA's warps
         // may serve consecutive jobs of one plan (they share the CTA's record
         // copies), so only plan changes round up to a whole CTA.
-        const bool by_warp = key.kind >= 3 && key.kind <= 6;
+        const bool by_warp = (key.kind >= 3 && key.kind <= 6) || fused;
         const int warps_per_cta = per_block / 32;
         const int vectors_per_warp = key.kind == 4 ? 64 : 32;
         // Jobs of one plan stay together (they share record copies); plans
@@ -1183,7 +1222,13 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
         for (auto &it : items) {
             const int vectors = is_stream ? it.stream.vectors : it.axis.vectors;
             if (vectors <= 0) continue;
-            if (by_warp) {
+            if (fused) {
+                // One CTA per tile; every job starts on a CTA.
+                warps = (warps + warps_per_cta - 1) / warps_per_cta * warps_per_cta;
+                it.stream.first_block = warps;
+                warps += it.tiles * warps_per_cta;
+                blocks = warps / warps_per_cta;
+            } else if (by_warp) {
                 if (warps && (it.stream.plan.forward != run_plan || it.stream.chunk_begin != run_chunk))
                     warps = (warps + warps_per_cta - 1) / warps_per_cta * warps_per_cta;
                 run_plan = it.stream.plan.forward;
@@ -1228,7 +1273,10 @@ void Executor::Impl::launch(const Compiled &c, const char *device_table, cudaStr
         }
         const char *dev_table = device_table + l.offset;
         int rc = 0;
-        if (l.kind == 7) {
+        if (l.kind == 9) {
+            rc = launch_tscore(reinterpret_cast<const dev::StreamJob *>(dev_table), l.count, l.blocks, l.hb,
+                               l.variant, l.record_floats, stream);
+        } else if (l.kind == 7) {
             rc = launch_refine64(reinterpret_cast<const dev::AxisJob *>(dev_table), l.count, l.blocks, l.threads,
                                  l.hb, l.in, status, stream);
         } else if (l.kind == 8) {
@@ -1280,7 +1328,7 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
     if (c.launches.empty()) return;
     ws.upload_table(c.table);
     launch(c, ws.jobs.data(), ws.stream, ws.status);
-    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind >= 6;
+    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || (l.kind >= 6 && l.kind <= 8);
     if (c.private_uploads > 0) {
         // Private plan uploads must outlive the kernels that read them.
         // (Cached plans evicted meanwhile are released by cudaFree, which
@@ -1760,8 +1808,10 @@ namespace {
 void validate_tasks(const std::vector<PlaneTask> &tasks) {
     for (const auto &t : tasks) {
         const AxisPlan *h = t.horizontal, *v = t.vertical;
-        if ((!h && !v) || !t.input || !t.output || (h && !h->valid()) || (v && !v->valid()))
+        if ((!h && !v) || !t.input || (!t.output && !t.score) || (h && !h->valid()) || (v && !v->valid()))
             throw std::invalid_argument("invalid batch plane");
+        if (t.score && (!h || !v || t.sample != dev::Sample::f32 || t.score_tiles <= 0))
+            throw std::invalid_argument("invalid fused scoring task");
         if (h && v) {
             if (t.input_stride < h->source_size || t.output_stride < h->destination_size)
                 throw std::invalid_argument("invalid batch plane strides");
@@ -1908,7 +1958,8 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
     // sources of the second, rows padded to 4) plus a forward plane of the
     // output's size, in the route's sample width; 2D planes also the forward
     // values of two-pass segments (margins included, at most twice a pass's
-    // whole chunks of forward values).
+    // whole chunks of forward values).  A fused scoring task's columns pass
+    // needs nothing beyond the intermediate.
     std::size_t bytes = kAlign;
     for (const auto &t : tasks) {
         const AxisPlan *h = t.horizontal, *v = t.vertical;
@@ -1918,14 +1969,23 @@ std::size_t Executor::batch_scratch_bound(const std::vector<PlaneTask> &tasks) {
         const std::size_t hd = h ? static_cast<std::size_t>(h->destination_size) : static_cast<std::size_t>(t.vectors);
         const std::size_t vs = v ? (static_cast<std::size_t>(v->source_size) + 3) / 4 * 4 : static_cast<std::size_t>(t.vectors);
         const std::size_t vd = v ? static_cast<std::size_t>(v->destination_size) : static_cast<std::size_t>(t.vectors);
-        bytes += align_up(hd * vs * es) + align_up(hd * vd * es);
+        bytes += align_up(hd * vs * es) + (t.score ? 0 : align_up(hd * vd * es));
         if (h && v) {
             const std::size_t hc = (hd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
             const std::size_t vc = (vd + kStreamChunk - 1) / kStreamChunk * kStreamChunk;
-            bytes += align_up(2 * hc * vs * es) + align_up(2 * vc * hd * es);
+            bytes += align_up(2 * hc * vs * es) + (t.score ? 0 : align_up(2 * vc * hd * es));
         }
     }
     return bytes;
+}
+
+int Executor::fused_scoring_window(const AxisPlan &vertical, const std::shared_ptr<const AxisPlan> &keep) {
+    DeviceGuard guard(impl_->device);
+    if (!vertical.valid()) throw std::invalid_argument("invalid plan");
+    if (vertical.requires_float64()) return -1;
+    std::vector<std::shared_ptr<DevicePlan>> held;
+    int private_uploads = 0;
+    return impl_->fused_window(impl_->device_plan(vertical, keep, held, private_uploads));
 }
 
 std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTask> &tasks,

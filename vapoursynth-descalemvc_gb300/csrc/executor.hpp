@@ -50,6 +50,12 @@ struct PlaneTask {
     // up in (or added to) the executor's device plan cache when its owner is
     // given; otherwise it is uploaded for this submission only.
     std::shared_ptr<const AxisPlan> horizontal_keep, vertical_keep;
+    // Sweep scoring fused into the columns pass (Float32 2D tasks whose
+    // vertical plan has an Executor::fused_scoring_window >= 0): a device
+    // dev::ScoreEpilogue (score.cuh) and its tile count; `output` is then
+    // not written (and may be null).
+    const void *score = nullptr;
+    std::int32_t score_tiles = 0;
 };
 
 // One host-frame plane of a multi-plane call (Executor::inverse_2d_planes).
@@ -212,6 +218,14 @@ public:
                                                              int vectors_per_warp = 0, int parts = 0);
     // Upper bound of the scratch bytes prepare_batch needs for `tasks`.
     [[nodiscard]] static std::size_t batch_scratch_bound(const std::vector<PlaneTask> &tasks);
+
+    // The records window (0 for the plan's own, 8, 12 or 16) of the fused
+    // scoring columns pass (PlaneTask::score) for Float32 2D tasks with this
+    // vertical plan, or -1 where the plan's columns pass runs another kernel
+    // (not chunk-delayed, half-bandwidth above 7, or DSMVC_GB_EXACT=1).  The
+    // plan is uploaded (cached with its owner) as a batch would.
+    [[nodiscard]] int fused_scoring_window(const AxisPlan &vertical,
+                                           const std::shared_ptr<const AxisPlan> &keep = nullptr);
 
     [[nodiscard]] ExecutorStats stats() const;
 

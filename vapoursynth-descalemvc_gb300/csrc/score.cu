@@ -226,7 +226,7 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
 }
 
 __global__ void __launch_bounds__(kScoreThreads)
-score_finalize_kernel(const ScoreJob *__restrict__ jobs, float *scores) {
+score_finalize_kernel(const ScoreJob *__restrict__ jobs) {
     __shared__ double sums[kScoreThreads];
     const ScoreJob &job = jobs[blockIdx.x];
     const int n = job.column_tiles * ((job.height + kScoreRowBlock - 1) / kScoreRowBlock);
@@ -239,10 +239,32 @@ score_finalize_kernel(const ScoreJob *__restrict__ jobs, float *scores) {
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        scores[blockIdx.x] = static_cast<float>(sums[0] / (static_cast<double>(job.width) * job.height));
+        *job.score = static_cast<float>(sums[0] / (static_cast<double>(job.width) * job.height));
+}
+
+__global__ void __launch_bounds__(kScoreThreads)
+fused_score_finalize_kernel(const dev::ScoreEpilogue *__restrict__ epilogues) {
+    __shared__ double sums[kScoreThreads];
+    const dev::ScoreEpilogue &ep = epilogues[blockIdx.x];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < ep.tiles; i += blockDim.x) acc += ep.partials[i];
+    sums[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (static_cast<int>(threadIdx.x) < w) sums[threadIdx.x] += sums[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        *ep.score = static_cast<float>(sums[0] / (static_cast<double>(ep.width) * ep.height));
 }
 
 } // namespace
+
+int launch_fused_score_finalize(const dev::ScoreEpilogue *epilogues, int count, void *stream) {
+    if (count <= 0) return 0;
+    fused_score_finalize_kernel<<<count, kScoreThreads, 0, static_cast<cudaStream_t>(stream)>>>(epilogues);
+    return static_cast<int>(cudaGetLastError());
+}
 
 int launch_score_tiles(const dev::ScoreJob *jobs, int count, int blocks, int max_span_rows, void *stream) {
     if (blocks <= 0) return 0;
@@ -255,9 +277,9 @@ int launch_score_tiles(const dev::ScoreJob *jobs, int count, int blocks, int max
     return static_cast<int>(cudaGetLastError());
 }
 
-int launch_score_finalize(const dev::ScoreJob *jobs, int count, float *scores, void *stream) {
+int launch_score_finalize(const dev::ScoreJob *jobs, int count, void *stream) {
     if (count <= 0) return 0;
-    score_finalize_kernel<<<count, kScoreThreads, 0, static_cast<cudaStream_t>(stream)>>>(jobs, scores);
+    score_finalize_kernel<<<count, kScoreThreads, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
     return static_cast<int>(cudaGetLastError());
 }
 

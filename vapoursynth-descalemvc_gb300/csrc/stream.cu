@@ -136,4 +136,20 @@ int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, 
     }
 }
 
+int launch_tscore_hb1(const dev::StreamJob *, int, int, int, int, void *);
+int launch_tscore_hb3(const dev::StreamJob *, int, int, int, int, void *);
+int launch_tscore_hb5(const dev::StreamJob *, int, int, int, int, void *);
+int launch_tscore_hb7(const dev::StreamJob *, int, int, int, int, void *);
+
+int launch_tscore(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth, int window,
+                  int record_floats, void *stream) {
+    switch (half_bandwidth) {
+    case 1: return launch_tscore_hb1(jobs, job_count, total_blocks, window, record_floats, stream);
+    case 3: return launch_tscore_hb3(jobs, job_count, total_blocks, window, record_floats, stream);
+    case 5: return launch_tscore_hb5(jobs, job_count, total_blocks, window, record_floats, stream);
+    case 7: return launch_tscore_hb7(jobs, job_count, total_blocks, window, record_floats, stream);
+    default: return static_cast<int>(cudaErrorInvalidValue);
+    }
+}
+
 } // namespace dsmvc_gb

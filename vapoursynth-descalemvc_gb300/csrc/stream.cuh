@@ -60,6 +60,9 @@ struct StreamJob {
     // vector, storing its forward values from its first computed chunk on
     // at y (rows of y_elem).
     std::int32_t margin;
+    // Columns passes with fused candidate scoring (tscore_impl.cuh): the
+    // device ScoreEpilogue (score.cuh); the pass then stores no output.
+    const void *score;
 };
 
 } // namespace dsmvc_gb::dev
@@ -97,6 +100,14 @@ int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, 
 int launch_tstream2(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
                     int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
                     void *stream);
+
+// Columns passes with fused candidate scoring (tscore_impl.cuh): as
+// launch_tstream for Float32 intermediates with chunk-delayed records
+// (window 0, 8, 12 or 16) and half-bandwidths 1..7, every job carrying a
+// ScoreEpilogue (score.cuh) and starting on a CTA of kScoreCtaThreads
+// threads, one CTA per tile; nothing is stored but the tiles' partials.
+int launch_tscore(const dev::StreamJob *jobs, int job_count, int total_blocks, int half_bandwidth, int window,
+                  int record_floats, void *stream);
 
 // Two-pass transposing 2D passes (tsolve_impl.cuh): exact forward and
 // backward sweeps through the jobs' forward-value planes; half-bandwidths

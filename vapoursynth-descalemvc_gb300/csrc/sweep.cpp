@@ -2,6 +2,7 @@
 #include "sweep.hpp"
 
 #include "score.cuh"
+#include "stream.cuh"
 
 #include <cuda_runtime.h>
 
@@ -74,6 +75,47 @@ HostForward forward_csr(const AxisPlan &p) {
     return f;
 }
 
+// Dense operator rows of the fused scoring (dev::ScoreEpilogue): 12 floats
+// a row.  `ok` is false where an operator does not fit: an empty row or a
+// window wider than `max_taps`.  (Windows need not move monotonically: a
+// sample that falls on a descaled sample has one entry, narrower than its
+// neighbours'.)
+struct DenseRows {
+    bool ok = false;
+    int taps = 0;               // 4 or 8
+    int widest = 0;             // largest last - first index of a row
+    std::vector<float> rows;    // 12 floats a row
+    std::vector<int> first, last;
+};
+
+DenseRows dense_rows(const HostForward &f, int max_taps) {
+    DenseRows d;
+    const int n = static_cast<int>(f.offsets.size()) - 1;
+    d.first.resize(static_cast<std::size_t>(n));
+    d.last.resize(static_cast<std::size_t>(n));
+    for (int r = 0; r < n; ++r) {
+        const std::uint32_t e0 = f.offsets[static_cast<std::size_t>(r)], e1 = f.offsets[static_cast<std::size_t>(r) + 1];
+        if (e0 == e1) return d;
+        const int a = f.indices[e0], b = f.indices[e1 - 1];
+        d.first[static_cast<std::size_t>(r)] = a;
+        d.last[static_cast<std::size_t>(r)] = b;
+        d.widest = std::max(d.widest, b - a);
+    }
+    if (d.widest + 1 > max_taps) return d;
+    d.taps = d.widest + 1 <= 4 ? 4 : 8;
+    d.ok = true;
+    return d;
+}
+
+// Fills row r's window from `start` (weights at index - start).
+void put_dense(std::vector<float> &out, const HostForward &f, int r, int start) {
+    float *row = out.data() + static_cast<std::size_t>(r) * 12;
+    std::int32_t bits = start;
+    std::memcpy(row, &bits, 4);
+    for (std::uint32_t e = f.offsets[static_cast<std::size_t>(r)]; e < f.offsets[static_cast<std::size_t>(r) + 1]; ++e)
+        row[4 + (f.indices[e] - start)] = f.weights[e];
+}
+
 } // namespace
 
 constexpr int kSegments[] = {16, 32, 64, 128};        // multiples of kScoreRowBlock
@@ -94,16 +136,27 @@ struct Sweep::Impl {
         std::vector<PlaneTask> tasks;
         std::unique_ptr<PreparedBatch> batch;
         int column_blocks = 0;
-        std::array<int, 4> max_span{};   // per entry of kSegments
+        std::array<int, 4> max_span{};   // per entry of kSegments (unfused candidates)
+        int fused_first = 0, fused = 0;       // its fused candidates' epilogues
+        int unfused_first = 0, unfused = 0;   // its unfused candidates' score jobs
     };
     std::vector<Wave> waves;
     std::vector<std::size_t> y_offset, partial_offset;   // within a wave's buffers
     Buffer forward_mem, y_mem, partial_mem, scratch_mem, job_mem, plain_job_mem, score_mem;
+    // Fused scoring (dev::ScoreEpilogue): per candidate its epilogue index
+    // (-1: descaled to HBM and scored by score_tiles_kernel) and tile count;
+    // the epilogues of fused candidates in candidate order, the unfused
+    // candidates' score jobs likewise.
+    std::vector<int> epilogue_of, tiles_of, unfused_of;
+    int fused_count = 0, unfused_count = 0;
+    Buffer epilogue_mem;
+    const dev::ScoreEpilogue *epilogues = nullptr;
     // Per vertical plan and segment length: the most descaled rows one
     // segment of source rows touches.
     std::map<const AxisPlan *, std::array<int, 4>> spans;
     std::size_t scratch_capacity = 0;
     std::map<const AxisPlan *, dev::ForwardCsr> forward;
+    std::map<const AxisPlan *, HostForward> host_forward;   // while building
     int segment_rows = 32;
     int best_segment = 32;
     int vectors_per_warp = 0;   // 0: the executor's default; 32 / 64 once tuned
@@ -120,21 +173,20 @@ struct Sweep::Impl {
     }
 
     void upload_forward() {
-        std::map<const AxisPlan *, HostForward> host;
         std::size_t bytes = 0;
         for (const auto &[h, v] : candidates) {
             for (const AxisPlan *p : {h, v}) {
-                if (host.count(p)) continue;
+                if (host_forward.count(p)) continue;
                 auto f = forward_csr(*p);
                 bytes += align_up(f.offsets.size() * 4) + align_up(f.indices.size() * 4)
                     + align_up(f.weights.size() * 4);
-                host.emplace(p, std::move(f));
+                host_forward.emplace(p, std::move(f));
             }
         }
         std::vector<char> blob(std::max<std::size_t>(bytes, kAlign), 0);
         forward_mem.allocate(blob.size());
         std::size_t at = 0;
-        for (auto &[p, f] : host) {
+        for (auto &[p, f] : host_forward) {
             dev::ForwardCsr c{};
             auto put = [&](const void *src, std::size_t n) {
                 std::memcpy(blob.data() + at, src, n);
@@ -167,41 +219,247 @@ struct Sweep::Impl {
               "uploading forward operators");
     }
 
+    // Decides per candidate whether its scoring fuses into its columns pass
+    // (the executor runs that pass with the fused kernel and both operators
+    // fit the epilogue's windows) and uploads the fused candidates' operator
+    // tables, tile bounds, partial sums and epilogues.
+    void build_epilogues() {
+        const std::size_t n = candidates.size();
+        epilogue_of.assign(n, -1);
+        tiles_of.assign(n, 0);
+        unfused_of.assign(n, -1);
+        struct VTable {
+            DenseRows d;
+            std::vector<std::int32_t> emit;
+        };
+        struct HTable {
+            DenseRows d;
+            int tiles = 0;
+            std::vector<std::int32_t> sources, origins;
+        };
+        std::map<const AxisPlan *, VTable> vtab;
+        std::map<const AxisPlan *, HTable> htab;
+        std::map<const AxisPlan *, int> windows;
+        auto vertical_table = [&](const AxisPlan *v) -> const VTable & {
+            auto it = vtab.find(v);
+            if (it != vtab.end()) return it->second;
+            VTable t;
+            const HostForward &f = host_forward.at(v);
+            t.d = dense_rows(f, kScoreMaxVerticalTaps);
+            if (t.d.ok) {
+                const int rows = static_cast<int>(f.offsets.size()) - 1;
+                const int chunks = (v->destination_size + kStreamChunk - 1) / kStreamChunk;
+                t.d.rows.assign(static_cast<std::size_t>(rows) * 12, 0.0f);
+                t.emit.assign(static_cast<std::size_t>(chunks), 0);
+                // A row is re-upscaled after the first chunk that holds its
+                // last entry and every earlier row's; its window then lies in
+                // that chunk and the ring rows before it.
+                int q = 0;
+                for (int r = 0; r < rows && t.d.ok; ++r) {
+                    q = std::max(q, t.d.last[static_cast<std::size_t>(r)] / kStreamChunk);
+                    const int start = std::min(t.d.first[static_cast<std::size_t>(r)],
+                                               kStreamChunk * (q + 1) - t.d.taps);
+                    // The window's ring slots: [start - (32 q - halo), + taps)
+                    // within the kScoreRingRows the kernel keeps.
+                    const int slot = start - (kStreamChunk * q - (kScoreRingRows - kStreamChunk));
+                    if (q >= chunks || slot < 0 || slot + t.d.taps > kScoreRingRows) t.d.ok = false;
+                    else put_dense(t.d.rows, f, r, start);
+                    t.emit[static_cast<std::size_t>(q < chunks ? q : 0)] = r + 1;
+                }
+                for (int c = 1; c < chunks; ++c)
+                    t.emit[static_cast<std::size_t>(c)] = std::max(t.emit[static_cast<std::size_t>(c)],
+                                                                   t.emit[static_cast<std::size_t>(c) - 1]);
+                if (chunks < 1 || t.emit.back() != rows) t.d.ok = false;
+            }
+            return vtab.emplace(v, std::move(t)).first->second;
+        };
+        auto horizontal_table = [&](const AxisPlan *h) -> const HTable & {
+            auto it = htab.find(h);
+            if (it != htab.end()) return it->second;
+            HTable t;
+            const HostForward &f = host_forward.at(h);
+            t.d = dense_rows(f, kScoreMaxHorizontalTaps);
+            if (t.d.ok) {
+                const int cols = static_cast<int>(f.offsets.size()) - 1;
+                t.d.rows.assign(static_cast<std::size_t>(cols) * 12, 0.0f);
+                for (int s = 0; s < cols; ++s) put_dense(t.d.rows, f, s, t.d.first[static_cast<std::size_t>(s)]);
+                // Tiles: runs of consecutive source columns as long as their
+                // windows lie within kScoreCtaThreads descaled columns from
+                // the run's lowest window start (the tile's origin) and their
+                // padded windows within the row buffer's 8 zero columns after.
+                for (int s = 0; s < cols;) {
+                    int lo = t.d.first[static_cast<std::size_t>(s)], hi = -1, pad = 0, e = s;
+                    for (; e < cols; ++e) {
+                        const int nlo = std::min(lo, t.d.first[static_cast<std::size_t>(e)]);
+                        const int nhi = std::max(hi, t.d.last[static_cast<std::size_t>(e)]);
+                        const int npad = std::max(pad, t.d.first[static_cast<std::size_t>(e)] + t.d.taps);
+                        if (e > s && (nhi - nlo >= kScoreCtaThreads || npad - nlo > kScoreCtaThreads + 8)) break;
+                        lo = nlo;
+                        hi = nhi;
+                        pad = npad;
+                    }
+                    t.sources.push_back(s);
+                    t.origins.push_back(lo);
+                    s = e;
+                }
+                t.sources.push_back(cols);
+                t.tiles = static_cast<int>(t.origins.size());
+            }
+            return htab.emplace(h, std::move(t)).first->second;
+        };
+        for (std::size_t i = 0; i < n; ++i) {
+            const auto &[h, v] = candidates[i];
+            bool ok = options.fused_scoring;
+            if (ok) {
+                auto w = windows.find(v);
+                if (w == windows.end()) w = windows.emplace(v, executor->fused_scoring_window(*v, owners[i].second)).first;
+                ok = w->second >= 0;
+            }
+            ok = ok && vertical_table(v).d.ok && horizontal_table(h).d.ok;
+            if (ok) {
+                epilogue_of[i] = fused_count++;
+                tiles_of[i] = htab.at(h).tiles;
+            } else {
+                unfused_of[i] = unfused_count++;
+            }
+        }
+        if (!fused_count) return;
+        // One allocation: the tables, then each fused candidate's partials,
+        // then the epilogues.
+        std::size_t bytes = 0;
+        std::map<const AxisPlan *, std::size_t> at_v, at_h;
+        for (std::size_t i = 0; i < n; ++i) {
+            if (epilogue_of[i] < 0) continue;
+            const auto &[h, v] = candidates[i];
+            if (!at_v.count(v)) {
+                at_v[v] = bytes;
+                const auto &t = vtab.at(v);
+                bytes += align_up(t.d.rows.size() * 4) + align_up(t.emit.size() * 4);
+            }
+            if (!at_h.count(h)) {
+                at_h[h] = bytes;
+                const auto &t = htab.at(h);
+                bytes += align_up(t.d.rows.size() * 4) + align_up(t.sources.size() * 4)
+                    + align_up(t.origins.size() * 4);
+            }
+        }
+        std::vector<std::size_t> at_partials(n, 0);
+        for (std::size_t i = 0; i < n; ++i) {
+            if (epilogue_of[i] < 0) continue;
+            at_partials[i] = bytes;
+            bytes += align_up(static_cast<std::size_t>(tiles_of[i]) * sizeof(double));
+        }
+        const std::size_t at_epilogues = bytes;
+        bytes += static_cast<std::size_t>(fused_count) * sizeof(dev::ScoreEpilogue);
+        std::vector<char> blob(bytes, 0);
+        epilogue_mem.allocate(bytes);
+        char *base = epilogue_mem.data();
+        auto put = [&](std::size_t at, const void *src, std::size_t len) {
+            if (len) std::memcpy(blob.data() + at, src, len);
+        };
+        for (const auto &[v, at] : at_v) {
+            const auto &t = vtab.at(v);
+            put(at, t.d.rows.data(), t.d.rows.size() * 4);
+            put(at + align_up(t.d.rows.size() * 4), t.emit.data(), t.emit.size() * 4);
+        }
+        for (const auto &[h, at] : at_h) {
+            const auto &t = htab.at(h);
+            put(at, t.d.rows.data(), t.d.rows.size() * 4);
+            put(at + align_up(t.d.rows.size() * 4), t.sources.data(), t.sources.size() * 4);
+            put(at + align_up(t.d.rows.size() * 4) + align_up(t.sources.size() * 4), t.origins.data(),
+                t.origins.size() * 4);
+        }
+        auto *eps = reinterpret_cast<dev::ScoreEpilogue *>(blob.data() + at_epilogues);
+        for (std::size_t i = 0; i < n; ++i) {
+            if (epilogue_of[i] < 0) continue;
+            const auto &[h, v] = candidates[i];
+            const auto &vt = vtab.at(v);
+            const auto &ht = htab.at(h);
+            dev::ScoreEpilogue e{};
+            e.frame = frame;
+            e.frame_stride = frame_stride;
+            e.width = width;
+            e.height = height;
+            e.v_rows = reinterpret_cast<const float *>(base + at_v.at(v));
+            e.v_emit = reinterpret_cast<const std::int32_t *>(base + at_v.at(v) + align_up(vt.d.rows.size() * 4));
+            e.h_cols = reinterpret_cast<const float *>(base + at_h.at(h));
+            e.tile_sources = reinterpret_cast<const std::int32_t *>(base + at_h.at(h)
+                                                                    + align_up(ht.d.rows.size() * 4));
+            e.tile_origins = e.tile_sources + align_up(ht.sources.size() * 4) / 4;
+            e.v_taps = vt.d.taps;
+            e.h_taps = ht.d.taps;
+            e.tiles = ht.tiles;
+            e.partials = reinterpret_cast<double *>(base + at_partials[i]);
+            e.score = reinterpret_cast<float *>(score_mem.data()) + i;
+            eps[epilogue_of[i]] = e;
+        }
+        check(cudaMemcpy(base, blob.data(), bytes, cudaMemcpyHostToDevice), "uploading fused scoring tables");
+        epilogues = reinterpret_cast<const dev::ScoreEpilogue *>(base + at_epilogues);
+    }
+
     [[nodiscard]] int column_tiles() const { return (width + kScoreThreads - 1) / kScoreThreads; }
     [[nodiscard]] int segments(int seg) const { return (height + seg - 1) / seg; }
 
     // Splits the candidates into waves within the memory budget and lays
-    // out each wave's descaled planes, row-pass planes and partial sums.
+    // out each wave's descaled planes (unfused candidates), row-pass scratch
+    // and partial sums.
     void plan_waves() {
         const std::size_t budget = options.memory_budget ? options.memory_budget : (32ULL << 30);
         const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kScoreRowBlock) * 4);
         std::size_t y_bytes = 0, p_bytes = 0, s_bytes = 0;
         std::size_t y_max = 0, p_max = 0, s_max = 0;
-        y_offset.resize(candidates.size());
-        partial_offset.resize(candidates.size());
+        y_offset.assign(candidates.size(), 0);
+        partial_offset.assign(candidates.size(), 0);
         Wave cur;
+        int fused_seen = 0, unfused_seen = 0;
+        auto task_of = [&](std::size_t i) {
+            PlaneTask t;
+            t.horizontal = candidates[i].first;
+            t.vertical = candidates[i].second;
+            t.horizontal_keep = owners[i].first;
+            t.vertical_keep = owners[i].second;
+            t.input = frame;
+            t.input_stride = frame_stride;
+            t.output_stride = candidates[i].first->destination_size;
+            t.sample = dev::Sample::f32;
+            if (epilogue_of[i] >= 0) {
+                t.score = epilogues + epilogue_of[i];
+                t.score_tiles = tiles_of[i];
+            }
+            return t;
+        };
         for (std::size_t i = 0; i < candidates.size(); ++i) {
             const auto &[h, v] = candidates[i];
-            const std::size_t y = align_up(static_cast<std::size_t>(h->destination_size) * v->destination_size * 4);
-            PlaneTask probe;
-            probe.horizontal = h;
-            probe.vertical = v;
-            const std::size_t s = Executor::batch_scratch_bound({probe});
-            if (cur.count > 0 && y_bytes + p_bytes + s_bytes + y + partials + s > budget) {
+            const bool fused = epilogue_of[i] >= 0;
+            const std::size_t y = fused ? 0 : align_up(static_cast<std::size_t>(h->destination_size) * v->destination_size * 4);
+            const std::size_t part = fused ? 0 : partials;
+            const std::size_t s = Executor::batch_scratch_bound({task_of(i)});
+            if (cur.count > 0 && y_bytes + p_bytes + s_bytes + y + part + s > budget) {
                 waves.push_back(std::move(cur));
                 cur = Wave{};
                 y_bytes = p_bytes = s_bytes = 0;
             }
-            if (cur.count == 0) cur.first = static_cast<int>(i);
+            if (cur.count == 0) {
+                cur.first = static_cast<int>(i);
+                cur.fused_first = fused_seen;
+                cur.unfused_first = unfused_seen;
+            }
             ++cur.count;
-            y_offset[i] = y_bytes;
-            partial_offset[i] = p_bytes;
+            if (fused) {
+                ++cur.fused;
+                ++fused_seen;
+            } else {
+                ++cur.unfused;
+                ++unfused_seen;
+                y_offset[i] = y_bytes;
+                partial_offset[i] = p_bytes;
+                const auto &sp = spans.at(v);
+                for (std::size_t k = 0; k < sp.size(); ++k) cur.max_span[k] = std::max(cur.max_span[k], sp[k]);
+            }
             y_bytes += y;
-            p_bytes += partials;
+            p_bytes += part;
             s_bytes += s;
             y_max = std::max(y_max, y_bytes);
-            const auto &sp = spans.at(v);
-            for (std::size_t k = 0; k < sp.size(); ++k) cur.max_span[k] = std::max(cur.max_span[k], sp[k]);
             p_max = std::max(p_max, p_bytes);
             s_max = std::max(s_max, s_bytes);
         }
@@ -213,31 +471,25 @@ struct Sweep::Impl {
         for (auto &w : waves) {
             for (int k = 0; k < w.count; ++k) {
                 const std::size_t i = static_cast<std::size_t>(w.first + k);
-                PlaneTask t;
-                t.horizontal = candidates[i].first;
-                t.vertical = candidates[i].second;
-                t.horizontal_keep = owners[i].first;
-                t.vertical_keep = owners[i].second;
-                t.input = frame;
-                t.input_stride = frame_stride;
-                t.output = y_mem.data() + y_offset[i];
-                t.output_stride = candidates[i].first->destination_size;
-                t.sample = dev::Sample::f32;
+                PlaneTask t = task_of(i);
+                if (epilogue_of[i] < 0) t.output = y_mem.data() + y_offset[i];
                 w.tasks.push_back(t);
             }
         }
     }
 
-    // Score jobs of every candidate with `seg` source rows per column-pass
-    // block; block numbering restarts at each wave (`plain`: at each job).
+    // Score jobs of the unfused candidates (in candidate order) with `seg`
+    // source rows per column-pass block; block numbering restarts at each
+    // wave (`plain`: at each job).
     std::vector<dev::ScoreJob> score_jobs(int seg, bool plain) {
-        std::vector<dev::ScoreJob> jobs(candidates.size());
+        std::vector<dev::ScoreJob> jobs(static_cast<std::size_t>(unfused_count));
         for (auto &w : waves) {
             int cols = 0;
             for (int k = 0; k < w.count; ++k) {
                 const std::size_t i = static_cast<std::size_t>(w.first + k);
+                if (unfused_of[i] < 0) continue;
                 const AxisPlan *h = candidates[i].first, *v = candidates[i].second;
-                auto &j = jobs[i];
+                auto &j = jobs[static_cast<std::size_t>(unfused_of[i])];
                 j.descaled = reinterpret_cast<const float *>(y_mem.data() + y_offset[i]);
                 j.descaled_stride = h->destination_size;
                 j.rows = v->destination_size;
@@ -249,6 +501,7 @@ struct Sweep::Impl {
                 j.h = forward.at(h);
                 j.v = forward.at(v);
                 j.partials = reinterpret_cast<float *>(partial_mem.data() + partial_offset[i]);
+                j.score = reinterpret_cast<float *>(score_mem.data()) + i;
                 j.segment_rows = seg;
                 j.column_tiles = column_tiles();
                 j.first_block = plain ? 0 : cols;
@@ -260,17 +513,15 @@ struct Sweep::Impl {
     }
 
     void upload_jobs(Buffer &mem, const std::vector<dev::ScoreJob> &jobs) {
-        const std::size_t n = jobs.size() * sizeof(dev::ScoreJob);
+        const std::size_t n = std::max<std::size_t>(jobs.size(), 1) * sizeof(dev::ScoreJob);
         if (mem.bytes < n) mem.allocate(n);
-        check(cudaMemcpy(mem.data(), jobs.data(), n, cudaMemcpyHostToDevice), "uploading score jobs");
+        if (!jobs.empty())
+            check(cudaMemcpy(mem.data(), jobs.data(), jobs.size() * sizeof(dev::ScoreJob), cudaMemcpyHostToDevice),
+                  "uploading score jobs");
     }
 
     [[nodiscard]] const dev::ScoreJob *wave_jobs(const Wave &w) const {
-        return reinterpret_cast<const dev::ScoreJob *>(job_mem.data()) + w.first;
-    }
-
-    [[nodiscard]] float *wave_scores(const Wave &w) const {
-        return reinterpret_cast<float *>(score_mem.data()) + w.first;
+        return reinterpret_cast<const dev::ScoreJob *>(job_mem.data()) + w.unfused_first;
     }
 
     [[nodiscard]] int span_rows(const Wave &w) const {
@@ -282,8 +533,12 @@ struct Sweep::Impl {
     // A wave's scores are reduced before the next wave reuses its buffers
     // (descaled planes and partial sums).
     void enqueue_scoring(const Wave &w, cudaStream_t s) {
-        check(launch_score_tiles(wave_jobs(w), w.count, w.column_blocks, span_rows(w), s), "launching scoring");
-        check(launch_score_finalize(wave_jobs(w), w.count, wave_scores(w), s), "launching score finalize");
+        if (w.unfused) {
+            check(launch_score_tiles(wave_jobs(w), w.unfused, w.column_blocks, span_rows(w), s), "launching scoring");
+            check(launch_score_finalize(wave_jobs(w), w.unfused, s), "launching score finalize");
+        }
+        if (w.fused)
+            check(launch_fused_score_finalize(epilogues + w.fused_first, w.fused, s), "launching score finalize");
     }
 
     void enqueue_all(cudaStream_t s) {
@@ -312,8 +567,9 @@ struct Sweep::Impl {
     // Times the first wave's descale with one and with two right-hand sides
     // a lane (32 or 64 vectors a warp), then every launch group of it at
     // each candidate CTA size, and the scoring column pass at each row
-    // segment; keeps the fastest of each.  Scores do not depend on the
-    // choices: every kernel variant gives each output bit for bit.
+    // segment (unfused candidates); keeps the fastest of each.  Scores do
+    // not depend on the choices: every kernel variant gives each output bit
+    // for bit, and the fused scoring kernel has one launch shape.
     void autotune() {
         const auto t0 = std::chrono::steady_clock::now();
         Wave &w = waves.front();
@@ -337,7 +593,7 @@ struct Sweep::Impl {
             BatchTuning all;
             for (const auto &g : keys) {
                 const int most = g.kind >= 3 ? 256 : 128;
-                if (g.kind != 2 && threads <= most) all[g.key] = threads;
+                if (g.kind != 2 && g.kind <= 6 && threads <= most) all[g.key] = threads;
             }
             if (all.empty()) continue;
             auto batch = executor->prepare_batch(w.tasks, &all, scratch_mem.data(), scratch_capacity,
@@ -356,12 +612,12 @@ struct Sweep::Impl {
         float best_ms = 0.0F;
         const int fallback = segment_rows;
         bool any = false;
-        for (std::size_t k = 0; k < std::size(kSegments); ++k) {
+        for (std::size_t k = 0; w.unfused && k < std::size(kSegments); ++k) {
             if (w.max_span[k] > kMaxSpanRows) continue;
             upload_jobs(job_mem, score_jobs(kSegments[k], false));
             segment_rows = kSegments[k];
             const float ms = time_ms([&] {
-                check(launch_score_tiles(wave_jobs(w), w.count, w.column_blocks, span_rows(w), stream), "launching");
+                check(launch_score_tiles(wave_jobs(w), w.unfused, w.column_blocks, span_rows(w), stream), "launching");
             }, 3);
             if (!any || ms < best_ms) {
                 best_ms = ms;
@@ -375,9 +631,11 @@ struct Sweep::Impl {
 
     void build() {
         check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "creating stream");
-        upload_forward();
-        plan_waves();
         score_mem.allocate(candidates.size() * sizeof(float));
+        upload_forward();
+        build_epilogues();
+        host_forward.clear();
+        plan_waves();
         if (options.autotune) autotune();
         // Every wave's row span at the chosen segment must fit the staging.
         for (const auto &w : waves) {
@@ -456,15 +714,19 @@ void Sweep::run_plain(void *stream) {
     for (const auto &w : m.waves) {
         for (int k = 0; k < w.count; ++k) {
             const std::size_t i = static_cast<std::size_t>(w.first + k);
-            const AxisPlan *v = m.candidates[i].second;
             m.executor->run_batch({w.tasks[static_cast<std::size_t>(k)]}, stream, false);
-            const int col_blocks = m.column_tiles() * m.segments(m.segment_rows);
-            int span = 0;
-            for (std::size_t q = 0; q < std::size(kSegments); ++q)
-                if (kSegments[q] == m.segment_rows) span = m.spans.at(v)[q];
-            check(launch_score_tiles(jobs + i, 1, col_blocks, span, s), "launching");
-            check(launch_score_finalize(jobs + i, 1, reinterpret_cast<float *>(m.score_mem.data()) + i, s),
-                  "launching");
+            if (m.epilogue_of[i] >= 0) {
+                check(launch_fused_score_finalize(m.epilogues + m.epilogue_of[i], 1, s), "launching");
+            } else {
+                const AxisPlan *v = m.candidates[i].second;
+                const int col_blocks = m.column_tiles() * m.segments(m.segment_rows);
+                int span = 0;
+                for (std::size_t q = 0; q < std::size(kSegments); ++q)
+                    if (kSegments[q] == m.segment_rows) span = m.spans.at(v)[q];
+                const dev::ScoreJob *job = jobs + m.unfused_of[i];
+                check(launch_score_tiles(job, 1, col_blocks, span, s), "launching");
+                check(launch_score_finalize(job, 1, s), "launching");
+            }
             check(cudaStreamSynchronize(s), "synchronizing");
         }
     }
@@ -481,9 +743,11 @@ std::array<double, 3> Sweep::stage_milliseconds(void *stream) {
             check(cudaEventRecord(ev[0], s), "recording event");
             w.batch->launch(s);
             check(cudaEventRecord(ev[1], s), "recording event");
-            check(launch_score_tiles(m.wave_jobs(w), w.count, w.column_blocks, m.span_rows(w), s), "launching");
+            if (w.unfused)
+                check(launch_score_tiles(m.wave_jobs(w), w.unfused, w.column_blocks, m.span_rows(w), s), "launching");
             check(cudaEventRecord(ev[2], s), "recording event");
-            check(launch_score_finalize(m.wave_jobs(w), w.count, m.wave_scores(w), s), "launching");
+            if (w.unfused) check(launch_score_finalize(m.wave_jobs(w), w.unfused, s), "launching");
+            if (w.fused) check(launch_fused_score_finalize(m.epilogues + w.fused_first, w.fused, s), "launching");
             check(cudaEventRecord(ev[3], s), "recording event");
             check(cudaEventSynchronize(ev[3]), "waiting for event");
             for (int k = 0; k < 3; ++k) {
@@ -515,9 +779,11 @@ SweepInfo Sweep::info() const {
     SweepInfo i;
     i.candidates = static_cast<int>(m.candidates.size());
     i.waves = static_cast<int>(m.waves.size());
-    i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.partial_mem.bytes
-        + m.scratch_mem.bytes + m.job_mem.bytes + m.plain_job_mem.bytes + m.score_mem.bytes;
-    for (const auto &w : m.waves) i.kernel_launches += w.batch->kernel_launches() + 2;
+    i.device_bytes = m.forward_mem.bytes + m.y_mem.bytes + m.partial_mem.bytes + m.scratch_mem.bytes
+        + m.job_mem.bytes + m.plain_job_mem.bytes + m.score_mem.bytes + m.epilogue_mem.bytes;
+    for (const auto &w : m.waves)
+        i.kernel_launches += w.batch->kernel_launches() + (w.unfused ? 2 : 0) + (w.fused ? 1 : 0);
+    i.fused_candidates = m.fused_count;
     i.tune_milliseconds = m.tune_ms;
     i.segment_rows = m.segment_rows;
     i.vectors_per_warp = m.vectors_per_warp ? m.vectors_per_warp : 32;

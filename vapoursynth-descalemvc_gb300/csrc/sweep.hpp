@@ -7,13 +7,17 @@
 // back to the source size and a PlaneStats-style average
 // (docs/release-benchmark.md, "getfnative" case).  Here the candidates are
 // packed into waves that fit a device-memory budget; each wave is one
-// prepared batch (every descale of the wave in one launch per pass) plus two
-// scoring launches (a fused re-upscale and error sum, then the per-candidate
-// reduction), and the waves share their buffers.  CTA sizes of every
-// launch group and the row segment of the scoring pass are chosen by timing
-// the alternatives on the first wave (autotuning).  Scores do not depend on
-// the chosen launch shapes: each candidate's arithmetic is the same whatever
-// its wave, CTA size or neighbours.
+// prepared batch (every descale of the wave in one launch per pass) and the
+// waves share their buffers.  Each candidate is descaled to HBM and scored
+// by two more launches (a re-upscale and error sum, then the reduction),
+// or, with fused scoring, where its columns pass runs the chunk-delayed
+// kernel and its operators fit the fused windows, scored inside that pass
+// (tscore_impl.cuh: its descaled plane never leaves the chip) and reduced
+// by one finalize launch.  CTA sizes of the tunable launch groups and the row segment
+// of the separate scoring pass are chosen by timing the alternatives on the
+// first wave (autotuning).  Scores do not depend on the chosen launch
+// shapes: each candidate's arithmetic is the same whatever its wave, CTA
+// size or neighbours.
 #pragma once
 
 #include "executor.hpp"
@@ -31,6 +35,12 @@ struct SweepOptions {
     std::size_t memory_budget = 0;   // bytes per wave; 0 = 32 GiB
     bool autotune = true;
     bool graph = true;
+    // Score in the columns pass where the candidate allows it (the descaled
+    // plane never reaches HBM: one wave where the separate scoring needs
+    // several); otherwise every candidate is descaled to HBM and scored by a
+    // kernel of its own (faster on the C3 sweep: the fused pass couples the
+    // scoring to the substitution's 168-register warps).
+    bool fused_scoring = false;
 };
 
 struct SweepInfo {
@@ -41,6 +51,7 @@ struct SweepInfo {
     double tune_milliseconds = 0.0;
     int segment_rows = 0;
     int vectors_per_warp = 32;        // chosen right-hand sides per warp (32 or 64)
+    int fused_candidates = 0;         // scored inside their columns pass
     BatchTuning tuning;               // chosen CTA sizes per launch group
 };
 

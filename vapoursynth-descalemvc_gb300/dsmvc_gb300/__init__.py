@@ -109,14 +109,15 @@ class StreamInfoC(C.Structure):
 
 
 class SweepOptionsC(C.Structure):
-    _fields_ = [("memory_budget", C.c_int64), ("autotune", C.c_int32), ("graph", C.c_int32)]
+    _fields_ = [("memory_budget", C.c_int64), ("autotune", C.c_int32), ("graph", C.c_int32),
+                ("fused_scoring", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SweepInfoC(C.Structure):
     _fields_ = [("candidates", C.c_int32), ("waves", C.c_int32), ("device_bytes", C.c_int64),
                 ("kernel_launches", C.c_int64), ("tune_milliseconds", C.c_double),
                 ("segment_rows", C.c_int32), ("tuned_groups", C.c_int32),
-                ("vectors_per_warp", C.c_int32)]
+                ("vectors_per_warp", C.c_int32), ("fused_candidates", C.c_int32)]
 
 
 class ServerOptionsC(C.Structure):
@@ -638,15 +639,19 @@ class PreparedBatch:
 
 class Sweep:
     """dsmvc_gb_sweep_*: candidates (h, v) descaled from one device frame,
-    re-upscaled and scored (mean absolute error), one CUDA graph per run."""
+    re-upscaled and scored (mean absolute error), one CUDA graph per run.
+    `fused_scoring`: score each candidate inside its columns pass where it
+    allows (its descaled plane never reaches HBM) instead of by a kernel of
+    its own over the descaled plane."""
 
     def __init__(self, executor: Executor, candidates: Sequence[tuple], frame_ptr: int,
                  frame_stride: int, memory_budget: int = 0, autotune: bool = True,
-                 graph: bool = True):
+                 graph: bool = True, fused_scoring: bool = False):
         n = len(candidates)
         hs = (C.c_void_p * n)(*[h.handle.value for h, _ in candidates])
         vs = (C.c_void_p * n)(*[v.handle.value for _, v in candidates])
-        opts = SweepOptionsC(int(memory_budget), 1 if autotune else 0, 1 if graph else 0)
+        opts = SweepOptionsC(int(memory_budget), 1 if autotune else 0, 1 if graph else 0,
+                             1 if fused_scoring else 0, 0)
         h = C.c_void_p()
         _check(lib().dsmvc_gb_sweep_create(executor._h, hs, vs, n, C.c_void_p(frame_ptr),
                                            int(frame_stride), C.byref(opts), C.byref(h)))
