@@ -101,24 +101,33 @@ __device__ __forceinline__ void fused_emit(const FusedTile &f, float *dr, float 
     stage_rows(vrec, ep.v_rows, r_begin, min(kScoreBatchRows, r_end - r_begin));
     __syncthreads();
     int buf = 0;
+    const int c_lo = f.c_lo, s_end = f.s_end, s_first = f.s_begin + tid;
     for (int rb = r_begin; rb < r_end; rb += kScoreBatchRows, buf ^= 1) {
         const int nb = min(kScoreBatchRows, r_end - rb);
         const float *rec = vrec + buf * (kScoreBatchRows * 12);
-        // Vertical operator: rows rb .. rb + nb of this lane's column.
+        // The frame rows of this thread's first source column, in flight
+        // during the vertical operator and the barrier.
+        float fv[kScoreBatchRows];
+        const float *fr = ep.frame + static_cast<std::int64_t>(rb) * ep.frame_stride;
+#pragma unroll
+        for (int i = 0; i < kScoreBatchRows; ++i)
+            fv[i] = i < nb && s_first < s_end ? __ldg(fr + i * ep.frame_stride + s_first) : 0.0f;
+        // Vertical operator: rows rb .. rb + nb of this lane's column (even
+        // and odd taps in two sums).
 #pragma unroll
         for (int i = 0; i < kScoreBatchRows; ++i) {
             if (i < nb) {
                 const float *ri = rec + i * 12;
                 const float *d = dr + (__float_as_int(ri[0]) - slot_row0) * 32;
-                float acc = 0.0f;
+                float a0 = 0.0f, a1 = 0.0f;
                 for (int e = 0; e < vt; e += 4) {
                     const float4 w = *reinterpret_cast<const float4 *>(ri + 4 + e);
-                    acc = fmaf(w.x, d[(e + 0) * 32], acc);
-                    acc = fmaf(w.y, d[(e + 1) * 32], acc);
-                    acc = fmaf(w.z, d[(e + 2) * 32], acc);
-                    acc = fmaf(w.w, d[(e + 3) * 32], acc);
+                    a0 = fmaf(w.x, d[(e + 0) * 32], a0);
+                    a1 = fmaf(w.y, d[(e + 1) * 32], a1);
+                    a0 = fmaf(w.z, d[(e + 2) * 32], a0);
+                    a1 = fmaf(w.w, d[(e + 3) * 32], a1);
                 }
-                vb[i * kFPitch + tid] = col_ok ? acc : 0.0f;
+                vb[i * kFPitch + tid] = col_ok ? a0 + a1 : 0.0f;
             }
         }
         __syncthreads();
@@ -128,13 +137,12 @@ __device__ __forceinline__ void fused_emit(const FusedTile &f, float *dr, float 
                        min(kScoreBatchRows, r_end - rb - kScoreBatchRows));
         // Horizontal operator and the error sums of the tile's source columns.
         float sum = 0.0f;
-        const int c_lo = f.c_lo, s_end = f.s_end;
-        for (int s = f.s_begin + tid; s < s_end; s += kScoreCtaThreads) {
+        for (int s = s_first; s < s_end; s += kScoreCtaThreads) {
             const float4 *hr = reinterpret_cast<const float4 *>(ep.h_cols + static_cast<std::int64_t>(s) * 12);
-            const float *fr = ep.frame + static_cast<std::int64_t>(rb) * ep.frame_stride + s;
-            float fv[kScoreBatchRows];
+            if (s != s_first) {
 #pragma unroll
-            for (int i = 0; i < kScoreBatchRows; ++i) fv[i] = i < nb ? __ldg(fr + i * ep.frame_stride) : 0.0f;
+                for (int i = 0; i < kScoreBatchRows; ++i) fv[i] = i < nb ? __ldg(fr + i * ep.frame_stride + s) : 0.0f;
+            }
             const float4 h0 = __ldg(hr);
             const float4 w0 = __ldg(hr + 1);
             const float4 w1 = ht > 4 ? __ldg(hr + 2) : make_float4(0, 0, 0, 0);
@@ -143,18 +151,18 @@ __device__ __forceinline__ void fused_emit(const FusedTile &f, float *dr, float 
             for (int i = 0; i < kScoreBatchRows; ++i) {
                 if (i < nb) {
                     const float *vr = v + i * kFPitch;
-                    float acc = 0.0f;
-                    acc = fmaf(w0.x, vr[0], acc);
-                    acc = fmaf(w0.y, vr[1], acc);
-                    acc = fmaf(w0.z, vr[2], acc);
-                    acc = fmaf(w0.w, vr[3], acc);
+                    float a0 = 0.0f, a1 = 0.0f;
+                    a0 = fmaf(w0.x, vr[0], a0);
+                    a1 = fmaf(w0.y, vr[1], a1);
+                    a0 = fmaf(w0.z, vr[2], a0);
+                    a1 = fmaf(w0.w, vr[3], a1);
                     if (ht > 4) {
-                        acc = fmaf(w1.x, vr[4], acc);
-                        acc = fmaf(w1.y, vr[5], acc);
-                        acc = fmaf(w1.z, vr[6], acc);
-                        acc = fmaf(w1.w, vr[7], acc);
+                        a0 = fmaf(w1.x, vr[4], a0);
+                        a1 = fmaf(w1.y, vr[5], a1);
+                        a0 = fmaf(w1.z, vr[6], a0);
+                        a1 = fmaf(w1.w, vr[7], a1);
                     }
-                    sum += fabsf(acc - fv[i]);
+                    sum += fabsf((a0 + a1) - fv[i]);
                 }
             }
         }
