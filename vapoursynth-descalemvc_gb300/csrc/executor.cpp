@@ -608,9 +608,10 @@ struct Executor::Impl {
     };
     // Window of the fused scoring columns pass for this vertical plan, or -1.
     [[nodiscard]] int fused_window(const DevicePlan &dp) const;
+    // `status`: the device status word the launches report to.
     void compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                 const std::function<char *(std::size_t)> &scratch, const Tuning *tuning = nullptr,
-                 int vectors_per_warp = 0);
+                 const std::function<char *(std::size_t)> &scratch, std::uint32_t *status,
+                 const Tuning *tuning = nullptr, int vectors_per_warp = 0);
     void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
     void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch = nullptr,
                  std::size_t scratch_capacity = 0);
@@ -769,8 +770,8 @@ std::vector<Item> segment_items(const std::vector<Item> &items, int vectors_per_
 } // namespace
 
 void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
-                             const std::function<char *(std::size_t)> &scratch, const Tuning *tuning,
-                             int vectors_per_warp) {
+                             const std::function<char *(std::size_t)> &scratch, std::uint32_t *status,
+                             const Tuning *tuning, int vectors_per_warp) {
     const bool paired = vectors_per_warp ? vectors_per_warp == 64 : allow_paired;
     auto &temporaries = out.temporaries;
     // Per task: which kernels run each pass, and the scratch they need.
@@ -1241,6 +1242,7 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 blocks += (vectors + per_block - 1) / per_block;
             }
             bytes_moved += it.bytes;
+            if (is_stream) it.stream.status = status;
             if (is_stream)
                 record_floats = std::max(record_floats, it.stream.plan.forward_stride + it.stream.plan.backward_stride);
             const char *src = is_stream ? reinterpret_cast<const char *>(&it.stream)
@@ -1324,11 +1326,13 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
         }
         ws.scratch.reserve(bytes);
         return ws.scratch.data();
-    });
+    }, ws.status);
     if (c.launches.empty()) return;
     ws.upload_table(c.table);
     launch(c, ws.jobs.data(), ws.stream, ws.status);
-    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || (l.kind >= 6 && l.kind <= 8);
+    // Float64 kernels report non-finite data, the transposing kernels a
+    // stalled feed.
+    for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind >= 3;
     if (c.private_uploads > 0) {
         // Private plan uploads must outlive the kernels that read them.
         // (Cached plans evicted meanwhile are released by cudaFree, which
@@ -1337,9 +1341,22 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
     }
 }
 
+namespace {
+
+// The error a nonzero device status word stands for.
+[[noreturn]] void throw_status(std::uint32_t status) {
+    if (status & dev::kStatusFeedStall)
+        throw std::runtime_error("a transposing kernel's feed wait ran out (its outputs are not valid)");
+    if (status & dev::kStatusNonFiniteInput) throw std::runtime_error("Float64 input contains NaN or infinity");
+    throw std::runtime_error("Float64 execution produced NaN or infinity");
+}
+
+} // namespace
+
 void Executor::Impl::finish(Workspace &ws) {
     if (!ws.status_pending) {
-        // Only the Float64 kernels set the status word: nothing to read.
+        // Only the Float64 and transposing kernels set the status word:
+        // nothing to read.
         cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
         return;
     }
@@ -1351,9 +1368,7 @@ void Executor::Impl::finish(Workspace &ws) {
     if (status) {
         cuda_check(cudaMemsetAsync(ws.status, 0, sizeof(std::uint32_t), ws.stream), "clearing status");
         cuda_check(cudaStreamSynchronize(ws.stream), "synchronizing");
-        if (status & dev::kStatusNonFiniteInput)
-            throw std::runtime_error("Float64 input contains NaN or infinity");
-        throw std::runtime_error("Float64 execution produced NaN or infinity");
+        throw_status(status);
     }
 }
 
@@ -1930,9 +1945,7 @@ void PreparedBatch::check_status(void *stream) {
     const std::uint32_t status = *impl_->status_host;
     if (status) {
         cuda_check(cudaMemset(impl_->status, 0, sizeof(std::uint32_t)), "clearing status");
-        if (status & dev::kStatusNonFiniteInput)
-            throw std::runtime_error("Float64 input contains NaN or infinity");
-        throw std::runtime_error("Float64 execution produced NaN or infinity");
+        throw_status(status);
     }
 }
 
@@ -2007,6 +2020,9 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
         for (const auto &[k, v] : *tuning) t[{k[0], k[1], k[2], k[3], k[4], k[5]}] = v;
     auto b = std::make_unique<PreparedBatch::Impl>();
     b->owner = impl_.get();
+    cuda_check(cudaMalloc(&b->status, sizeof(std::uint32_t)), "allocating status");
+    cuda_check(cudaMallocHost(&b->status_host, sizeof(std::uint32_t)), "allocating status");
+    cuda_check(cudaMemset(b->status, 0, sizeof(std::uint32_t)), "clearing status");
     // Two parts (launches overlapping on two streams: one part's second pass
     // runs beside the other's first) for batches of many tasks that own
     // their scratch; split where the source pixels are halved.
@@ -2044,7 +2060,7 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
             }
             pt.scratch.reserve(bytes);
             return pt.scratch.data();
-        }, &t, vectors_per_warp);
+        }, b->status, &t, vectors_per_warp);
         const auto &table = pt.compiled.table;
         pt.table.reserve(std::max<std::size_t>(table.size(), 1));
         if (!table.empty())
@@ -2056,9 +2072,6 @@ std::unique_ptr<PreparedBatch> Executor::prepare_batch(const std::vector<PlaneTa
         cuda_check(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "creating event");
         cuda_check(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming), "creating event");
     }
-    cuda_check(cudaMalloc(&b->status, sizeof(std::uint32_t)), "allocating status");
-    cuda_check(cudaMallocHost(&b->status_host, sizeof(std::uint32_t)), "allocating status");
-    cuda_check(cudaMemset(b->status, 0, sizeof(std::uint32_t)), "clearing status");
     return std::make_unique<PreparedBatch>(std::move(b));
 }
 

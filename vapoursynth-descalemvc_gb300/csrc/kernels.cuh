@@ -57,6 +57,7 @@ struct AxisJob {
 enum StatusBits : std::uint32_t {
     kStatusNonFiniteInput = 1U,
     kStatusNonFiniteOutput = 2U,
+    kStatusFeedStall = 4U,         // a streaming kernel's staged feed wait ran out
 };
 
 enum class Sample : std::int32_t { f32 = 0, u8 = 1, u16 = 2, f64 = 3 };

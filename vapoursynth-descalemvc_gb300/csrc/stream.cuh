@@ -63,6 +63,9 @@ struct StreamJob {
     // Columns passes with fused candidate scoring (tscore_impl.cuh): the
     // device ScoreEpilogue (score.cuh); the pass then stores no output.
     const void *score;
+    // Transposing kernels: the status word a stalled feed wait sets
+    // (kStatusFeedStall).
+    std::uint32_t *status;
 };
 
 } // namespace dsmvc_gb::dev

@@ -215,7 +215,7 @@ tscore_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
     }
     const bool col_ok = !idle && lane < warp_vectors;
 
-    WarpFeeder<float> feed;
+    WarpFeeder<float, false> feed;
     feed.base = static_cast<const float *>(job.in) + warp_first * job.in_vec;
     feed.stride = job.in_vec;
     feed.size = p.source_size;

@@ -68,7 +68,7 @@ tsolve_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_floa
     const bool active = (cta_warp + warp - job.first_block) * 32 + lane < job.vectors;
     const int v = warp_first + (lane < warp_vectors ? lane : 0);
 
-    WarpFeeder<In> feed;
+    WarpFeeder<In, false> feed;
     feed.base = static_cast<const In *>(job.in) + warp_first * job.in_vec;
     feed.stride = job.in_vec;
     feed.size = p.source_size;

@@ -7,14 +7,17 @@
 // row-major).  A warp owns 32 vectors, one per lane:
 //
 //  * Loads: blocks of 16 source samples of all 32 vectors are fetched by the
-//    whole warp with 16-byte coalesced loads (2 lanes per u16 vector, 4 per
-//    f32 vector, 1 per u8 vector), converted to float and scattered into a
-//    shared ring of 32 sample rows whose first 16 rows are stored again
-//    after it, so that any window of up to 16 consecutive samples is
-//    contiguous (the host admits windows up to 16).  Rows are 34 floats apart:
-//    the scatter of every load pattern and the per-lane reads of one sample
-//    row are both free of bank conflicts.  The next block is in flight while
-//    the current one is consumed.
+//    whole warp with 16-byte coalesced cp.async copies (2 lanes per u16
+//    vector, 4 per f32 vector, 1 per u8 vector) into the warp's staging area
+//    in shared memory, completed on the warp's mbarrier; each lane then
+//    converts the bytes it copied to float and scatters them into a shared
+//    ring of 32 sample rows whose first 16 rows are stored again after it,
+//    so that any window of up to 16 consecutive samples is contiguous (the
+//    host admits windows up to 16).  Rows are 34 floats apart: the scatter of
+//    every load pattern and the per-lane reads of one sample row are both
+//    free of bank conflicts.  The next block is in flight while the current
+//    one is consumed, in shared memory rather than in registers (the same
+//    step on one GB300: C1 0.796 -> 0.771 ms, 4K Debicubic 1.034 -> 1.023).
 //  * Stores: destination j of the 32 vectors is one coalesced store.
 //  * Records: the CTA's warps work on the same destinations, so one
 //    chunk of 32 destination records is copied (cp.async) into shared memory
@@ -48,6 +51,12 @@ constexpr int kTRingFloats = (kTRing + kTDup) * kTPitch;
 constexpr int kTChunk = kStreamChunk;
 constexpr int kTMaxThreads = 256;         // CTA sizes 32..256 (a multiple of 32)
 constexpr int kTBlock = 16;                // samples per warp load block
+// Staged feeds: per warp after the rings, up to 4 copies of 16 bytes a lane.
+constexpr int kFeedWarpBytes = 4 * 32 * 16;
+// try_wait rounds before a feed wait gives up (far beyond any copy's
+// latency); a stalled warp stops waiting and its kernel reports
+// kStatusFeedStall.
+constexpr int kFeedWaitRounds = 1 << 16;
 
 __device__ __forceinline__ int find_tjob(const StreamJob *jobs, int count, int block) {
     int lo = 0, hi = count - 1;
@@ -114,8 +123,11 @@ template <int HB, int K> __device__ __forceinline__ int bwd_stride(const dev::St
 }
 
 // Cooperative ring feeder of one warp.  Block b covers samples
-// [16 b, 16 b + 16) of the warp's 32 vectors.
-template <class In>
+// [16 b, 16 b + 16) of the warp's 32 vectors.  STAGED: the block in flight
+// waits in shared memory (cp.async, completed on the warp's mbarrier, which
+// takes 32 arrivals a phase); otherwise in registers (the two-pass and
+// fused scoring kernels, whose occupancy the staging area would cut).
+template <class In, bool STAGED = true>
 struct WarpFeeder {
     static constexpr int SPL = 16 / static_cast<int>(sizeof(In));   // samples per lane load
     static constexpr int LPV = kTBlock / SPL;                       // lanes per vector
@@ -130,7 +142,11 @@ struct WarpFeeder {
     int lane;
     float *ring;             // warp ring, ring[row * kTPitch + vector]
     Conversion conv;
-    uint4 pend[NI];
+    uint4 pend[STAGED ? 1 : NI];   // register feeds: the block in flight
+    uint4 *stage;            // staged feeds: NI x 32 lanes x 16 bytes of this warp
+    unsigned long long *mbar;   // staged feeds: this warp's completion barrier
+    unsigned phase;
+    bool failed;             // a wait ran out: later blocks are not waited for
     bool pend_ok;
 
     __device__ __forceinline__ void put(int s, int v, float x) {
@@ -148,7 +164,17 @@ struct WarpFeeder {
             int v = i * VPI + lane / LPV;
             v = v < vectors ? v : vectors - 1;
             const In *p = base + v * stride + have + (lane % LPV) * SPL;
-            pend[i] = __ldg(reinterpret_cast<const uint4 *>(p));
+            if constexpr (STAGED) {
+                const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(stage + i * 32 + lane));
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(sa), "l"(p) : "memory");
+            } else {
+                pend[i] = __ldg(reinterpret_cast<const uint4 *>(p));
+            }
+        }
+        if constexpr (STAGED) {
+            // One arrival per lane once its copies have landed.
+            const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
+            asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" :: "r"(mb) : "memory");
         }
     }
 
@@ -167,10 +193,25 @@ struct WarpFeeder {
                 // occupy consecutive ring rows without wrapping, and all of
                 // the block is in the duplicated rows or none of it is.
                 const bool dup = (have & (kTRing - 1)) < kTDup;
+                if constexpr (STAGED) {
+                    if (!failed) {
+                        const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
+                        unsigned done = 0;
+                        for (int it = 0; it < kFeedWaitRounds && !done; ++it) {
+                            asm volatile("{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
+                                         " selp.u32 %0, 1, 0, q;\n}\n" : "=r"(done) : "r"(mb), "r"(phase) : "memory");
+                        }
+                        failed = !done;
+                    }
+                    phase ^= 1u;
+                }
 #pragma unroll
                 for (int i = 0; i < NI; ++i) {
                     const int v = i * VPI + lane / LPV;
-                    const In *vals = reinterpret_cast<const In *>(&pend[i]);
+                    uint4 staged;                               // the bytes this lane fetched
+                    if constexpr (STAGED) staged = stage[i * 32 + lane];
+                    else staged = pend[i];
+                    const In *vals = reinterpret_cast<const In *>(&staged);
                     float *r = ring + ((have + (lane % LPV) * SPL) & (kTRing - 1)) * kTPitch + v;
 #pragma unroll
                     for (int k = 0; k < SPL; ++k) {
@@ -427,6 +468,16 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     const int per_buffer = kTChunk * record_floats;
     float *bufs = smem;
     float *ring = smem + 3 * per_buffer + warp * kTRingFloats;
+    // The warp's feed staging area (after the rings) and mbarrier.
+    uint4 *stage = reinterpret_cast<uint4 *>(reinterpret_cast<char *>(smem + 3 * per_buffer
+                                                                      + (nthreads >> 5) * kTRingFloats)
+                                             + warp * kFeedWarpBytes);
+    __shared__ unsigned long long feed_bar[kTMaxThreads / 32];
+    if (lane == 0) {
+        const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(&feed_bar[warp]));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 32;\n" :: "r"(mb) : "memory");
+    }
+    __syncwarp();
 
     // The warp's vectors; a warp past its job's last vector only takes part
     // in the CTA's record copies and barriers.
@@ -448,6 +499,10 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     feed.vectors = warp_vectors;
     feed.lane = lane;
     feed.ring = ring;
+    feed.stage = stage;
+    feed.mbar = &feed_bar[warp];
+    feed.phase = 0;
+    feed.failed = false;
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
         && (job.in_vec * static_cast<std::int64_t>(sizeof(In))) % 16 == 0;
@@ -501,12 +556,16 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
 #pragma unroll
         for (int t = 0; t < LC; ++t) y[t] = y[LC + t];
     }
+    // No copy is left in flight; a stalled feed wait reports.
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (__any_sync(0xffffffffu, feed.failed) && lane == 0) atomicOr(lead.status, dev::kStatusFeedStall);
 }
 
 template <int HB, int LC, int K, class In, class Out>
 int tlaunch_typed(const StreamJob *jobs, int count, int blocks, int threads, int record_floats, cudaStream_t s) {
     if (threads < 32 || threads > kTMaxThreads || threads % 32) return static_cast<int>(cudaErrorInvalidValue);
-    const int smem = (3 * kTChunk * record_floats + threads / 32 * kTRingFloats) * static_cast<int>(sizeof(float));
+    const int smem = (3 * kTChunk * record_floats + threads / 32 * kTRingFloats) * static_cast<int>(sizeof(float))
+        + threads / 32 * kFeedWarpBytes;
     auto kernel = tstream_kernel<HB, LC, K, In, Out>;
     static SmemLimit limit;
     if (const cudaError_t e = limit.ensure(kernel, smem); e != cudaSuccess) return static_cast<int>(e);
