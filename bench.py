@@ -978,6 +978,49 @@ def workload_config():
             "l2": "inputs (398 MB) larger than L2; no flush", "parallelism": "replicas"}
 
 
+def pageable_frames(ex, gb, calls, pix_step, steps):
+    """The same multi-plane call with the step's frames in ordinary
+    (pageable) host memory, one ring per direction as a frame pool would
+    hold them: as they are, and after the host block registry has
+    page-locked both rings (reported twice, within a 1 GiB limit)."""
+    total_in = sum(c[2].size for c in calls)
+    total_out = sum(c[4].size for c in calls)
+    ring_in = np.empty(total_in, np.uint16)
+    ring_out = np.empty(total_out, np.uint16)
+    planes, at_in, at_out = [], 0, 0
+    for h, v, pin, conv, pout in calls:
+        src = ring_in[at_in:at_in + pin.size].reshape(pin.shape)
+        src[...] = pin
+        dst = ring_out[at_out:at_out + pout.size].reshape(pout.shape)
+        at_in += pin.size
+        at_out += pout.size
+        planes.append((h, v, src, dst, conv))
+
+    def rate():
+        run = ex.host_planes(planes)
+        run.run()   # warm-up
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            run.run()
+        return steps * pix_step / (time.perf_counter() - t0) / 1e6
+
+    plain = rate()
+    hb = gb.host_blocks
+    owner = id(ring_in)
+    hb.set_limit(owner, 1 << 30)
+    s0 = hb.stats()
+    for _ in range(2):
+        hb.note_array(owner, ring_in)
+        hb.note_array(owner, ring_out)
+    registered = hb.covered(ring_in.ctypes.data, ring_in.nbytes) and hb.covered(ring_out.ctypes.data, ring_out.nbytes)
+    fast = rate() if registered else None
+    s1 = hb.stats()
+    hb.drop_owner(owner)
+    return {"unit": "Mpix/s", "unregistered": plain, "registered": fast,
+            "registrations": s1["registrations"] - s0["registrations"],
+            "api": "dsmvc_gb_inverse_2d_planes after dsmvc_gb_host_blocks_note_use (second use registers)"}
+
+
 def main():
     global FRAMES
     ap = argparse.ArgumentParser()
@@ -1153,6 +1196,7 @@ def main():
                 list(pool.map(call, calls))
             e2e_calls = world * args.e2e_steps * pix_step / (time.perf_counter() - t0) / 1e6
     link = link_bandwidth(h2d, d2h) if calls else None
+    pageable = pageable_frames(ex, gb, calls, pix_step * world, args.e2e_steps) if calls else None
 
     hbm, peak_kind = peaks()
     total_ms = sum(k["milliseconds"] for k in ktimes)
@@ -1185,7 +1229,8 @@ def main():
                 "per_plane_calls_16_threads": e2e_calls,
                 "link": link,
                 "link_frac": (((h2d + d2h) / (pix_step / (e2e * 1e6)) / 1e9) / link["concurrent_gbs"])
-                if link and e2e else None},
+                if link and e2e else None,
+                "pageable_frames": pageable},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,

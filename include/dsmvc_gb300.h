@@ -456,6 +456,38 @@ int dsmvc_gb_sweep_get_info(const dsmvc_gb_sweep *sweep, dsmvc_gb_sweep_info *ou
 int dsmvc_gb_sweep_profile(dsmvc_gb_sweep *sweep, void *stream, double *milliseconds);
 void dsmvc_gb_sweep_destroy(dsmvc_gb_sweep *sweep);
 
+/* Host block registry: the reference's direct block registration for its
+ * CUDA domain (include/dsmvc/host_blocks.hpp, src/host_blocks.cpp,
+ * src/vs_frame_memory.cpp).  A frame host reports the host blocks (frame
+ * pool allocations) its planes live in before each transfer; a block is
+ * page-locked (cudaHostRegister) on its second use while the owner's
+ * registered bytes stay within its limit (set_limit; 0, the default,
+ * registers nothing), after which copies from and to planes inside it run
+ * as DMA.  A block someone else page-locked counts as registered and is
+ * never unregistered here.  Owners are opaque tokens.  release must come
+ * before a block is freed; drop_owner releases all of an owner's blocks.
+ * covered tells whether a range lies in a registered block.
+ * dsmvc_gb_host_blocks_test_registrar replaces the CUDA calls (releasing
+ * everything first) for tests: 0 CUDA, 1 a fake that registers, 2 a fake
+ * that finds every block registered by someone else, 3 a fake that fails. */
+typedef struct dsmvc_gb_host_block_stats {
+    uint64_t registrations;       /* blocks registered (ours or foreign) */
+    uint64_t failures;
+    uint64_t cap_refusals;        /* second uses refused by the owner's limit */
+    uint64_t hits;                /* covered() inside a registered block */
+    uint64_t misses;
+    uint64_t released;            /* blocks unregistered by the registry */
+    uint64_t registered_bytes;    /* currently registered by the registry */
+    uint64_t peak_bytes;
+} dsmvc_gb_host_block_stats;
+int dsmvc_gb_host_blocks_set_limit(const void *owner, int64_t bytes);
+int dsmvc_gb_host_blocks_note_use(const void *owner, void *base, int64_t size);
+int dsmvc_gb_host_blocks_covered(const void *pointer, int64_t bytes, int32_t *covered);
+int dsmvc_gb_host_blocks_release(void *base, int64_t size);
+int dsmvc_gb_host_blocks_drop_owner(const void *owner);
+int dsmvc_gb_host_blocks_get_stats(dsmvc_gb_host_block_stats *out);
+int dsmvc_gb_host_blocks_test_registrar(int32_t mode);
+
 /* Request loop (continuous batching; no reference counterpart beyond its
  * synchronous per-frame calls on execution slots,
  * src/cuda/cuda_executor.cpp:1462-1503).  Requests of one or more 2D planes

@@ -28,7 +28,7 @@ NVCCFLAGS = ARCH + ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
                     "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 HOST_SOURCES = ["planner.cpp", "stream_plan.cpp", "executor.cpp", "sweep.cpp", "server.cpp",
-                "capi.cpp"]
+                "host_blocks.cpp", "capi.cpp"]
 TSTREAM2_SOURCES = [f"tstream2_hb{hb}_k{k}.cu" for hb in (1, 3, 5, 7) for k in (0, 8)]
 TSOLVE_SOURCES = ([f"tsolve_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)]
                   + [f"tsolve64_hb{hb}.cu" for hb in (1, 3, 5, 7, 9, 11)])

@@ -3,6 +3,7 @@
 #include "../../include/dsmvc_gb300.h"
 
 #include "executor.hpp"
+#include "host_blocks.hpp"
 #include "noalloc.hpp"
 #include "peak.hpp"
 #include "server.hpp"
@@ -814,5 +815,79 @@ int dsmvc_gb_server_reset_stats(dsmvc_gb_server *server) {
 }
 
 void dsmvc_gb_server_destroy(dsmvc_gb_server *server) { delete server; }
+
+} // extern "C"
+
+namespace {
+
+// Fake registrations for the registry's tests (no page-locking).
+dsmvc_gb::BlockRegistration fake_owned(void *, std::size_t) { return dsmvc_gb::BlockRegistration::owned; }
+dsmvc_gb::BlockRegistration fake_foreign(void *, std::size_t) { return dsmvc_gb::BlockRegistration::foreign; }
+dsmvc_gb::BlockRegistration fake_failed(void *, std::size_t) { return dsmvc_gb::BlockRegistration::failed; }
+void fake_unregister(void *, std::size_t) {}
+
+} // namespace
+
+extern "C" {
+
+int dsmvc_gb_host_blocks_set_limit(const void *owner, int64_t bytes) {
+    return guarded([&] {
+        if (bytes < 0) throw std::invalid_argument("negative limit");
+        dsmvc_gb::host_blocks::set_limit(owner, static_cast<std::size_t>(bytes));
+    });
+}
+
+int dsmvc_gb_host_blocks_note_use(const void *owner, void *base, int64_t size) {
+    return guarded([&] {
+        if (size < 0) throw std::invalid_argument("negative block size");
+        dsmvc_gb::host_blocks::note_use(owner, base, static_cast<std::size_t>(size));
+    });
+}
+
+int dsmvc_gb_host_blocks_covered(const void *pointer, int64_t bytes, int32_t *covered) {
+    return guarded([&] {
+        if (!covered || bytes < 0) throw std::invalid_argument("invalid range or null output");
+        *covered = dsmvc_gb::host_blocks::covered(pointer, static_cast<std::size_t>(bytes)) ? 1 : 0;
+    });
+}
+
+int dsmvc_gb_host_blocks_release(void *base, int64_t size) {
+    return guarded([&] {
+        if (size < 0) throw std::invalid_argument("negative block size");
+        dsmvc_gb::host_blocks::release_block(base, static_cast<std::size_t>(size));
+    });
+}
+
+int dsmvc_gb_host_blocks_drop_owner(const void *owner) {
+    return guarded([&] { dsmvc_gb::host_blocks::drop_owner(owner); });
+}
+
+int dsmvc_gb_host_blocks_get_stats(dsmvc_gb_host_block_stats *out) {
+    return guarded([&] {
+        if (!out) throw std::invalid_argument("output is null");
+        const auto s = dsmvc_gb::host_blocks::stats();
+        out->registrations = s.registrations;
+        out->failures = s.failures;
+        out->cap_refusals = s.cap_refusals;
+        out->hits = s.hits;
+        out->misses = s.misses;
+        out->released = s.released;
+        out->registered_bytes = s.registered_bytes;
+        out->peak_bytes = s.peak_bytes;
+    });
+}
+
+int dsmvc_gb_host_blocks_test_registrar(int32_t mode) {
+    return guarded([&] {
+        using dsmvc_gb::BlockRegistrar;
+        switch (mode) {
+        case 0: dsmvc_gb::host_blocks::set_registrar(BlockRegistrar{}); break;
+        case 1: dsmvc_gb::host_blocks::set_registrar(BlockRegistrar{fake_owned, fake_unregister}); break;
+        case 2: dsmvc_gb::host_blocks::set_registrar(BlockRegistrar{fake_foreign, fake_unregister}); break;
+        case 3: dsmvc_gb::host_blocks::set_registrar(BlockRegistrar{fake_failed, fake_unregister}); break;
+        default: throw std::invalid_argument("registrar mode must be 0..3");
+        }
+    });
+}
 
 } // extern "C"

@@ -224,6 +224,13 @@ SIGNATURES = {
     "dsmvc_gb_server_reset_stats": ([C.c_void_p], C.c_int),
     "dsmvc_gb_server_destroy": ([C.c_void_p], None),
     "dsmvc_gb_measure_fp64_peak": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
+    "dsmvc_gb_host_blocks_set_limit": ([C.c_void_p, C.c_int64], C.c_int),
+    "dsmvc_gb_host_blocks_note_use": ([C.c_void_p, C.c_void_p, C.c_int64], C.c_int),
+    "dsmvc_gb_host_blocks_covered": ([C.c_void_p, C.c_int64, C.POINTER(C.c_int32)], C.c_int),
+    "dsmvc_gb_host_blocks_release": ([C.c_void_p, C.c_int64], C.c_int),
+    "dsmvc_gb_host_blocks_drop_owner": ([C.c_void_p], C.c_int),
+    "dsmvc_gb_host_blocks_get_stats": ([C.c_void_p], C.c_int),
+    "dsmvc_gb_host_blocks_test_registrar": ([C.c_int32], C.c_int),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -392,6 +399,57 @@ def import_plan(source) -> AxisPlan:
     _check(lib().dsmvc_gb_plan_import(C.byref(a), C.byref(h)))
     req = AxisRequest(a.source_size, a.destination_size, a.active_length, a.shift, "custom")
     return AxisPlan(req, _handle=h.value)
+
+
+class HostBlockStatsC(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in ("registrations", "failures", "cap_refusals", "hits", "misses",
+                                                 "released", "registered_bytes", "peak_bytes")]
+
+
+class host_blocks:
+    """dsmvc_gb_host_blocks_*: host blocks (a frame pool's allocations)
+    page-locked on their second transfer within a per-owner byte limit, so
+    that plane copies from and to them run as DMA.  Owners are integers
+    (opaque tokens); blocks are (address, size) pairs."""
+
+    @staticmethod
+    def set_limit(owner: int, nbytes: int) -> None:
+        _check(lib().dsmvc_gb_host_blocks_set_limit(C.c_void_p(owner), int(nbytes)))
+
+    @staticmethod
+    def note_use(owner: int, base: int, size: int) -> None:
+        _check(lib().dsmvc_gb_host_blocks_note_use(C.c_void_p(owner), C.c_void_p(base), int(size)))
+
+    @staticmethod
+    def note_array(owner: int, array: np.ndarray) -> None:
+        """note_use of the memory a numpy array spans."""
+        host_blocks.note_use(owner, array.ctypes.data, array.nbytes)
+
+    @staticmethod
+    def covered(pointer: int, nbytes: int) -> bool:
+        out = C.c_int32()
+        _check(lib().dsmvc_gb_host_blocks_covered(C.c_void_p(pointer), int(nbytes), C.byref(out)))
+        return bool(out.value)
+
+    @staticmethod
+    def release(base: int, size: int) -> None:
+        _check(lib().dsmvc_gb_host_blocks_release(C.c_void_p(base), int(size)))
+
+    @staticmethod
+    def drop_owner(owner: int) -> None:
+        _check(lib().dsmvc_gb_host_blocks_drop_owner(C.c_void_p(owner)))
+
+    @staticmethod
+    def stats() -> dict:
+        out = HostBlockStatsC()
+        _check(lib().dsmvc_gb_host_blocks_get_stats(C.byref(out)))
+        return {k: getattr(out, k) for k, _ in out._fields_}
+
+    @staticmethod
+    def test_registrar(mode: int) -> None:
+        """0: CUDA; fakes for tests: 1 registers, 2 finds blocks registered
+        elsewhere, 3 fails (each switch releases every block first)."""
+        _check(lib().dsmvc_gb_host_blocks_test_registrar(int(mode)))
 
 
 def measure_fp64_peak(device: int = 0) -> float:
