@@ -448,6 +448,9 @@ struct Executor::Impl {
     // kernels in place (mapped through unified addressing) instead of being
     // staged by copies.
     bool host_direct = false;
+    // DSMVC_GB_FEED_STALL_TEST=1: the staged feeds wait for a barrier phase
+    // nothing completes (tests of the bounded wait and its status report).
+    bool feed_stall_test = false;
 
     // Optional per-launch CUDA-event timing (dsmvc_gb_profile).
     struct Record {
@@ -1242,7 +1245,10 @@ void Executor::Impl::compile(const std::vector<PlaneTask> &tasks, Compiled &out,
                 blocks += (vectors + per_block - 1) / per_block;
             }
             bytes_moved += it.bytes;
-            if (is_stream) it.stream.status = status;
+            if (is_stream) {
+                it.stream.status = status;
+                it.stream.feed_stall_test = feed_stall_test ? 1 : 0;
+            }
             if (is_stream)
                 record_floats = std::max(record_floats, it.stream.plan.forward_stride + it.stream.plan.backward_stride);
             const char *src = is_stream ? reinterpret_cast<const char *>(&it.stream)
@@ -1390,6 +1396,7 @@ Executor::Executor(int device) : impl_(std::make_unique<Impl>()) {
         impl_->f64_fused = std::string(env) != "1" && !impl_->prefer_exact;
     if (const char *env = std::getenv("DSMVC_GB_F64_REFINE")) impl_->f64_refine = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_HOST_DIRECT")) impl_->host_direct = std::string(env) == "1";
+    if (const char *env = std::getenv("DSMVC_GB_FEED_STALL_TEST")) impl_->feed_stall_test = std::string(env) == "1";
     if (const char *env = std::getenv("DSMVC_GB_PIPELINE_MB")) {
         char *end = nullptr;
         const long v = std::strtol(env, &end, 10);

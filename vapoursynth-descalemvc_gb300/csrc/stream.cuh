@@ -66,6 +66,9 @@ struct StreamJob {
     // Transposing kernels: the status word a stalled feed wait sets
     // (kStatusFeedStall).
     std::uint32_t *status;
+    // Nonzero: the staged feed waits for a barrier phase nothing completes,
+    // so that its bounded wait runs out (tests of the stall report).
+    std::int32_t feed_stall_test;
 };
 
 } // namespace dsmvc_gb::dev

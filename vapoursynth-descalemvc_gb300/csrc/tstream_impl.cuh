@@ -54,10 +54,11 @@ constexpr int kTMaxThreads = 256;         // CTA sizes 32..256 (a multiple of 32
 constexpr int kTBlock = 16;                // samples per warp load block
 // Staged feeds: per warp after the rings, up to 4 copies of 16 bytes a lane.
 constexpr int kFeedWarpBytes = 4 * 32 * 16;
-// try_wait rounds before a feed wait gives up (far beyond any copy's
-// latency); a stalled warp stops waiting and its kernel reports
-// kStatusFeedStall.
+// try_wait rounds before a feed wait gives up, each suspending at most
+// kFeedWaitSuspendNs (about 65 ms in all, far beyond any copy's latency); a
+// stalled warp stops waiting and its kernel reports kStatusFeedStall.
 constexpr int kFeedWaitRounds = 1 << 16;
+constexpr unsigned kFeedWaitSuspendNs = 1000;
 
 __device__ __forceinline__ int find_tjob(const StreamJob *jobs, int count, int block) {
     int lo = 0, hi = count - 1;
@@ -199,8 +200,9 @@ struct WarpFeeder {
                         const unsigned mb = static_cast<unsigned>(__cvta_generic_to_shared(mbar));
                         unsigned done = 0;
                         for (int it = 0; it < kFeedWaitRounds && !done; ++it) {
-                            asm volatile("{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n"
-                                         " selp.u32 %0, 1, 0, q;\n}\n" : "=r"(done) : "r"(mb), "r"(phase) : "memory");
+                            asm volatile("{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2, %3;\n"
+                                         " selp.u32 %0, 1, 0, q;\n}\n"
+                                         : "=r"(done) : "r"(mb), "r"(phase), "r"(kFeedWaitSuspendNs) : "memory");
                         }
                         failed = !done;
                     }
@@ -502,7 +504,8 @@ tstream_kernel(const StreamJob *__restrict__ jobs, int job_count, int record_flo
     feed.ring = ring;
     feed.stage = stage;
     feed.mbar = &feed_bar[warp];
-    feed.phase = 0;
+    // A stall test waits for the phase after the one the copies complete.
+    feed.phase = lead.feed_stall_test ? 1u : 0u;
     feed.failed = false;
     feed.conv = job.conv;
     feed.vec_ok = (reinterpret_cast<std::uintptr_t>(job.in) % 16 == 0)
