@@ -117,6 +117,7 @@ typedef struct dsmvc_gb_executor_stats {
     uint64_t plan_cache_misses;
     uint64_t plan_cache_evictions;
     uint64_t plan_cache_bytes;
+    uint64_t compile_reuses;      /* calls that reused their slot's compiled launches */
 } dsmvc_gb_executor_stats;
 
 /* One plane of a device-resident batch.  `horizontal`/`vertical` may be

@@ -421,6 +421,7 @@ int dsmvc_gb_executor_get_stats(dsmvc_gb_executor *executor, dsmvc_gb_executor_s
         out->plan_cache_misses = s.plan_cache_misses;
         out->plan_cache_evictions = s.plan_cache_evictions;
         out->plan_cache_bytes = s.plan_cache_bytes;
+        out->compile_reuses = s.compile_reuses;
     });
 }
 

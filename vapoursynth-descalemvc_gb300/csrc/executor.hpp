@@ -94,6 +94,9 @@ struct ExecutorStats {
     std::uint64_t plan_cache_misses = 0;
     std::uint64_t plan_cache_evictions = 0;
     std::size_t plan_cache_bytes = 0;
+    // Host calls that repeated their slot's last task list and reused its
+    // compiled launches (no routing, no plan lookups).
+    std::uint64_t compile_reuses = 0;
 };
 
 class Executor;

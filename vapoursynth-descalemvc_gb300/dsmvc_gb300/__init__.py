@@ -83,7 +83,7 @@ class ExecutorStatsC(C.Structure):
                 ("plan_uploads", C.c_uint64), ("device_plan_bytes", C.c_uint64),
                 ("workspace_bytes", C.c_uint64), ("plan_cache_hits", C.c_uint64),
                 ("plan_cache_misses", C.c_uint64), ("plan_cache_evictions", C.c_uint64),
-                ("plan_cache_bytes", C.c_uint64)]
+                ("plan_cache_bytes", C.c_uint64), ("compile_reuses", C.c_uint64)]
 
 
 class PlaneTaskC(C.Structure):
