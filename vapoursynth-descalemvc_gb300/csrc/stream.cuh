@@ -95,7 +95,7 @@ constexpr int kPairedRingPitch = 66;
 // 32 (one warp per 32 vectors).
 constexpr int kTStreamThreads = 128;   // default CTA size
 constexpr int kTResidentWarps = 16;    // resident warps per SM (128 registers a thread)
-constexpr int kMinSegmentChunks = 2;   // shortest segment, in chunks (StreamJob)
+constexpr int kMinSegmentChunks = 1;   // shortest segment, in chunks (StreamJob)
 int launch_tstream(const dev::StreamJob *jobs, int job_count, int total_blocks, int threads,
                    int half_bandwidth, int window, dev::Sample in, dev::Sample out, int record_floats,
                    void *stream);
