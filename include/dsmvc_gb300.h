@@ -414,7 +414,7 @@ int dsmvc_gb_inverse_2d_noalloc(const dsmvc_gb_plan *horizontal,
  * `fused_scoring`, inside each candidate's columns pass where the pass and
  * the operators allow it (the descaled plane never reaches HBM, the sweep
  * needs a fraction of the memory; `fused_candidates` counts them).  The
- * candidates run in waves within `memory_budget` bytes (0 = 64 GiB), one
+ * candidates run in waves within `memory_budget` bytes (0 = 32 GiB), one
  * prepared batch per wave, the whole sweep captured into one CUDA graph
  * (`graph`), with CTA sizes and the scoring row segment chosen by timing the
  * alternatives on the first wave (`autotune`).  dsmvc_gb_sweep_run enqueues

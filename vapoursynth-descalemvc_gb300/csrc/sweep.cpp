@@ -404,7 +404,7 @@ struct Sweep::Impl {
     // out each wave's descaled planes (unfused candidates), row-pass scratch
     // and partial sums.
     void plan_waves() {
-        const std::size_t budget = options.memory_budget ? options.memory_budget : (64ULL << 30);
+        const std::size_t budget = options.memory_budget ? options.memory_budget : (32ULL << 30);
         const std::size_t partials = align_up(static_cast<std::size_t>(column_tiles()) * segments(kScoreRowBlock) * 4);
         std::size_t y_bytes = 0, p_bytes = 0, s_bytes = 0;
         std::size_t y_max = 0, p_max = 0, s_max = 0;

@@ -32,7 +32,7 @@
 namespace dsmvc_gb {
 
 struct SweepOptions {
-    std::size_t memory_budget = 0;   // bytes per wave; 0 = 64 GiB
+    std::size_t memory_budget = 0;   // bytes per wave; 0 = 32 GiB
     bool autotune = true;
     bool graph = true;
     // Score in the columns pass where the candidate allows it (the descaled
