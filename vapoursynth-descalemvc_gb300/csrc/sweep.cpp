@@ -573,21 +573,22 @@ struct Sweep::Impl {
     void autotune() {
         const auto t0 = std::chrono::steady_clock::now();
         Wave &w = waves.front();
-        {
-            float best_ms = 0.0F;
-            for (const int vpw : {32, 64}) {
-                auto batch = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity, vpw);
-                const float ms = time_ms([&] { batch->launch(stream); }, 3);
-                check(cudaStreamSynchronize(stream), "synchronizing");
-                if (vpw == 32 || ms < best_ms) {
-                    best_ms = ms;
-                    vectors_per_warp = vpw;
-                }
-            }
+        // Two right-hand sides a lane only where some plan admits the paired
+        // kernels: otherwise both batches are the same launches.
+        auto single = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity, 32);
+        auto paired = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity, 64);
+        const auto paired_groups = paired->groups();
+        vectors_per_warp = 32;
+        if (std::any_of(paired_groups.begin(), paired_groups.end(), [](const BatchGroup &g) { return g.kind == 4; })) {
+            const float ms32 = time_ms([&] { single->launch(stream); }, 2);
+            const float ms64 = time_ms([&] { paired->launch(stream); }, 2);
+            check(cudaStreamSynchronize(stream), "synchronizing");
+            if (ms64 < ms32) vectors_per_warp = 64;
         }
         std::map<std::array<int, 6>, std::pair<float, int>> best;
-        const auto keys = executor->prepare_batch(w.tasks, nullptr, scratch_mem.data(), scratch_capacity,
-                                                  vectors_per_warp)->groups();
+        const auto keys = (vectors_per_warp == 64 ? paired : single)->groups();
+        single.reset();
+        paired.reset();
         // 32-thread CTAs never win on these kernels (one warp per record copy).
         for (const int threads : {64, 128, 256}) {
             BatchTuning all;
@@ -601,7 +602,7 @@ struct Sweep::Impl {
             const auto groups = batch->groups();
             for (std::size_t gi = 0; gi < groups.size(); ++gi) {
                 if (!all.count(groups[gi].key)) continue;
-                const float ms = time_ms([&] { batch->launch_group(gi, stream); }, 3);
+                const float ms = time_ms([&] { batch->launch_group(gi, stream); }, 1);
                 auto it = best.find(groups[gi].key);
                 if (it == best.end() || ms < it->second.first) best[groups[gi].key] = {ms, threads};
             }
@@ -618,7 +619,7 @@ struct Sweep::Impl {
             segment_rows = kSegments[k];
             const float ms = time_ms([&] {
                 check(launch_score_tiles(wave_jobs(w), w.unfused, w.column_blocks, span_rows(w), stream), "launching");
-            }, 3);
+            }, 1);
             if (!any || ms < best_ms) {
                 best_ms = ms;
                 any = true;
