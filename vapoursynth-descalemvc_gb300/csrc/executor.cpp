@@ -343,12 +343,18 @@ struct Workspace {
     // A kernel that may set the status word ran on this stream since the
     // status was last read.
     bool status_pending = false;
-    // The last compiled task list (Executor::Impl::Compiled, type-erased),
-    // reused while calls repeat it (same plans with their owners, pointers,
-    // strides, conversion) and the scratch has not moved.
-    std::shared_ptr<void> compiled;
-    std::vector<PlaneTask> compiled_tasks;
-    char *compiled_scratch = nullptr;
+    // The last few compiled task lists (Executor::Impl::Compiled,
+    // type-erased), most recent first, reused when a call repeats one (same
+    // plans with their owners, pointers, strides, conversion) and the
+    // scratch has not moved: a frame server alternates the luma and chroma
+    // planes of its frames through one slot.
+    struct CompiledEntry {
+        std::shared_ptr<void> compiled;
+        std::vector<PlaneTask> tasks;
+        char *scratch = nullptr;
+    };
+    static constexpr std::size_t kCompiledEntries = 4;
+    std::vector<CompiledEntry> compiled;
     std::vector<char> host_table;
     // Job tables travel through two pinned slots, each reused only after
     // its previous copy has finished; an unchanged table is not copied.
@@ -1347,14 +1353,19 @@ bool same_task(const PlaneTask &a, const PlaneTask &b) {
 
 void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch,
                              std::size_t scratch_capacity) {
-    // A call that repeats the workspace's last task list (a frame server's
-    // next frame through the same slot) reuses its compiled launches.
-    const bool reuse = !scratch && ws.compiled && ws.compiled_scratch == ws.scratch.data()
-        && ws.compiled_tasks.size() == tasks.size()
-        && std::equal(tasks.begin(), tasks.end(), ws.compiled_tasks.begin(), same_task);
+    // A call that repeats one of the workspace's recent task lists (a frame
+    // server's next frame through the same slot) reuses its compiled launches.
+    auto hit = ws.compiled.end();
+    if (!scratch) {
+        hit = std::find_if(ws.compiled.begin(), ws.compiled.end(), [&](const Workspace::CompiledEntry &e) {
+            return e.scratch == ws.scratch.data() && e.tasks.size() == tasks.size()
+                && std::equal(tasks.begin(), tasks.end(), e.tasks.begin(), same_task);
+        });
+    }
     std::shared_ptr<Compiled> held;
-    if (reuse) {
-        held = std::static_pointer_cast<Compiled>(ws.compiled);
+    if (hit != ws.compiled.end()) {
+        held = std::static_pointer_cast<Compiled>(hit->compiled);
+        std::rotate(ws.compiled.begin(), hit, hit + 1);
         std::scoped_lock lock(mutex);
         ++stats.compile_reuses;
     } else {
@@ -1368,14 +1379,17 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
             return ws.scratch.data();
         }, ws.status);
         // Only task lists whose plans all stay resident (prepared, or cached
-        // with their owners) are kept: a private upload is for one call.
-        if (!scratch && held->private_uploads == 0) {
-            ws.compiled = held;
-            ws.compiled_tasks = tasks;
-            ws.compiled_scratch = ws.scratch.data();
-        } else {
-            ws.compiled.reset();
-            ws.compiled_tasks.clear();
+        // with their owners) are kept: a private upload is for one call.  A
+        // compile may have moved the scratch: entries on the old one go.
+        if (!scratch) {
+            char *now = ws.scratch.data();
+            ws.compiled.erase(std::remove_if(ws.compiled.begin(), ws.compiled.end(),
+                                             [now](const Workspace::CompiledEntry &e) { return e.scratch != now; }),
+                              ws.compiled.end());
+            if (held->private_uploads == 0) {
+                ws.compiled.insert(ws.compiled.begin(), Workspace::CompiledEntry{held, tasks, now});
+                if (ws.compiled.size() > Workspace::kCompiledEntries) ws.compiled.pop_back();
+            }
         }
     }
     const Compiled &c = *held;
