@@ -489,6 +489,19 @@ int dsmvc_gb_host_blocks_drop_owner(const void *owner);
 int dsmvc_gb_host_blocks_get_stats(dsmvc_gb_host_block_stats *out);
 int dsmvc_gb_host_blocks_test_registrar(int32_t mode);
 
+/* One block's page-locking, for a frame host that keeps its own registry
+ * (the reference engine's, include/dsmvc/host_blocks.hpp): the CUDA
+ * domain's Registrar of the reference's backend
+ * (src/cuda/cuda_executor.cpp:1327-1361, installed at 1425-1441).
+ * dsmvc_gb_host_register page-locks [base, base + size) for this library's
+ * copies (cudaHostRegister, portable) and sets *outcome to 0 (page-locked
+ * here: the caller unregisters it), 1 (already page-locked by someone
+ * else: usable, never to be unregistered by the caller) or -1 (failed:
+ * copies from and to it stay staged by the driver; the call still returns
+ * DSMVC_GB_OK).  dsmvc_gb_host_unregister undoes an outcome of 0. */
+int dsmvc_gb_host_register(void *base, int64_t size, int32_t *outcome);
+int dsmvc_gb_host_unregister(void *base);
+
 /* Request loop (continuous batching; no reference counterpart beyond its
  * synchronous per-frame calls on execution slots,
  * src/cuda/cuda_executor.cpp:1462-1503).  Requests of one or more 2D planes

@@ -9,15 +9,20 @@
 //   adapter_check gpu     the reference plans run through the adapter class
 //                         (prepared and unprepared) give the GB300 executor's
 //                         own results bit for bit
+//   adapter_check blocks  the adapter's registrar in the engine's host block
+//                         registry page-locks a frame-pool block reported
+//                         twice (none with DSMVC_CUDA_DIRECT_IO=0)
 #include "gb300_cuda_executor.hpp"
 
 #include "dsmvc_gb300.h"
 
 #include <dsmvc/engine.hpp>
+#include <dsmvc/host_blocks.hpp>
 
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -234,6 +239,67 @@ void check_gpu() {
     std::printf("gpu ok\n");
 }
 
+// The engine's host block registry with the adapter's registrar installed:
+// a frame-pool block reported twice is page-locked (registering it again
+// finds it page-locked elsewhere), calls from and to it give the same bytes
+// as from plain memory, and dropping its owner unregisters it.  With
+// DSMVC_CUDA_DIRECT_IO=0 no registrar is installed and nothing is locked.
+void check_blocks() {
+    namespace hb = dsmvc::host_blocks;
+    const char *direct = std::getenv("DSMVC_CUDA_DIRECT_IO");
+    const bool installed = !(direct && std::string(direct) == "0") && !std::getenv("DSMVC_CUDA_HOST_TRANSFER");
+    const auto all = cases();
+    dsmvc::gb300_detail::Gb300Executor adapter;
+    expect(hb::enabled(hb::Domain::cuda) == installed, "registrar installed as requested");
+    const auto h = dsmvc::build_axis_plan(all[0].ref);
+    const auto v = dsmvc::build_axis_plan(all[1].ref);
+    const dsmvc::IntegerConversion conv{4096.0F, 1.0F / 56064.0F, 56064.0F, 4096.0F, 65535U};
+    const auto x = frame_u16(1920, 1080, 5);
+    std::vector<std::uint16_t> want(1440 * 810);
+    adapter.inverse_2d_u16(h, v, x.data(), 1920, want.data(), 1440, conv, {});
+    // One pool block holding a source frame and a destination frame.
+    std::vector<std::uint16_t> pool(x.size() + want.size());
+    const std::size_t bytes = pool.size() * sizeof(std::uint16_t);
+    std::uint16_t *out = pool.data() + x.size();
+    int token = 0;
+    const void *owner = &token;
+    hb::set_limit(owner, 64U << 20);
+    const auto s0 = hb::stats(hb::Domain::cuda);
+    for (int use = 0; use < 3; ++use) {
+        std::memcpy(pool.data(), x.data(), x.size() * sizeof(std::uint16_t));
+        std::memset(out, 0, want.size() * sizeof(std::uint16_t));
+        hb::note_use(hb::Domain::cuda, owner, pool.data(), bytes);
+        adapter.inverse_2d_u16(h, v, pool.data(), 1920, out, 1440, conv, {});
+        expect(std::memcmp(out, want.data(), want.size() * sizeof(std::uint16_t)) == 0,
+               "frames in the pool block descale alike (use " + std::to_string(use) + ")");
+    }
+    const auto s1 = hb::stats(hb::Domain::cuda);
+    const bool leased = static_cast<bool>(hb::acquire(hb::Domain::cuda, pool.data(), bytes));
+    std::int32_t outcome = -2;
+    expect(dsmvc_gb_host_register(pool.data(), static_cast<std::int64_t>(bytes), &outcome) == DSMVC_GB_OK,
+           "register call");
+    if (installed) {
+        expect(s1.registrations - s0.registrations == 1 && s1.failures == s0.failures, "one registration");
+        expect(s1.registered_bytes - s0.registered_bytes == bytes, "registered bytes");
+        expect(leased, "the block is leased");
+        expect(outcome == 1, "the block is page-locked");
+    } else {
+        expect(s1.registrations == s0.registrations && !leased, "nothing registered");
+        expect(outcome == 0, "the block is not page-locked");
+        expect(dsmvc_gb_host_unregister(pool.data()) == DSMVC_GB_OK, "unregister call");
+    }
+    hb::drop_owner(owner);
+    if (installed) {
+        expect(hb::stats(hb::Domain::cuda).released - s1.released == 1, "dropping the owner releases");
+        outcome = -2;
+        expect(dsmvc_gb_host_register(pool.data(), static_cast<std::int64_t>(bytes), &outcome) == DSMVC_GB_OK &&
+                   outcome == 0,
+               "the block is unregistered");
+        expect(dsmvc_gb_host_unregister(pool.data()) == DSMVC_GB_OK, "unregister call");
+    }
+    std::printf("blocks ok (%s)\n", installed ? "registrar installed" : "no registrar");
+}
+
 } // namespace
 
 int main(int argc, char **argv) {
@@ -241,6 +307,7 @@ int main(int argc, char **argv) {
     try {
         if (mode == "plans") check_plans();
         else if (mode == "gpu") check_gpu();
+        else if (mode == "blocks") check_blocks();
         else {
             std::printf("unknown mode %s\n", mode.c_str());
             return 2;

@@ -11,7 +11,10 @@ libdsmvc_gb300.so, and runs tests/adapter/adapter_check.cpp:
     hashes); invalid plans are refused like AxisPlan::check_valid refuses
     them;
   * GPU: reference plans run through the adapter, prepared and unprepared,
-    Float32, Float64 and u16, give the executor's own results bit for bit.
+    Float32, Float64 and u16, give the executor's own results bit for bit;
+    the adapter installs the CUDA domain's registrar in the engine's host
+    block registry (page-locking frame-pool blocks reported twice) unless
+    DSMVC_CUDA_DIRECT_IO=0.
 
 Skipped where the reference headers or the reference engine are absent."""
 import os
@@ -44,8 +47,9 @@ def adapter_check(gb, tmp_path_factory):
     return exe
 
 
-def _run(exe, mode):
-    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=600)
+def _run(exe, mode, env=None):
+    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=600,
+                       env=None if env is None else {**os.environ, **env})
     sys.stdout.write(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     return r.stdout
@@ -60,3 +64,10 @@ def test_reference_plans_import_bit_identical(adapter_check):
 def test_adapter_runs_reference_plans_like_the_executor(adapter_check):
     out = _run(adapter_check, "gpu")
     assert "gpu ok" in out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("direct_io", ["1", "0"])
+def test_adapter_registers_frame_pool_blocks(adapter_check, direct_io):
+    out = _run(adapter_check, "blocks", {"DSMVC_CUDA_DIRECT_IO": direct_io})
+    assert ("blocks ok (registrar installed)" if direct_io == "1" else "blocks ok (no registrar)") in out

@@ -5,9 +5,13 @@
 
 #include "dsmvc_gb300.h"
 
+#include <dsmvc/host_blocks.hpp>
+
+#include <cstdlib>
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <string_view>
 #include <unordered_map>
 
 namespace dsmvc::gb300_detail {
@@ -73,6 +77,48 @@ dsmvc_gb_plan *import(const AxisPlan &p) {
         "backend does not provide; use host frames");
 }
 
+// Direct transfers from and to the plugin's frame-pool blocks.  The
+// reference plugin reports its blocks to the engine's host block registry
+// (include/dsmvc/host_blocks.hpp, src/vs_frame_memory.cpp), and only while
+// a registrar is installed for the CUDA domain (vs_frame_memory.cpp:155);
+// the reference's CUDA backend installs one with its runtime
+// (src/cuda/cuda_executor.cpp:198-202, 1327-1361, 1425-1441).  This one
+// page-locks a block through dsmvc_gb_host_register, after which the GB300
+// executor's copies from and to planes inside it run as DMA.  It is
+// installed with the first executor and stays for the process's life, like
+// the reference's shared runtime; DSMVC_CUDA_DIRECT_IO=0 or an explicit
+// DSMVC_CUDA_HOST_TRANSFER leave it out, as in the reference.
+bool block_direct_io_requested() noexcept {
+    const char *direct = std::getenv("DSMVC_CUDA_DIRECT_IO");
+    return !(direct && std::string_view{direct} == "0") && !std::getenv("DSMVC_CUDA_HOST_TRANSFER");
+}
+
+host_blocks::Registered register_block(void *base, std::size_t size) noexcept {
+    std::int32_t outcome = -1;
+    if (dsmvc_gb_host_register(base, static_cast<std::int64_t>(size), &outcome) != DSMVC_GB_OK) return {};
+    if (outcome == 0) return {host_blocks::Outcome::owned, {}};
+    if (outcome == 1) return {host_blocks::Outcome::foreign, {}};
+    return {};
+}
+
+void unregister_block(void *base, std::size_t, const std::shared_ptr<void> &) noexcept {
+    (void)dsmvc_gb_host_unregister(base);
+}
+
+struct DirectBlocks {
+    bool installed = false;
+    DirectBlocks() {
+        if (!block_direct_io_requested()) return;
+        host_blocks::install(host_blocks::Domain::cuda, {&register_block, &unregister_block});
+        installed = true;
+    }
+    ~DirectBlocks() {
+        if (installed) host_blocks::uninstall(host_blocks::Domain::cuda);
+    }
+    DirectBlocks(const DirectBlocks &) = delete;
+    DirectBlocks &operator=(const DirectBlocks &) = delete;
+};
+
 } // namespace
 
 bool backend_available() noexcept { return dsmvc_gb_cuda_available() != 0; }
@@ -86,7 +132,10 @@ struct Gb300Executor::Impl {
     };
     std::unordered_map<const AxisPlan *, Prepared> prepared;
 
-    Impl() { check(dsmvc_gb_executor_create(-1, &executor)); }
+    Impl() {
+        check(dsmvc_gb_executor_create(-1, &executor));
+        static DirectBlocks direct_blocks;
+    }
     ~Impl() { dsmvc_gb_executor_destroy(executor); }
 
     // The handle of a prepared plan, or a one-call import.

@@ -12,8 +12,12 @@
 // reference's prepared set (src/cuda/cuda_executor.cpp:2490-2525).  A plan
 // that was not prepared is imported for the one call.  Errors arrive as the
 // reference's exception types: std::invalid_argument, std::length_error,
-// std::runtime_error.  GPU frames exported by a Vulkan core need graphics
-// interop, which this backend does not have: those calls throw.
+// std::runtime_error.  The first executor installs the CUDA domain's
+// registrar in the engine's host block registry (include/dsmvc/
+// host_blocks.hpp), as the reference's CUDA runtime does, so that the
+// plugin's frame-pool blocks are page-locked for direct transfers.  GPU
+// frames exported by a Vulkan core need graphics interop, which this
+// backend does not have: those calls throw.
 #pragma once
 
 #include <dsmvc/engine.hpp>

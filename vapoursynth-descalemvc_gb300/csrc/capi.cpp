@@ -891,4 +891,18 @@ int dsmvc_gb_host_blocks_test_registrar(int32_t mode) {
     });
 }
 
+int dsmvc_gb_host_register(void *base, int64_t size, int32_t *outcome) {
+    return guarded([&] {
+        if (!base || size <= 0 || !outcome) throw std::invalid_argument("invalid block or null output");
+        *outcome = static_cast<int32_t>(dsmvc_gb::host_blocks::cuda_register(base, static_cast<std::size_t>(size)));
+    });
+}
+
+int dsmvc_gb_host_unregister(void *base) {
+    return guarded([&] {
+        if (!base) throw std::invalid_argument("block is null");
+        dsmvc_gb::host_blocks::cuda_unregister(base, 0);
+    });
+}
+
 } // extern "C"

@@ -10,7 +10,7 @@
 #include <unordered_map>
 
 namespace dsmvc_gb {
-namespace {
+namespace host_blocks {
 
 BlockRegistration cuda_register(void *base, std::size_t size) {
     const cudaError_t e = cudaHostRegister(base, size, cudaHostRegisterPortable);
@@ -22,6 +22,13 @@ BlockRegistration cuda_register(void *base, std::size_t size) {
 void cuda_unregister(void *base, std::size_t) {
     if (cudaHostUnregister(base) != cudaSuccess) cudaGetLastError();
 }
+
+} // namespace host_blocks
+
+namespace {
+
+using host_blocks::cuda_register;
+using host_blocks::cuda_unregister;
 
 enum class State { seen, registering, registered, failed };
 

@@ -55,6 +55,10 @@ void drop_owner(const void *owner);
 // Replaces the registration calls (everything registered is released first);
 // a registrar with null calls restores CUDA's.
 void set_registrar(const BlockRegistrar &registrar);
+// CUDA's registration of one block, outside the registry (for a frame host
+// that keeps its own).
+[[nodiscard]] BlockRegistration cuda_register(void *base, std::size_t size);
+void cuda_unregister(void *base, std::size_t size);
 
 } // namespace host_blocks
 } // namespace dsmvc_gb

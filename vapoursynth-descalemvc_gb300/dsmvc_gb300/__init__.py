@@ -231,6 +231,8 @@ SIGNATURES = {
     "dsmvc_gb_host_blocks_drop_owner": ([C.c_void_p], C.c_int),
     "dsmvc_gb_host_blocks_get_stats": ([C.c_void_p], C.c_int),
     "dsmvc_gb_host_blocks_test_registrar": ([C.c_int32], C.c_int),
+    "dsmvc_gb_host_register": ([C.c_void_p, C.c_int64, C.POINTER(C.c_int32)], C.c_int),
+    "dsmvc_gb_host_unregister": ([C.c_void_p], C.c_int),
     "dsmvc_gb_profile": ([C.c_void_p, C.c_int32], C.c_int),
     "dsmvc_gb_profile_read": ([C.c_void_p, C.POINTER(KernelTimeC), C.c_int32,
                                C.POINTER(C.c_int32)], C.c_int),
@@ -450,6 +452,18 @@ class host_blocks:
         """0: CUDA; fakes for tests: 1 registers, 2 finds blocks registered
         elsewhere, 3 fails (each switch releases every block first)."""
         _check(lib().dsmvc_gb_host_blocks_test_registrar(int(mode)))
+
+    @staticmethod
+    def register(base: int, size: int) -> int:
+        """Page-locks one block outside the registry (dsmvc_gb_host_register):
+        0 page-locked here, 1 already page-locked elsewhere, -1 failed."""
+        out = C.c_int32()
+        _check(lib().dsmvc_gb_host_register(C.c_void_p(base), int(size), C.byref(out)))
+        return out.value
+
+    @staticmethod
+    def unregister(base: int) -> None:
+        _check(lib().dsmvc_gb_host_unregister(C.c_void_p(base)))
 
 
 def measure_fp64_peak(device: int = 0) -> float:
