@@ -42,9 +42,12 @@ __device__ __forceinline__ float tap_run(const float *__restrict__ y, const floa
 template <int N>
 __device__ __forceinline__ void row_pass(float *z, const float *y, std::int64_t ys, int nj, bool run,
                                          const float (&w)[8], const int (&c)[8]) {
+    // Four rows' loads in flight at a time.
     if (run) {
+
         for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_run<N>(y + jj * ys, w);
     } else {
+
         for (int jj = 0; jj < nj; ++jj) z[jj * kScoreThreads] = tap_sum<N>(y + jj * ys, w, c);
     }
 }
@@ -65,7 +68,9 @@ __device__ __forceinline__ float col_run(const float2 *we, const char *zb) {
 // candidate: the row-pass values Z[j][s] = sum_c A_h[s, c] Y[j][c] of the
 // rows j the segment needs are computed into shared memory, then each
 // source row r of the segment is sum_j A_v[r, j] Z[j][s], compared with the
-// frame.  Errors are summed per block of kScoreRowBlock rows.  Both passes
+// frame.  Errors are summed per block of kScoreRowBlock rows (each block's
+// warp sums wait in shared memory; the segment's blocks are reduced
+// together after its last, one barrier pair a segment).  Both passes
 // run exact-length unrolled sums, with immediate offsets where a column's
 // (row's) entries are consecutive, as they are away from the borders; the
 // segment's A_v entries sit in shared memory as (weight, byte offset of the
@@ -74,7 +79,8 @@ __device__ __forceinline__ float col_run(const float2 *we, const char *zb) {
 __global__ void __launch_bounds__(kScoreThreads)
 score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     extern __shared__ float zt[];                  // [rows of the segment's span][kScoreThreads]
-    __shared__ float warp_sums[kScoreThreads / 32];
+    constexpr int kWarps = kScoreThreads / 32, kPendingBlocks = 16;
+    __shared__ float warp_sums[kPendingBlocks * kWarps];   // per pending row block, per warp
     __shared__ float2 seg_e[kScoreSegmentEntries]; // (weight, byte offset of the staged row, as bits)
     __shared__ int4 seg_r[kScoreMaxSegmentRows];   // (first entry, count, first offset, consecutive)
     __shared__ int span_lo[kScoreThreads / 32], span_hi[kScoreThreads / 32];
@@ -174,54 +180,73 @@ score_tiles_kernel(const ScoreJob *__restrict__ jobs, int count) {
     const char *zb = reinterpret_cast<const char *>(zt + tid);
     const int row_blocks = (job.height + kScoreRowBlock - 1) / kScoreRowBlock;
     const int seg_blocks = job.segment_rows / kScoreRowBlock;
-    for (int rb = segment * seg_blocks; rb < min(row_blocks, (segment + 1) * seg_blocks); ++rb) {
+    const int rb_end = min(row_blocks, (segment + 1) * seg_blocks);
+    int pending = 0;
+    for (int rb = segment * seg_blocks; rb < rb_end; ++rb) {
         const int ra = rb * kScoreRowBlock, rz = min(job.height, ra + kScoreRowBlock);
         float sum = 0.0f;
         if (s < job.width) {
-            const float *fr = f + static_cast<std::int64_t>(ra) * job.frame_stride;
-            for (int r = ra; r < rz; ++r, fr += job.frame_stride) {
-                float acc = 0.0f;
-                if (staged) {
-                    const int4 h = seg_r[r - r0];
-                    const float2 *we = seg_e + h.x;
-                    const char *zr = zb + h.z;
-                    if (h.w) {
-                        switch (h.y) {
-                        case 1: acc = col_run<1>(we, zr); break;
-                        case 2: acc = col_run<2>(we, zr); break;
-                        case 3: acc = col_run<3>(we, zr); break;
-                        case 4: acc = col_run<4>(we, zr); break;
-                        case 5: acc = col_run<5>(we, zr); break;
-                        case 6: acc = col_run<6>(we, zr); break;
-                        case 7: acc = col_run<7>(we, zr); break;
-                        case 8: acc = col_run<8>(we, zr); break;
-                        default:
+            // Two rows at a time, both frame samples loaded first (more
+            // rows at once spill at this kernel's 64 registers).
+            constexpr int kFetch = 2;
+            for (int rf = ra; rf < rz; rf += kFetch) {
+                const float *fr = f + static_cast<std::int64_t>(rf) * job.frame_stride;
+                float fv[kFetch];
+#pragma unroll
+                for (int k = 0; k < kFetch; ++k)
+                    fv[k] = rf + k < rz ? __ldg(fr + static_cast<std::int64_t>(k) * job.frame_stride) : 0.0f;
+#pragma unroll
+                for (int k = 0; k < kFetch; ++k) {
+                    const int r = rf + k;
+                    if (r >= rz) continue;
+                    float acc = 0.0f;
+                    if (staged) {
+                        const int4 h = seg_r[r - r0];
+                        const float2 *we = seg_e + h.x;
+                        const char *zr = zb + h.z;
+                        if (h.w) {
+                            switch (h.y) {
+                            case 1: acc = col_run<1>(we, zr); break;
+                            case 2: acc = col_run<2>(we, zr); break;
+                            case 3: acc = col_run<3>(we, zr); break;
+                            case 4: acc = col_run<4>(we, zr); break;
+                            case 5: acc = col_run<5>(we, zr); break;
+                            case 6: acc = col_run<6>(we, zr); break;
+                            case 7: acc = col_run<7>(we, zr); break;
+                            case 8: acc = col_run<8>(we, zr); break;
+                            default:
+                                for (int e = 0; e < h.y; ++e)
+                                    acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zr + e * kScoreThreads * 4), acc);
+                                break;
+                            }
+                        } else {
                             for (int e = 0; e < h.y; ++e)
-                                acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zr + e * kScoreThreads * 4), acc);
-                            break;
+                                acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zb + __float_as_int(we[e].y)), acc);
                         }
                     } else {
-                        for (int e = 0; e < h.y; ++e)
-                            acc = fmaf(we[e].x, *reinterpret_cast<const float *>(zb + __float_as_int(we[e].y)), acc);
+                        const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
+                        for (std::uint32_t e = e0; e < e1; ++e)
+                            acc = fmaf(job.v.weights[e], zt[(job.v.indices[e] - j_lo) * kScoreThreads + tid], acc);
                     }
-                } else {
-                    const std::uint32_t e0 = job.v.offsets[r], e1 = job.v.offsets[r + 1];
-                    for (std::uint32_t e = e0; e < e1; ++e)
-                        acc = fmaf(job.v.weights[e], zt[(job.v.indices[e] - j_lo) * kScoreThreads + tid], acc);
+                    sum += fabsf(acc - fv[k]);
                 }
-                sum += fabsf(acc - *fr);
             }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-        if (lane == 0) warp_sums[warp] = sum;
-        __syncthreads();
-        if (tid == 0) {
-            float total = 0.0f;
-            for (int w = 0; w < kScoreThreads / 32; ++w) total += warp_sums[w];
-            job.partials[static_cast<std::int64_t>(rb) * job.column_tiles + tile] = total;
+        if (lane == 0) warp_sums[pending * kWarps + warp] = sum;
+        // The pending blocks' sums, one thread a block, after the last
+        // block of the segment (or when the buffer is full).
+        if (++pending == kPendingBlocks || rb + 1 == rb_end) {
+            __syncthreads();
+            if (tid < pending) {
+                float total = 0.0f;
+                for (int w = 0; w < kWarps; ++w) total += warp_sums[tid * kWarps + w];
+                job.partials[static_cast<std::int64_t>(rb + 1 - pending + tid) * job.column_tiles + tile] = total;
+            }
+            __syncthreads();
+            pending = 0;
         }
-        __syncthreads();
     }
 }
 
