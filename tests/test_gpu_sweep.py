@@ -158,3 +158,26 @@ def test_fused_scoring_in_a_prepared_batch(gb, whole_executor, setup):
                           fused_scoring=True)
     assert info["waves"] == len(pairs)
     assert np.array_equal(one, waved)
+
+
+def test_sweep_odd_frame_sizes_match_oracle(gb, executor):
+    """An odd frame height (the last scoring row block holds 7 rows, the last
+    row pair one) and an odd width (a partial column tile): scores match
+    the oracle like the even-sized sweep's, and the graph-captured
+    autotuned run agrees within 1e-6 relative (segments may split
+    differently under other launch shapes)."""
+    torch = pytest.importorskip("torch")
+    from dsmvc_gb300 import synthetic
+    width, height, base_h = 161, 87, 65
+    frame = synthetic.gray_frame(width, height, synthetic.sweep_width(base_h, width / height), base_h, seed=5)
+    cands = synthetic.native_resolution_candidates(width, height, [51, 58, 65, 73])
+    reqs = [r for c in cands for r in (c[3], c[4])]
+    plans = gb.build_plans(reqs, threads=4)
+    pairs = [(plans[2 * i], plans[2 * i + 1]) for i in range(len(cands))]
+    dframe = torch.from_numpy(frame).cuda()
+    got, _ = _scores(gb, executor, dframe, pairs, autotune=False, graph=False)
+    tuned, _ = _scores(gb, executor, dframe, pairs, autotune=True, graph=True)
+    for i, c in enumerate(cands):
+        want = _oracle_score(frame, c[3], c[4])
+        assert abs(got[i] - want) <= 2e-5 + 1e-3 * abs(want), (c[:3], got[i], want)
+    assert np.max(np.abs(tuned - got) / np.abs(got)) <= 1e-6
