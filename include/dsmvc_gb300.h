@@ -322,8 +322,9 @@ typedef struct dsmvc_gb_host_plane {
 /* Synchronous host-frame call over many planes (frames x planes; no
  * reference counterpart beyond one inverse_2d call per plane): the planes
  * travel in groups of about DSMVC_GB_PIPELINE_MB (default 96) MiB of input
- * and output through three streams, so the upload of one group, the kernels
- * of the previous group and the download of the one before overlap.  Each
+ * and output (uploads in order on one stream, kernels on four workspace
+ * streams, downloads in order on another), so the upload of one group, the
+ * kernels of the previous group and the download of the one before overlap.  Each
  * output equals the per-plane call's.  Host buffers should be pinned for the
  * copies to overlap.  Float64 non-finite data in any plane fails the call. */
 int dsmvc_gb_inverse_2d_planes(dsmvc_gb_executor *executor,

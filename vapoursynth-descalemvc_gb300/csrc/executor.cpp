@@ -348,10 +348,13 @@ struct Workspace {
     // plans with their owners, pointers, strides, conversion) and the
     // scratch has not moved: a frame server alternates the luma and chroma
     // planes of its frames through one slot.
+    // Each entry keeps its job table on the device, copied once: a repeated
+    // call launches with no copy.
     struct CompiledEntry {
         std::shared_ptr<void> compiled;
         std::vector<PlaneTask> tasks;
         char *scratch = nullptr;
+        std::unique_ptr<DeviceBuffer> table;
     };
     static constexpr std::size_t kCompiledEntries = 4;
     std::vector<CompiledEntry> compiled;
@@ -364,8 +367,13 @@ struct Workspace {
     int pinned_next = 0;
     std::vector<char> device_table;   // what ws.jobs holds
 
-    void upload_table(const std::vector<char> &table) {
-        if (table == device_table) return;
+    // Copies `table` into `dst` through a pinned slot, on `copies` (the
+    // workspace's own stream by default; the caller orders the kernels after
+    // it).  `dst` is not in use by kernels still to run on that stream's
+    // side: the copy follows them in stream order.
+    void copy_table(DeviceBuffer &dst, const std::vector<char> &table, cudaStream_t copies) {
+        const cudaStream_t s = copies ? copies : stream;
+        dst.reserve(table.size());
         const int k = pinned_next;
         pinned_next ^= 1;
         if (pinned_done[k]) cuda_check(cudaEventSynchronize(pinned_done[k]), "waiting for a job table slot");
@@ -377,11 +385,23 @@ struct Workspace {
             pinned_bytes[k] = table.size();
         }
         std::memcpy(pinned[k], table.data(), table.size());
-        jobs.reserve(table.size());
-        cuda_check(cudaMemcpyAsync(jobs.data(), pinned[k], table.size(), cudaMemcpyHostToDevice, stream),
+        cuda_check(cudaMemcpyAsync(dst.data(), pinned[k], table.size(), cudaMemcpyHostToDevice, s),
                    "uploading job table");
-        cuda_check(cudaEventRecord(pinned_done[k], stream), "recording event");
+        cuda_check(cudaEventRecord(pinned_done[k], s), "recording event");
+    }
+    // The shared job table `jobs` for task lists not kept in `compiled`.
+    void upload_table(const std::vector<char> &table, cudaStream_t copies = nullptr) {
+        if (table == device_table) return;
+        copy_table(jobs, table, copies);
         device_table = table;
+    }
+
+    // The workspace's stream waits for the work issued so far on `copies`.
+    cudaEvent_t copies_done = nullptr;
+    void follow(cudaStream_t copies) {
+        if (!copies_done) cuda_check(cudaEventCreateWithFlags(&copies_done, cudaEventDisableTiming), "creating event");
+        cuda_check(cudaEventRecord(copies_done, copies), "recording event");
+        cuda_check(cudaStreamWaitEvent(stream, copies_done, 0), "ordering kernels");
     }
 
     explicit Workspace(cudaStream_t s) : stream(s) {
@@ -406,7 +426,44 @@ struct Workspace {
             if (pinned_done[k]) cudaEventDestroy(pinned_done[k]);
         }
         if (status_host) cudaFreeHost(status_host);
+        if (copies_done) cudaEventDestroy(copies_done);
         if (owns_stream) cudaStreamDestroy(stream);
+    }
+};
+
+// Workspaces of the multi-plane host call: a group's upload waits for the
+// downloads of the group kPipeDepth before it (three left the last group of
+// 64 YUV420P16 frames waiting 0.1 ms for one).
+constexpr std::size_t kPipeDepth = 4;
+
+// The multi-plane host call's copy streams: every upload in issue order on
+// one stream, every download on another, linked to the workspaces' kernels
+// by events (one set per workspace).  Copies issued on the workspaces' own
+// streams ran concurrently, shared the link and finished out of order, so
+// each group's kernels started late (64 YUV420P16 frames 1080p -> 810p:
+// 2.45 ms a call, the last group waiting 0.11 ms for its workspace).
+struct CopyLanes {
+    cudaStream_t up = nullptr, down = nullptr;
+    std::array<cudaEvent_t, kPipeDepth> computed{}, downloaded{};
+
+    void create() {
+        for (cudaStream_t *s : {&up, &down})
+            if (!*s) cuda_check(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking), "creating stream");
+        for (auto *set : {&computed, &downloaded})
+            for (auto &e : *set)
+                if (!e) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "creating event");
+    }
+    void synchronize() const {
+        for (cudaStream_t s : {up, down})
+            if (s) cudaStreamSynchronize(s);
+    }
+    ~CopyLanes() {
+        synchronize();
+        for (auto *set : {&computed, &downloaded})
+            for (auto e : *set)
+                if (e) cudaEventDestroy(e);
+        for (cudaStream_t s : {up, down})
+            if (s) cudaStreamDestroy(s);
     }
 };
 
@@ -453,10 +510,12 @@ struct Executor::Impl {
     std::condition_variable slot_free;
     std::map<cudaStream_t, std::unique_ptr<Workspace>> stream_spaces;
     ExecutorStats stats;
-    // Multi-plane host calls: three workspaces with their own streams, one
-    // such call at a time.
+    // Multi-plane host calls: kPipeDepth workspaces whose kernels run on
+    // their own streams, the copies on two shared ones; one such call at a
+    // time.
     std::mutex pipe_mutex;
-    std::array<std::unique_ptr<Workspace>, 3> pipe;
+    std::array<std::unique_ptr<Workspace>, kPipeDepth> pipe;
+    CopyLanes pipe_copies;   // destroyed first: its streams wait for their copies
     std::size_t pipe_group_bytes = 96ULL << 20;
     // DSMVC_GB_HOST_DIRECT=1: planes of the multi-plane host call whose
     // buffers are page-locked host memory are read and written by the
@@ -631,8 +690,10 @@ struct Executor::Impl {
                  const std::function<char *(std::size_t)> &scratch, std::uint32_t *status,
                  const Tuning *tuning = nullptr, int vectors_per_warp = 0);
     void launch(const Compiled &c, const char *device_table, cudaStream_t stream, std::uint32_t *status);
+    // `copies`: a stream holding the tasks' input copies; the job table is
+    // copied behind them there and the kernels wait for both.
     void enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch = nullptr,
-                 std::size_t scratch_capacity = 0);
+                 std::size_t scratch_capacity = 0, cudaStream_t copies = nullptr);
     void finish(Workspace &ws);
 };
 
@@ -1352,7 +1413,7 @@ bool same_task(const PlaneTask &a, const PlaneTask &b) {
 } // namespace
 
 void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks, char *scratch,
-                             std::size_t scratch_capacity) {
+                             std::size_t scratch_capacity, cudaStream_t copies) {
     // A call that repeats one of the workspace's recent task lists (a frame
     // server's next frame through the same slot) reuses its compiled launches.
     auto hit = ws.compiled.end();
@@ -1363,9 +1424,11 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
         });
     }
     std::shared_ptr<Compiled> held;
+    const char *device_table = nullptr;
     if (hit != ws.compiled.end()) {
         held = std::static_pointer_cast<Compiled>(hit->compiled);
         std::rotate(ws.compiled.begin(), hit, hit + 1);
+        device_table = ws.compiled.front().table->data();
         std::scoped_lock lock(mutex);
         ++stats.compile_reuses;
     } else {
@@ -1386,16 +1449,29 @@ void Executor::Impl::enqueue(Workspace &ws, const std::vector<PlaneTask> &tasks,
             ws.compiled.erase(std::remove_if(ws.compiled.begin(), ws.compiled.end(),
                                              [now](const Workspace::CompiledEntry &e) { return e.scratch != now; }),
                               ws.compiled.end());
-            if (held->private_uploads == 0) {
-                ws.compiled.insert(ws.compiled.begin(), Workspace::CompiledEntry{held, tasks, now});
-                if (ws.compiled.size() > Workspace::kCompiledEntries) ws.compiled.pop_back();
+            if (held->private_uploads == 0 && !held->launches.empty()) {
+                // The least recent entry's table buffer is reused (freeing
+                // device memory would wait for the whole device).
+                std::unique_ptr<DeviceBuffer> table;
+                if (ws.compiled.size() >= Workspace::kCompiledEntries) {
+                    table = std::move(ws.compiled.back().table);
+                    ws.compiled.pop_back();
+                }
+                if (!table) table = std::make_unique<DeviceBuffer>();
+                ws.copy_table(*table, held->table, copies);
+                ws.compiled.insert(ws.compiled.begin(), Workspace::CompiledEntry{held, tasks, now, std::move(table)});
+                device_table = ws.compiled.front().table->data();
             }
         }
     }
     const Compiled &c = *held;
+    if (!device_table && !c.launches.empty()) {
+        ws.upload_table(c.table, copies);
+        device_table = ws.jobs.data();
+    }
+    if (copies) ws.follow(copies);
     if (c.launches.empty()) return;
-    ws.upload_table(c.table);
-    launch(c, ws.jobs.data(), ws.stream, ws.status);
+    launch(c, device_table, ws.stream, ws.status);
     // Float64 kernels report non-finite data, the transposing kernels a
     // stalled feed.
     for (const auto &l : c.launches) ws.status_pending |= l.kind == 1 || l.kind >= 3;
@@ -1719,6 +1795,8 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
         if (!ws) ws = std::make_unique<Workspace>(nullptr);
         ws->staging.reserve(most + kAlign);
     }
+    CopyLanes &lanes = impl_->pipe_copies;
+    lanes.create();
     // A group's staging holds its inputs back to back, then its outputs back
     // to back, each at a 16-byte boundary.  Planes whose rows are contiguous
     // on the host and whose host buffers follow one another exactly (a frame
@@ -1764,8 +1842,13 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
     std::size_t used = 0;
     try {
         for (std::size_t g = 0; g < groups.size(); ++g) {
-            Workspace &ws = *impl_->pipe[g % impl_->pipe.size()];
-            used = std::max(used, g % impl_->pipe.size() + 1);
+            const std::size_t w = g % impl_->pipe.size();
+            Workspace &ws = *impl_->pipe[w];
+            used = std::max(used, w + 1);
+            // The workspace's staging is free once its previous group's
+            // downloads are done (which followed that group's kernels).
+            if (g >= impl_->pipe.size())
+                cuda_check(cudaStreamWaitEvent(lanes.up, lanes.downloaded[w], 0), "ordering uploads");
             std::size_t in_total = 0;
             for (std::size_t i = groups[g].first; i < groups[g].second; ++i)
                 if (!direct_in[i]) in_total += pack(in_bytes(planes[i]));
@@ -1789,11 +1872,11 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
                     t.input_stride = p.input_stride;
                 } else {
                     if (static_cast<std::size_t>(p.input_stride) * es == in_row(p)) {
-                        extend(run, p.input, din, in_bytes(p), cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                        extend(run, p.input, din, in_bytes(p), cudaMemcpyHostToDevice, lanes.up, "uploading planes");
                     } else {
-                        flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
+                        flush(run, cudaMemcpyHostToDevice, lanes.up, "uploading planes");
                         cuda_check(copy_plane(din, in_row(p), p.input, p.input_stride * es, in_row(p),
-                                              p.vertical->source_size, cudaMemcpyHostToDevice, ws.stream),
+                                              p.vertical->source_size, cudaMemcpyHostToDevice, lanes.up),
                                    "uploading plane");
                     }
                     t.input = din;
@@ -1812,29 +1895,38 @@ void Executor::inverse_2d_planes(const std::vector<HostPlane> &planes, std::size
                 }
                 tasks.push_back(t);
             }
-            flush(run, cudaMemcpyHostToDevice, ws.stream, "uploading planes");
-            impl_->enqueue(ws, tasks);
+            flush(run, cudaMemcpyHostToDevice, lanes.up, "uploading planes");
+            // The job table follows the planes on the upload stream (on the
+            // workspace's stream it queued behind later groups' uploads).
+            impl_->enqueue(ws, tasks, nullptr, 0, lanes.up);
+            cuda_check(cudaEventRecord(lanes.computed[w], ws.stream), "recording event");
+            cuda_check(cudaStreamWaitEvent(lanes.down, lanes.computed[w], 0), "ordering downloads");
             for (std::size_t i = groups[g].first, k = 0; i < groups[g].second; ++i, ++k) {
                 if (!outs[k]) {
-                    flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
+                    flush(run, cudaMemcpyDeviceToHost, lanes.down, "downloading planes");
                     continue;
                 }
                 const HostPlane &p = planes[i];
                 const std::size_t es = sample_bytes(p.sample);
                 if (static_cast<std::size_t>(p.output_stride) * es == out_row(p)) {
-                    extend(run, p.output, outs[k], out_bytes(p), cudaMemcpyDeviceToHost, ws.stream,
+                    extend(run, p.output, outs[k], out_bytes(p), cudaMemcpyDeviceToHost, lanes.down,
                            "downloading planes");
                 } else {
-                    flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
+                    flush(run, cudaMemcpyDeviceToHost, lanes.down, "downloading planes");
                     cuda_check(copy_plane(p.output, p.output_stride * es, outs[k], out_row(p), out_row(p),
-                                          p.vertical->destination_size, cudaMemcpyDeviceToHost, ws.stream),
+                                          p.vertical->destination_size, cudaMemcpyDeviceToHost, lanes.down),
                                "downloading plane");
                 }
             }
-            flush(run, cudaMemcpyDeviceToHost, ws.stream, "downloading planes");
+            flush(run, cudaMemcpyDeviceToHost, lanes.down, "downloading planes");
+            cuda_check(cudaEventRecord(lanes.downloaded[w], lanes.down), "recording event");
         }
+        // Every group's downloads followed its kernels, which followed its
+        // uploads: the download stream is the last to finish.
+        cuda_check(cudaStreamSynchronize(lanes.down), "synchronizing");
         for (std::size_t k = 0; k < used; ++k) impl_->finish(*impl_->pipe[k]);
     } catch (...) {
+        lanes.synchronize();
         for (std::size_t k = 0; k < used; ++k) cudaStreamSynchronize(impl_->pipe[k]->stream);
         throw;
     }

@@ -182,9 +182,11 @@ public:
 
     // Synchronous host-frame call over many planes (frames x planes): the
     // planes go in groups of about `group_bytes` of input and output
-    // (0: DSMVC_GB_PIPELINE_MB, default 96 MiB) through three streams, so the
-    // upload of one group, the kernels of the previous one and the download
-    // of the one before overlap.  Results equal per-plane inverse_2d calls.
+    // (0: DSMVC_GB_PIPELINE_MB, default 96 MiB): uploads in order on one
+    // stream, each group's kernels on one of four workspace streams,
+    // downloads in order on another stream, so the upload of one group, the
+    // kernels of the previous one and the download of the one before
+    // overlap.  Results equal per-plane inverse_2d calls.
     // Host buffers should be pinned for the copies to overlap.
     void inverse_2d_planes(const std::vector<HostPlane> &planes, std::size_t group_bytes = 0);
 
