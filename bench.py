@@ -14,7 +14,8 @@ so no flush is needed between steps.
 Prints one JSON line (rank 0).  `value` is Mpix/s of source pixels summed
 over planes with inputs resident in HBM; `e2e` is the same metric through
 the synchronous host-frame C-ABI calls (pinned host planes, copies inside
-the timed region); `roofline` divides the algorithmic bytes of a step (the
+the timed region), beside it the same step as per-plane calls from 16
+Python threads and from 16 C++ threads (bench_host_calls.cpp); `roofline` divides the algorithmic bytes of a step (the
 sum over its kernel launches, each counted by the executor) by the step's
 CUDA-event time: the prepared batch runs as two parts on two streams whose
 kernels overlap, so the per-kernel event times (also reported, as shares)
@@ -1021,6 +1022,47 @@ def pageable_frames(ex, gb, calls, pix_step, steps):
             "api": "dsmvc_gb_inverse_2d_planes after dsmvc_gb_host_blocks_note_use (second use registers)"}
 
 
+def native_host_calls(gb, reqs, convs, frames, threads=16, steps=10):
+    """The per-plane synchronous calls of the step from `threads` C++
+    threads straight into the C ABI (bench_host_calls.cpp, compiled here
+    against the in-tree library): the plugin's calling pattern with no
+    Python between the threads and the library.  The Python-thread figure
+    beside it is bound by the binding's own per-call time, which holds the
+    interpreter lock."""
+    import shutil
+    import tempfile
+    here = os.path.dirname(os.path.abspath(__file__))
+    gxx = shutil.which("g++")
+    if not gxx:
+        return {"unavailable": "no g++ on this host"}
+    libdir = os.path.dirname(gb.LIB_PATH)
+
+    def req_arg(q):
+        c = q.to_c()
+        return ",".join(repr(getattr(c, f)) for f, _ in c._fields_)
+
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "bench_host_calls")
+        r = subprocess.run([gxx, "-std=c++20", "-O2", "-pthread", "-I", os.path.join(here, "include"),
+                            os.path.join(here, "bench_host_calls.cpp"), "-L", libdir, "-ldsmvc_gb300",
+                            f"-Wl,-rpath,{libdir}", "-o", exe], capture_output=True, text=True)
+        if r.returncode != 0:
+            return {"unavailable": "compiling bench_host_calls.cpp failed: "
+                    + ((r.stderr.strip().splitlines() or ["?"])[-1])[:200]}
+        args = [exe, str(threads), str(steps), str(frames)]
+        args += [req_arg(reqs[k]) for k in ("luma_h", "luma_v", "chroma_h", "chroma_v")]
+        args += [",".join(repr(x) for x in cv) for cv in convs]
+        r = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    try:
+        out = json.loads((r.stdout.strip().splitlines() or ["{}"])[-1])
+    except ValueError:
+        out = {"error": (r.stdout + r.stderr).strip()[-200:]}
+    if "mpix_s" in out:
+        out = {"value": out["mpix_s"], "unit": "Mpix/s", **out,
+               "api": "dsmvc_gb_inverse_2d_u16 per plane from C++ threads (bench_host_calls.cpp)"}
+    return out
+
+
 def main():
     global FRAMES
     ap = argparse.ArgumentParser()
@@ -1197,6 +1239,7 @@ def main():
             e2e_calls = world * args.e2e_steps * pix_step / (time.perf_counter() - t0) / 1e6
     link = link_bandwidth(h2d, d2h) if calls else None
     pageable = pageable_frames(ex, gb, calls, pix_step * world, args.e2e_steps) if calls else None
+    native = native_host_calls(gb, reqs, (luma_conv, chroma_conv), FRAMES) if calls and world == 1 else None
 
     hbm, peak_kind = peaks()
     total_ms = sum(k["milliseconds"] for k in ktimes)
@@ -1227,6 +1270,7 @@ def main():
         "e2e": {"value": e2e, "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "dsmvc_gb_inverse_2d_planes (192 planes in one pinned ring per direction)",
                 "per_plane_calls_16_threads": e2e_calls,
+                "per_plane_calls_16_native_threads": native,
                 "link": link,
                 "link_frac": (((h2d + d2h) / (pix_step / (e2e * 1e6)) / 1e9) / link["concurrent_gbs"])
                 if link and e2e else None,
