@@ -603,7 +603,8 @@ class Executor:
     def inverse_2d_planes(self, planes: Sequence[tuple]) -> None:
         """dsmvc_gb_inverse_2d_planes: [(h, v, input, output[, conversion])]
         with 2D numpy arrays (rows contiguous, same dtype in and out); the
-        planes are pipelined through three streams."""
+        planes are pipelined in groups (uploads, kernels and downloads of
+        successive groups overlap)."""
         self.host_planes(planes).run()
 
     def host_planes(self, planes: Sequence[tuple]) -> "HostPlanes":
