@@ -151,9 +151,11 @@ def test_unprepared_plans_use_the_device_plan_cache(gb):
 
 
 def test_pipelined_host_planes_equal_single_calls(gb):
-    """dsmvc_gb_inverse_2d_planes: many host planes pipelined through three
-    streams in groups (1 MiB groups here, so most planes are in different
-    groups) give exactly the per-plane calls' samples."""
+    """dsmvc_gb_inverse_2d_planes: many host planes pipelined in groups (1 MiB
+    groups here, so most planes are in different groups) give exactly the
+    per-plane calls' samples; a repeated call reuses its groups' compiled
+    launches and device job tables with the same samples, and a call that
+    fails on non-finite Float64 data leaves the next call correct."""
     from conftest import _executor_with
     # Whole vectors (no segments), so that groups and single calls run the
     # same arithmetic.
@@ -173,12 +175,24 @@ def test_pipelined_host_planes_equal_single_calls(gb):
     ex.inverse_2d_planes(planes)
     for (_h, _v, _x, out, _c), w in zip(planes, want):
         assert np.array_equal(out, w)
+    reuses = ex.stats()["compile_reuses"]
+    for _h, _v, _x, out, _c in planes:
+        out[...] = 0
+    ex.inverse_2d_planes(planes)
+    assert ex.stats()["compile_reuses"] > reuses
+    for (_h, _v, _x, out, _c), w in zip(planes, want):
+        assert np.array_equal(out, w)
     # Non-finite data in a Float64 plane fails the call.
     h, v, x, out, _ = planes[2]
     bad = x.copy()
     bad[1, 1] = np.inf
     with pytest.raises(gb.DescaleError):
         ex.inverse_2d_planes(planes[:2] + [(h, v, bad, out)])
+    for _h, _v, _x, out, _c in planes:
+        out[...] = 0
+    ex.inverse_2d_planes(planes)
+    for (_h, _v, _x, out, _c), w in zip(planes, want):
+        assert np.array_equal(out, w)
     ex.close()
 
 
