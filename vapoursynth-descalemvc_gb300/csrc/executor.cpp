@@ -368,9 +368,10 @@ struct Workspace {
     std::vector<char> device_table;   // what ws.jobs holds
 
     // Copies `table` into `dst` through a pinned slot, on `copies` (the
-    // workspace's own stream by default; the caller orders the kernels after
-    // it).  `dst` is not in use by kernels still to run on that stream's
-    // side: the copy follows them in stream order.
+    // workspace's own stream by default; the caller then orders the kernels
+    // after it).  No kernel still to run may read `dst`'s old contents: on
+    // the workspace's stream the copy follows them, and a caller passing a
+    // copy stream has made it wait for them.
     void copy_table(DeviceBuffer &dst, const std::vector<char> &table, cudaStream_t copies) {
         const cudaStream_t s = copies ? copies : stream;
         dst.reserve(table.size());
