@@ -9,6 +9,8 @@
 //   adapter_check gpu     the reference plans run through the adapter class
 //                         (prepared and unprepared) give the GB300 executor's
 //                         own results bit for bit
+//   adapter_check random [N]  N seeded random requests: the reference planner
+//                         and the GB300 planner agree bit for bit (no GPU)
 //   adapter_check blocks  the adapter's registrar in the engine's host block
 //                         registry page-locks a frame-pool block reported
 //                         twice (none with DSMVC_CUDA_DIRECT_IO=0)
@@ -88,9 +90,10 @@ bool same_array(const dsmvc_gb_plan *a, const dsmvc_gb_plan *b, int which) {
     return na == nb && (na == 0 || std::memcmp(pa, pb, na * sizeof(T)) == 0);
 }
 
-void check_plans() {
-    int checked = 0;
-    for (const auto &k : cases()) {
+// The reference planner's plan of `k`, imported, against the GB300 planner's
+// own plan of the same request: scalars, all ten arrays and both plan hashes.
+void compare_plan(const Case &k) {
+    {
         const auto ref = dsmvc::build_axis_plan(k.ref);
         auto *imported = static_cast<dsmvc_gb_plan *>(dsmvc::gb300_detail::Gb300Executor::import_plan(ref));
         dsmvc_gb_plan *own = nullptr;
@@ -120,6 +123,13 @@ void check_plans() {
                "plan hashes " + tag);
         dsmvc_gb_plan_release(imported);
         dsmvc_gb_plan_release(own);
+    }
+}
+
+void check_plans() {
+    int checked = 0;
+    for (const auto &k : cases()) {
+        compare_plan(k);
         ++checked;
     }
     // Invalid plans are refused like AxisPlan::check_valid refuses them.
@@ -300,6 +310,43 @@ void check_blocks() {
     std::printf("blocks ok (%s)\n", installed ? "registrar installed" : "no registrar");
 }
 
+// Seeded random requests (every kernel, border and Float64 mode; shifts,
+// active lengths and blur away from their defaults): the reference planner
+// and the GB300 planner give bit-identical plans, or both refuse the request.
+void check_random_plans(int count, unsigned seed) {
+    std::mt19937 rng(seed);
+    auto uniform = [&](double lo, double hi) { return std::uniform_real_distribution<double>(lo, hi)(rng); };
+    auto pick = [&](int lo, int hi) { return std::uniform_int_distribution<int>(lo, hi)(rng); };
+    const int kinds[] = {DSMVC_GB_BILINEAR, DSMVC_GB_BICUBIC, DSMVC_GB_LANCZOS,
+                         DSMVC_GB_SPLINE16, DSMVC_GB_SPLINE36, DSMVC_GB_SPLINE64};
+    int built = 0, refused = 0;
+    for (int i = 0; i < count; ++i) {
+        const int src = pick(9, 1200), dst = pick(8, src);
+        double active = uniform(0.0, 1.0) < 0.5 ? dst - uniform(0.0, 2.0) : dst;
+        if (active <= 0.0) active = dst;
+        const Case k = make_case(src, dst, active, uniform(-1.0, 1.0), kinds[pick(0, 5)], pick(1, 5),
+                                 uniform(0.0, 0.5), uniform(0.0, 0.6),
+                                 uniform(0.0, 1.0) < 0.6 ? 1.0 : uniform(0.8, 1.6), pick(0, 4), pick(0, 2));
+        bool ref_ok = true;
+        try {
+            (void)dsmvc::build_axis_plan(k.ref);
+        } catch (const std::exception &) {
+            ref_ok = false;
+        }
+        dsmvc_gb_plan *own = nullptr;
+        const bool own_ok = dsmvc_gb_plan_build(&k.own, nullptr, nullptr, &own) == DSMVC_GB_OK;
+        dsmvc_gb_plan_release(own);
+        expect(ref_ok == own_ok, "both planners accept or refuse request " + std::to_string(i));
+        if (ref_ok && own_ok) {
+            compare_plan(k);
+            ++built;
+        } else {
+            ++refused;
+        }
+    }
+    std::printf("random plans ok: %d bit-identical, %d refused by both\n", built, refused);
+}
+
 } // namespace
 
 int main(int argc, char **argv) {
@@ -308,6 +355,7 @@ int main(int argc, char **argv) {
         if (mode == "plans") check_plans();
         else if (mode == "gpu") check_gpu();
         else if (mode == "blocks") check_blocks();
+        else if (mode == "random") check_random_plans(argc > 2 ? std::atoi(argv[2]) : 300, 20261204U);
         else {
             std::printf("unknown mode %s\n", mode.c_str());
             return 2;

@@ -8,8 +8,9 @@ libdsmvc_gb300.so, and runs tests/adapter/adapter_check.cpp:
 
   * CPU: plans built by the reference planner import bit-identical to the
     GB300 planner's plans for the same requests (arrays, scalars, plan
-    hashes); invalid plans are refused like AxisPlan::check_valid refuses
-    them;
+    hashes), for eight fixed requests and 400 seeded random ones (every
+    kernel, border and Float64 mode); invalid plans are refused like
+    AxisPlan::check_valid refuses them;
   * GPU: reference plans run through the adapter, prepared and unprepared,
     Float32, Float64 and u16, give the executor's own results bit for bit;
     the adapter installs the CUDA domain's registrar in the engine's host
@@ -47,8 +48,8 @@ def adapter_check(gb, tmp_path_factory):
     return exe
 
 
-def _run(exe, mode, env=None):
-    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=600,
+def _run(exe, mode, env=None, *args):
+    r = subprocess.run([exe, mode, *args], capture_output=True, text=True, timeout=600,
                        env=None if env is None else {**os.environ, **env})
     sys.stdout.write(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -58,6 +59,11 @@ def _run(exe, mode, env=None):
 def test_reference_plans_import_bit_identical(adapter_check):
     out = _run(adapter_check, "plans")
     assert "plans ok: 8 imported bit-identical" in out
+
+
+def test_random_requests_plan_bit_identical_to_the_reference(adapter_check):
+    out = _run(adapter_check, "random", None, "400")
+    assert "random plans ok:" in out and "FAIL" not in out
 
 
 @pytest.mark.gpu
