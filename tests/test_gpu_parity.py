@@ -141,6 +141,56 @@ def test_2d_random_geometries(gb, executor, whole_executor, paired_executor, hq,
     assert np.abs(goti.astype(np.int64) - wanti.astype(np.int64)).max() <= INT_MAX_CODES
 
 
+def _varied_requests(count, seed):
+    """Seeded 2D requests away from the defaults: shifts, active lengths
+    below the destination size, blur, every built-in kernel family with
+    Lanczos 2 to 5 and Spline64, f64mode automatic or forced."""
+    rng = np.random.default_rng(seed)
+    kernels = [("bilinear", 3, 0, 0.5), ("bicubic", 3, 0, 0.5), ("bicubic", 3, 1 / 3, 1 / 3),
+               ("lanczos", 2, 0, 0.5), ("lanczos", 3, 0, 0.5), ("lanczos", 5, 0, 0.5),
+               ("spline16", 3, 0, 0.5), ("spline36", 3, 0, 0.5), ("spline64", 3, 0, 0.5)]
+    borders = ["zero", "repeat", "reflect101", "symmetric", "mirror"]
+    out = []
+    for i in range(count):
+        k, taps, b, c = kernels[i % len(kernels)]
+        border = borders[int(rng.integers(len(borders)))]
+        mode = (0, 0, 2)[i % 3]
+        axes = []
+        for src in (int(rng.integers(32, 300)), int(rng.integers(24, 200))):
+            dst = max(8, min(src, int(round(src / rng.uniform(1.0, 2.2)))))
+            active = float(dst) if rng.random() < 0.5 else float(dst) - float(rng.uniform(0.0, 1.0))
+            blur = 1.0 if rng.random() < 0.6 else float(rng.uniform(0.9, 1.3))
+            axes.append((src, dst, active, float(rng.uniform(-0.5, 0.5)), k, taps, b, c, blur, border, mode))
+        out.append(tuple(axes))
+    return out
+
+
+REQUESTS_2D = _varied_requests(27, 404)
+
+
+@pytest.mark.parametrize("hq,vq", REQUESTS_2D, ids=[f"r{i}" for i in range(len(REQUESTS_2D))])
+def test_2d_random_requests(gb, executor, hq, vq):
+    """Random requests with shifts, blur and forced Float64: the Float32
+    route within the reference tolerance of the CPU scalar route, the
+    Float64 route within 1 float32 ULP of it, integer output within 1 code."""
+    h, oh = plans(gb, executor, hq)
+    v, ov = plans(gb, executor, vq)
+    x = image(v.source_size, h.source_size, 21)
+    got = executor.inverse_2d(h, v, x)
+    want = O.inverse_2d(oh, ov, x)
+    if h.requires_float64 or v.requires_float64:
+        assert max_ulp(got, want) <= F64_MAX_ULP, (hq, vq)
+    else:
+        err = np.abs(got.astype(np.float64) - want)
+        assert err.max() <= F32_MAX_ABS and err.mean() <= F32_MEAN_ABS, (hq, vq, err.max())
+    for bits, sample in ((8, "u8"), (16, "u16")):
+        xi = make_input(v.source_size, h.source_size, sample, 22)
+        conv = gb.integer_conversion(bits, False, False)
+        goti = executor.inverse_2d(h, v, xi, conv)
+        wanti = O.inverse_2d(oh, ov, xi, conv)
+        assert np.abs(goti.astype(np.int64) - wanti.astype(np.int64)).max() <= INT_MAX_CODES, (hq, vq, sample)
+
+
 @pytest.mark.parametrize("sample", ["u8", "u16"])
 @pytest.mark.parametrize("name,hq,vq", CASES_2D[:3], ids=[c[0] for c in CASES_2D[:3]])
 def test_2d_integer(gb, executor, seq_executor, sample, name, hq, vq):
